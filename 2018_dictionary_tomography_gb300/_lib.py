@@ -1,0 +1,93 @@
+"""ctypes binding of the C ABI in include/gauss_radon.h.
+
+The compute path has no fallback: if the CUDA library cannot be built or
+loaded, or no CUDA device is present, every engine call raises.
+"""
+import ctypes
+import os
+import threading
+
+from . import build_ext
+
+GR_OK = 0
+GR_FIT_NONE, GR_FIT_L2, GR_FIT_KL = 0, 1, 2
+GR_MODE_FIELD, GR_MODE_L2_ATOM, GR_MODE_INNER = 0, 1, 2
+GR_OP_PROJECT, GR_OP_DERIVS_1, GR_OP_DERIVS_2 = 0, 1, 2
+
+
+class GrAtoms(ctypes.Structure):
+    _fields_ = [("n_atoms", ctypes.c_int),
+                ("I", ctypes.c_void_p),
+                ("x", ctypes.c_void_p),
+                ("r", ctypes.c_void_p),
+                ("r_iso", ctypes.c_int)]
+
+
+class GrGeometry(ctypes.Structure):
+    _fields_ = [("kdet", ctypes.c_int),
+                ("n_angles", ctypes.c_int),
+                ("frames", ctypes.c_void_p),
+                ("n_det", ctypes.c_int * 2),
+                ("det", ctypes.c_void_p * 2),
+                ("det_first", ctypes.c_float * 2),
+                ("det_inv_step", ctypes.c_float * 2)]
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
+           "gr_fit_forward", "gr_atom_derivs")
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path():
+    return build_ext.LIB
+
+
+def load(build_if_missing=True):
+    """Load libgauss_radon.so (building it first when allowed)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = build_ext.LIB
+        if build_if_missing:
+            path = build_ext.build()
+        if not os.path.exists(path):
+            raise EngineError("CUDA engine library not built: %s" % path)
+        lib = ctypes.CDLL(path)
+        P = ctypes.POINTER
+        lib.gr_version.restype = ctypes.c_int
+        lib.gr_status_string.restype = ctypes.c_char_p
+        lib.gr_status_string.argtypes = [ctypes.c_int]
+        lib.gr_workspace_bytes.restype = ctypes.c_size_t
+        lib.gr_workspace_bytes.argtypes = [ctypes.c_int, P(GrAtoms), P(GrGeometry)]
+        lib.gr_radproj.restype = ctypes.c_int
+        lib.gr_radproj.argtypes = [P(GrAtoms), P(GrGeometry), ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+        lib.gr_fit_forward.restype = ctypes.c_int
+        lib.gr_fit_forward.argtypes = [P(GrAtoms), P(GrGeometry), ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_float,
+                                       ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_size_t,
+                                       ctypes.c_void_p]
+        lib.gr_atom_derivs.restype = ctypes.c_int
+        lib.gr_atom_derivs.argtypes = [P(GrAtoms), P(GrGeometry), ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_float, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_size_t, ctypes.c_void_p]
+        _lib = lib
+        return lib
+
+
+def check(status, what):
+    if status != GR_OK:
+        msg = load().gr_status_string(int(status)).decode()
+        raise EngineError("%s failed: %s (status %d)" % (what, msg, status))

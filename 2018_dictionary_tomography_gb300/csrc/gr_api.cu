@@ -1,0 +1,132 @@
+// C ABI of the Gaussian-atom Radon engine (declared in include/gauss_radon.h).
+#include "gr_kernels.cuh"
+#include "gauss_radon.h"
+
+namespace {
+
+using namespace gr;
+
+bool to_internal(const gr_atoms *a, const gr_geometry *g, Atoms &at, Geom &ge,
+                 int *status) {
+  *status = GR_ERR_ARG;
+  if (!a || !g) return false;
+  if (g->kdet != 1 && g->kdet != 2) return false;
+  if (a->n_atoms < 0 || g->n_angles < 1 || !g->frames) return false;
+  if (a->n_atoms > 0 && (!a->I || !a->x || !a->r)) return false;
+  for (int k = 0; k < g->kdet; ++k) {
+    if (g->n_det[k] < 1 || !g->det[k]) return false;
+    if (!(g->det_inv_step[k] > 0.f)) {
+      *status = GR_ERR_SHAPE;
+      return false;
+    }
+  }
+  at.n = a->n_atoms;
+  at.I = a->I;
+  at.x = a->x;
+  at.r = a->r;
+  at.r_iso = a->r_iso ? 1 : 0;
+  ge.K = g->kdet;
+  ge.n_angles = g->n_angles;
+  ge.frames = g->frames;
+  for (int k = 0; k < kMaxK; ++k) {
+    const bool use = k < g->kdet;
+    ge.ax[k].coords = use ? g->det[k] : nullptr;
+    ge.ax[k].n = use ? g->n_det[k] : 1;
+    ge.ax[k].first = use ? g->det_first[k] : 0.f;
+    ge.ax[k].inv_step = use ? g->det_inv_step[k] : 1.f;
+  }
+  *status = GR_OK;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gr_version(void) { return 10000; }
+
+const char *gr_status_string(int status) {
+  switch (status) {
+    case GR_OK: return "ok";
+    case GR_ERR_ARG: return "invalid argument";
+    case GR_ERR_WORKSPACE: return "workspace missing or too small";
+    case GR_ERR_LAUNCH: return "CUDA launch or runtime error";
+    case GR_ERR_SHAPE: return "unsupported geometry";
+    default: return "unknown status";
+  }
+}
+
+size_t gr_workspace_bytes(int op, const gr_atoms *atoms, const gr_geometry *geom) {
+  Atoms at;
+  Geom g;
+  int st;
+  if (!to_internal(atoms, geom, at, g, &st)) return 0;
+  const int D1 = g.K == 2 ? g.ax[1].n : 1;
+  if (op == GR_OP_PROJECT)
+    return project_workspace_bytes(g.K, at.n, g.n_angles, g.ax[0].n, D1);
+  if (op == GR_OP_DERIVS_1 || op == GR_OP_DERIVS_2)
+    return derivs_workspace_bytes(g.K, at.n, g.n_angles, op == GR_OP_DERIVS_1 ? 1 : 2);
+  return 0;
+}
+
+int gr_radproj(const gr_atoms *atoms, const gr_geometry *geom, float *R,
+               void *workspace, size_t workspace_bytes, void *stream) {
+  Atoms at;
+  Geom g;
+  int st;
+  if (!to_internal(atoms, geom, at, g, &st)) return st;
+  if (!R) return GR_ERR_ARG;
+  ProjOut o{};
+  o.R = R;
+  o.epilogue = kEpiNone;
+  return launch_project(at, g, o, nullptr, workspace, workspace_bytes,
+                        static_cast<cudaStream_t>(stream));
+}
+
+int gr_fit_forward(const gr_atoms *atoms, const gr_geometry *geom, int fit,
+                   const float *data, float background, float *R, float *alpha,
+                   float *beta, double *loss, void *workspace,
+                   size_t workspace_bytes, void *stream) {
+  Atoms at;
+  Geom g;
+  int st;
+  if (!to_internal(atoms, geom, at, g, &st)) return st;
+  if (fit != GR_FIT_NONE && fit != GR_FIT_L2 && fit != GR_FIT_KL) return GR_ERR_ARG;
+  if (fit != GR_FIT_NONE && !data) return GR_ERR_ARG;
+  if (fit == GR_FIT_KL && !(background > 0.f)) return GR_ERR_ARG;
+  if (fit == GR_FIT_NONE && (!R || loss)) return GR_ERR_ARG;
+  ProjOut o{};
+  o.R = R;
+  o.epilogue = fit == GR_FIT_L2 ? kEpiL2 : fit == GR_FIT_KL ? kEpiKL : kEpiNone;
+  o.data = data;
+  o.bg = background;
+  o.alpha = alpha;
+  o.beta = beta;
+  return launch_project(at, g, o, loss, workspace, workspace_bytes,
+                        static_cast<cudaStream_t>(stream));
+}
+
+int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
+                   const float *field, const float *beta_field, float beta_const,
+                   int order, double *f, double *g_out, double *H, void *workspace,
+                   size_t workspace_bytes, void *stream) {
+  Atoms at;
+  Geom g;
+  int st;
+  if (!to_internal(atoms, geom, at, g, &st)) return st;
+  if (mode != GR_MODE_FIELD && mode != GR_MODE_L2_ATOM && mode != GR_MODE_INNER)
+    return GR_ERR_ARG;
+  if (order != 1 && order != 2) return GR_ERR_ARG;
+  if (!field || !f || !g_out || (order == 2 && !H)) return GR_ERR_ARG;
+  DerivIn in{};
+  in.mode = mode;
+  in.order = order;
+  in.alpha = field;
+  in.beta = mode == GR_MODE_FIELD ? beta_field : nullptr;
+  in.beta_const = mode == GR_MODE_FIELD ? beta_const : (mode == GR_MODE_L2_ATOM ? 1.f : 0.f);
+  DerivOut out{f, g_out, H};
+  return launch_derivs(at, g, in, out, workspace, workspace_bytes,
+                       static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

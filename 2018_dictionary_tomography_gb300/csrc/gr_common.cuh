@@ -1,0 +1,309 @@
+// Shared device helpers for the Gaussian-atom Radon kernels (sm_103a).
+//
+// Model (reference GaussDictCode/bin/NewtonBases2D.py:39-72 and
+// GaussDictCode/bin/NewtonBases.py:262-310): an atom (I, x, r) projects to
+//     R(y) = I / |r T| * exp(-30 m),   m = |(1 - t t^T) r (y - x)|^2,
+//     t = r T / |r T|,   R = 0 where m > 1,
+// for detector points y = sum_i q_i w_i.  With the frame B = [w_0 .. w_{K-1}, T]
+// and K_c = r B_c, Q = K^T K, the projection of the atom is the Gaussian
+//     m(q) = (q - q*)^T G (q - q*),  G = Q_ww - Q_wT Q_wT^T / Q_TT,
+//     q* = (B^{-1} x)[0:K],          1/|r T| = Q_TT^{-1/2},
+// i.e. a K-dimensional Gaussian whose precision is the Schur complement of
+// the atom precision in the frame.  Per (atom, angle) "pair" the kernels
+// compute G, q*, the amplitude and the support box once, and per detector
+// cell only the quadratic form and one exp2.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gr {
+
+constexpr int kMaxK = 2;                          // detector dimensions
+constexpr float kNegThirtyLog2e = -43.28085122666891f;  // -30 / ln 2
+constexpr int kFrameStride2D = 8;   // T(2) w0(2) wt0(2) pad(2)
+constexpr int kFrameStride3D = 16;  // T(3) w0(3) w1(3) wt0(3) wt1(3) pad(1)
+
+// Error codes shared with the C ABI.
+enum Status : int {
+  kOk = 0,
+  kErrArg = -1,
+  kErrWorkspace = -2,
+  kErrLaunch = -3,
+  kErrShape = -4,
+};
+
+__device__ __forceinline__ float ex2_approx(float v) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(v));
+  return y;
+}
+
+__device__ __forceinline__ float lg2_approx(float v) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(v));
+  return y;
+}
+
+// Error-free transforms (Knuth TwoSum, FMA TwoProduct) used for the
+// compensated projection centre and compensated accumulators.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+  p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+}
+
+// Compensated dot product of length n <= 3 (Ogita-Rump-Oishi Dot2): the
+// result hi + lo carries roughly twice the working precision.
+template <int N>
+__device__ __forceinline__ void dot2(const float *a, const float *b, float &hi,
+                                     float &lo) {
+  float s, c;
+  two_prod(a[0], b[0], s, c);
+#pragma unroll
+  for (int i = 1; i < N; ++i) {
+    float p, pe, t, te;
+    two_prod(a[i], b[i], p, pe);
+    two_sum(s, p, t, te);
+    s = t;
+    c += pe + te;
+  }
+  two_sum(s, c, hi, lo);
+}
+
+// Kahan-style compensated accumulator (Neumaier variant, exact when |v|>|s|).
+struct CAcc {
+  float s, c;
+  __device__ __forceinline__ void zero() { s = 0.f; c = 0.f; }
+  __device__ __forceinline__ void add(float v) {
+    float t = s + v;
+    c += (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
+    s = t;
+  }
+  __device__ __forceinline__ float get() const { return s + c; }
+};
+
+// Uniform detector grid: the coordinate of cell k is coords[k]; first and
+// inverse step locate the support box, the stored coordinates are what the
+// cell values use.
+struct DetAxis {
+  const float *coords;
+  int n;
+  float first;
+  float inv_step;
+};
+
+// Geometry of one problem in device memory.
+struct Geom {
+  int K;                 // 1: 2D sinogram (A, D0); 2: 3D / 2.5D (A, D0, D1)
+  int n_angles;
+  const float *frames;   // n_angles x stride, see kFrameStride*
+  DetAxis ax[kMaxK];
+};
+
+// Atoms in device memory: r is packed upper-triangular (2D: r00 r11 r01;
+// 3D: r00 r11 r22 r01 r12 r02) or, when r_iso, one radius per atom.
+struct Atoms {
+  int n;
+  const float *I;
+  const float *x;
+  const float *r;
+  int r_iso;
+};
+
+template <int K>
+struct Frame {
+  float T[K + 1];
+  float w[K][K + 1];
+  float wt[K][K + 1];  // rows 0..K-1 of B^{-1}
+};
+
+template <int K>
+__device__ __forceinline__ void load_frame(const float *frames, int a,
+                                           Frame<K> &f) {
+  constexpr int D = K + 1;
+  const float *p = frames + (size_t)a * (K == 1 ? kFrameStride2D : kFrameStride3D);
+#pragma unroll
+  for (int i = 0; i < D; ++i) f.T[i] = p[i];
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int i = 0; i < D; ++i) f.w[k][i] = p[D * (1 + k) + i];
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int i = 0; i < D; ++i) f.wt[k][i] = p[D * (1 + K + k) + i];
+}
+
+// Upper-triangular r as a dense (K+1)x(K+1) matrix.
+template <int K>
+__device__ __forceinline__ void load_r(const Atoms &at, int j,
+                                       float (&M)[K + 1][K + 1]) {
+  constexpr int D = K + 1;
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+#pragma unroll
+    for (int b = 0; b < D; ++b) M[a][b] = 0.f;
+  if (at.r_iso) {
+    float s = at.r[j];
+#pragma unroll
+    for (int a = 0; a < D; ++a) M[a][a] = s;
+  } else if constexpr (K == 1) {
+    const float *r = at.r + 3 * (size_t)j;
+    M[0][0] = r[0];
+    M[1][1] = r[1];
+    M[0][1] = r[2];
+  } else {
+    const float *r = at.r + 6 * (size_t)j;
+    M[0][0] = r[0];
+    M[1][1] = r[1];
+    M[2][2] = r[2];
+    M[0][1] = r[3];
+    M[1][2] = r[4];
+    M[0][2] = r[5];
+  }
+}
+
+// Packed r index p -> (row, col).
+template <int K>
+__host__ __device__ constexpr int rrow(int p) {
+  return K == 1 ? (p == 0 ? 0 : p == 1 ? 1 : 0)
+                : (p == 0 ? 0 : p == 1 ? 1 : p == 2 ? 2 : p == 3 ? 0 : p == 4 ? 1 : 0);
+}
+template <int K>
+__host__ __device__ constexpr int rcol(int p) {
+  return K == 1 ? (p == 0 ? 0 : p == 1 ? 1 : 1)
+                : (p == 0 ? 0 : p == 1 ? 1 : p == 2 ? 2 : p == 3 ? 1 : p == 4 ? 2 : 2);
+}
+template <int K>
+__host__ __device__ constexpr int n_rparam() { return K == 1 ? 3 : 6; }
+
+// Per (atom, angle) projection data.
+template <int K>
+struct Pair {
+  float qh[K], ql[K];  // projection centre q* = hi + lo
+  float G[3];          // G00, G01, G11 (K == 1: G00)
+  float n;             // 1 / |r T|
+  float l2amp;         // log2(I n)
+  int lo[K], hi[K];    // inclusive support box in cell indices (empty: lo > hi)
+  // quantities kept for the derivative assembly
+  float Kc[K + 1][K + 1];  // Kc[c][a] = (r B_c)_a, c = 0..K-1 detector axes, K = T
+  float Q[K + 1][K + 1];   // Q[c][d] = Kc[c] . Kc[d]
+};
+
+template <int K>
+__device__ __forceinline__ bool pair_setup(const Atoms &at, int j,
+                                           const Frame<K> &f, const Geom &g,
+                                           Pair<K> &p) {
+  constexpr int D = K + 1;
+  float M[D][D];
+  load_r<K>(at, j, M);
+  // K_c = r B_c for the detector axes and the ray direction
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const float *B = (c < K) ? f.w[c] : f.T;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      float s = 0.f;
+#pragma unroll
+      for (int b = a; b < D; ++b) s = fmaf(M[a][b], B[b], s);
+      p.Kc[c][a] = s;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < D; ++c)
+#pragma unroll
+    for (int d = c; d < D; ++d) {
+      float s = 0.f;
+#pragma unroll
+      for (int a = 0; a < D; ++a) s = fmaf(p.Kc[c][a], p.Kc[d][a], s);
+      p.Q[c][d] = s;
+      p.Q[d][c] = s;
+    }
+  const float qtt = p.Q[K][K];
+  const float iqtt = 1.f / qtt;
+  p.n = rsqrtf(qtt);
+  // G = U^T U with U_i = K_i - t (t . K_i), t = K_T / |K_T| (the projected
+  // detector axes); this Gram form stays positive semi-definite in FP32.
+  float U[K][D];
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    const float c = p.Q[i][K] * iqtt;
+#pragma unroll
+    for (int a = 0; a < D; ++a) U[i][a] = fmaf(-c, p.Kc[K][a], p.Kc[i][a]);
+  }
+  if constexpr (K == 1) {
+    p.G[0] = U[0][0] * U[0][0] + U[0][1] * U[0][1];
+    p.G[1] = 0.f;
+    p.G[2] = 0.f;
+  } else {
+    float g00 = 0.f, g01 = 0.f, g11 = 0.f;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      g00 = fmaf(U[0][a], U[0][a], g00);
+      g01 = fmaf(U[0][a], U[1][a], g01);
+      g11 = fmaf(U[1][a], U[1][a], g11);
+    }
+    p.G[0] = g00;
+    p.G[1] = g01;
+    p.G[2] = g11;
+  }
+  const float I = at.I[j];
+  p.l2amp = lg2_approx(I * p.n);
+  float xv[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) xv[a] = at.x[(size_t)D * j + a];
+#pragma unroll
+  for (int k = 0; k < K; ++k) dot2<D>(f.wt[k], xv, p.qh[k], p.ql[k]);
+
+  // support box of m <= 1: |d_i| <= sqrt((G^{-1})_ii)
+  float hw[K];
+  bool ok;
+  if constexpr (K == 1) {
+    ok = p.G[0] > 0.f && qtt > 0.f;
+    hw[0] = rsqrtf(p.G[0]);
+  } else {
+    float det = p.G[0] * p.G[2] - p.G[1] * p.G[1];
+    ok = p.G[0] > 0.f && det > 0.f && qtt > 0.f;
+    float idet = 1.f / det;
+    hw[0] = sqrtf(p.G[2] * idet);
+    hw[1] = sqrtf(p.G[0] * idet);
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const DetAxis &ax = g.ax[k];
+    // coordinates increase with the cell index (checked on the host)
+    float c = (p.qh[k] - ax.first) * ax.inv_step;
+    float h = hw[k] * ax.inv_step * 1.0001f + 1e-3f;
+    float lo = ceilf(c - h), hi = floorf(c + h);
+    bool fin = ok && (lo == lo) && (hi == hi) && fabsf(c) < 1e8f && h < 1e8f;
+    p.lo[k] = fin ? max(0, (int)lo) : 1;
+    p.hi[k] = fin ? min(ax.n - 1, (int)hi) : 0;
+  }
+  return ok;
+}
+
+// Squared Mahalanobis distance of cell offsets d from the centre.
+template <int K>
+__device__ __forceinline__ float quad(const Pair<K> &p, const float *d) {
+  if constexpr (K == 1) return p.G[0] * d[0] * d[0];
+  else return fmaf(d[0], fmaf(p.G[0], d[0], 2.f * p.G[1] * d[1]), p.G[2] * d[1] * d[1]);
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace gr

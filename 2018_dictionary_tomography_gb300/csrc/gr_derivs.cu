@@ -1,0 +1,687 @@
+// Per-atom derivatives of data fits (sm_103a).
+//
+// Replaces the reference's one-atom-per-launch kernels
+// __L2derivs_RadProj_aniso (GaussDictCode/bin/NewtonBases2D.py:331-401),
+// __derivs_RadProj_aniso (NewtonBases2D.py:446-515) and their 3D twins
+// (GaussDictCode/bin/NewtonBases.py:794-870, :995-1069), which evaluate a
+// 6x6 / 10x10 per-cell Hessian of one atom at every detector cell.
+//
+// For one (atom, angle) pair the projection is R(q) = I E(q),
+// E = n exp(-30 (q - q*)^T G (q - q*)) (see gr_common.cuh), so
+//   ln E = ln n - 30 d^T G d,   d = q - q*,
+// is linear in psi = (ln n, G, q*) up to the quadratic dependence on q*.
+// Every derivative sum over cells of a weight field w times a polynomial in d
+// is therefore a combination of a few cell moments  M_ij = sum w d0^i d1^j
+// (degree <= 2 for gradients, <= 4 for Hessians), and the chain rule from psi
+// to (I, x, r) is done once per pair:
+//   psi -> Q = (r B)^T (r B) -> r   and   q* = (B^{-1} x)[0:K].
+// Per cell the kernel evaluates one exp2 and a handful of FMAs; moments are
+// accumulated per detector row and folded with powers of d0 at row end.
+//
+// Work layout: lane = atom, a warp holds 32 atoms (or fewer atoms with the
+// angles of each atom split over several lanes), and loops over a chunk of
+// angles.  Gradients are accumulated per lane with compensated FP32 sums,
+// Hessians in FP32; lanes sharing an atom are combined by a fixed-order
+// butterfly; chunk partials are summed in FP64 in chunk order by
+// gr_deriv_finalize_kernel, which also applies the isotropic chain rule.
+// No float atomics anywhere: results are bitwise reproducible.
+#include "gr_kernels.cuh"
+
+namespace gr {
+
+template <int K>
+__host__ __device__ constexpr int n_psi() { return 1 + K * (K + 1) / 2 + K; }
+template <int K>
+__host__ __device__ constexpr int n_par() { return 1 + (K + 1) + n_rparam<K>(); }  // I, x, r
+template <int K, int DEG>
+__host__ __device__ constexpr int n_mom() { return K == 1 ? DEG + 1 : (DEG + 1) * (DEG + 2) / 2; }
+// monomial d0^i d1^j -> moment slot (ordered by total degree)
+__host__ __device__ constexpr int mi(int i, int j) {
+  return (i + j) * (i + j + 1) / 2 + j;
+}
+
+struct DerivCfg {
+  int ag;       // distinct atoms per warp (power of two)
+  int sg;       // lanes per atom (32 / ag)
+  int ch;       // angles per chunk
+  int nchunks;
+  int qn;       // partial values per atom
+};
+
+inline int next_pow2(int v) {
+  int p = 1;
+  while (p < v && p < 32) p <<= 1;
+  return p;
+}
+
+inline DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order) {
+  DerivCfg c;
+  c.ag = next_pow2(n_atoms < 1 ? 1 : n_atoms);
+  c.sg = 32 / c.ag;
+  const int warps_atoms = (n_atoms + c.ag - 1) / c.ag;
+  int nch = (8192 + warps_atoms - 1) / warps_atoms;
+  const int max_ch = (n_angles + c.sg - 1) / c.sg;
+  if (nch > max_ch) nch = max_ch;
+  if (nch < 1) nch = 1;
+  c.ch = (n_angles + nch - 1) / nch;
+  if (c.ch < 1) c.ch = 1;
+  c.nchunks = (n_angles + c.ch - 1) / c.ch;
+  const int P = 1 + (K + 1) + (K == 1 ? 3 : 6);
+  c.qn = 1 + P + (order > 1 ? P * (P + 1) / 2 : 0);
+  return c;
+}
+
+// Cell moments of one pair.
+template <int K, int DEG, bool GN>
+struct PairMoments {
+  float Ma[n_mom<K, DEG>()];
+  float Mb[GN ? n_mom<K, DEG>() : 1];
+  float X0, Y0;  // sum E*C and sum E^2 (per-atom L2 value)
+};
+
+template <int K, int DEG, bool GN>
+__device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
+                                             const DerivIn &in, int a, float I,
+                                             PairMoments<K, DEG, GN> &mo) {
+  constexpr int NM = n_mom<K, DEG>();
+#pragma unroll
+  for (int i = 0; i < NM; ++i) {
+    mo.Ma[i] = 0.f;
+    if (GN) mo.Mb[i] = 0.f;
+  }
+  mo.X0 = 0.f;
+  mo.Y0 = 0.f;
+  if (p.lo[0] > p.hi[0]) return;
+  if constexpr (K == 2)
+    if (p.lo[1] > p.hi[1]) return;
+  const float l2n = lg2_approx(p.n);
+  const int D0 = g.ax[0].n;
+  const int D1 = K == 2 ? g.ax[1].n : 1;
+  const float *__restrict__ field = in.alpha;
+  const float *__restrict__ bfield = in.beta;
+  const size_t abase = (size_t)a * D0 * D1;
+  for (int k0 = p.lo[0]; k0 <= p.hi[0]; ++k0) {
+    const float d0 = (__ldg(g.ax[0].coords + k0) - p.qh[0]) - p.ql[0];
+    if constexpr (K == 1) {
+      const float m = p.G[0] * d0 * d0;
+      if (m <= 1.f) {
+        const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
+        const float c = __ldg(field + abase + k0);
+        const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
+        float w = al * E;
+#pragma unroll
+        for (int q = 0; q < NM; ++q) {
+          mo.Ma[q] += w;
+          w *= d0;
+        }
+        if (GN) {
+          const float be = bfield ? __ldg(bfield + abase + k0) : in.beta_const;
+          float wb = be * E * E;
+#pragma unroll
+          for (int q = 0; q < NM; ++q) {
+            mo.Mb[q] += wb;
+            wb *= d0;
+          }
+        }
+        if (in.mode == kModeL2Atom) {
+          mo.X0 = fmaf(E, c, mo.X0);
+          mo.Y0 = fmaf(E, E, mo.Y0);
+        }
+      }
+    } else {
+      const float t0 = p.G[0] * d0 * d0;
+      const float u = 2.f * p.G[1] * d0;
+      float Sa[DEG + 1], Sb[GN ? DEG + 1 : 1];
+#pragma unroll
+      for (int q = 0; q <= DEG; ++q) {
+        Sa[q] = 0.f;
+        if (GN) Sb[q] = 0.f;
+      }
+      const size_t rbase = abase + (size_t)k0 * D1;
+      for (int k1 = p.lo[1]; k1 <= p.hi[1]; ++k1) {
+        const float d1 = (__ldg(g.ax[1].coords + k1) - p.qh[1]) - p.ql[1];
+        const float m = fmaf(d1, fmaf(p.G[2], d1, u), t0);
+        if (m <= 1.f) {
+          const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
+          const float c = __ldg(field + rbase + k1);
+          const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
+          float w = al * E;
+#pragma unroll
+          for (int q = 0; q <= DEG; ++q) {
+            Sa[q] += w;
+            w *= d1;
+          }
+          if (GN) {
+            const float be = bfield ? __ldg(bfield + rbase + k1) : in.beta_const;
+            float wb = be * E * E;
+#pragma unroll
+            for (int q = 0; q <= DEG; ++q) {
+              Sb[q] += wb;
+              wb *= d1;
+            }
+          }
+          if (in.mode == kModeL2Atom) {
+            mo.X0 = fmaf(E, c, mo.X0);
+            mo.Y0 = fmaf(E, E, mo.Y0);
+          }
+        }
+      }
+      float pw = 1.f;
+#pragma unroll
+      for (int i = 0; i <= DEG; ++i) {
+#pragma unroll
+        for (int j = 0; j <= DEG - i; ++j) {
+          mo.Ma[mi(i, j)] = fmaf(pw, Sa[j], mo.Ma[mi(i, j)]);
+          if (GN) mo.Mb[mi(i, j)] = fmaf(pw, Sb[j], mo.Mb[mi(i, j)]);
+        }
+        pw *= d0;
+      }
+    }
+  }
+}
+
+// Basis vector c of the frame: detector axes 0..K-1, then the ray direction.
+template <int K>
+__device__ __forceinline__ float basis(const Frame<K> &f, int c, int b) {
+  return c < K ? f.w[c][b] : f.T[b];
+}
+
+// A_psi = sum w dl/dpsi from moments (psi order: ln n, G params, q*).
+template <int K, int NM>
+__device__ __forceinline__ void first_psi(const float *M, const float *G,
+                                          float *A) {
+  A[0] = M[0];
+  if constexpr (K == 1) {
+    A[1] = -30.f * M[2];
+    A[2] = 60.f * G[0] * M[1];
+  } else {
+    A[1] = -30.f * M[mi(2, 0)];
+    A[2] = -60.f * M[mi(1, 1)];
+    A[3] = -30.f * M[mi(0, 2)];
+    A[4] = 60.f * (G[0] * M[mi(1, 0)] + G[1] * M[mi(0, 1)]);
+    A[5] = 60.f * (G[1] * M[mi(1, 0)] + G[2] * M[mi(0, 1)]);
+  }
+}
+
+// Gradient of sum_psi A_psi psi with respect to (x, r), times scale:
+// x part through q* = B^{-1} x, r part through Q = (rB)^T(rB) via the
+// adjoint Abar of psi(Q): d/dr_(ab) = 2 (Kc^T Abar B^T)_ab.
+template <int K>
+__device__ __forceinline__ void psi_grad(const Pair<K> &p, const Frame<K> &f,
+                                         const float *A, float *gx, float *gr) {
+  constexpr int D = K + 1;
+  constexpr int NG = K * (K + 1) / 2;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < K; ++i) s = fmaf(A[1 + NG + i], f.wt[i][c], s);
+    gx[c] = s;
+  }
+  const float iq = 1.f / p.Q[K][K];
+  float Ah[K][K];
+  if constexpr (K == 1) {
+    Ah[0][0] = A[1];
+  } else {
+    Ah[0][0] = A[1];
+    Ah[0][1] = 0.5f * A[2];
+    Ah[1][0] = 0.5f * A[2];
+    Ah[1][1] = A[3];
+  }
+  float Ab[D][D];
+  float hAh = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      Ab[i][j] = Ah[i][j];
+      s = fmaf(Ah[i][j], p.Q[j][K], s);
+    }
+    Ab[i][K] = -s * iq;
+    Ab[K][i] = -s * iq;
+    hAh = fmaf(p.Q[i][K], s, hAh);
+  }
+  Ab[K][K] = hAh * iq * iq - 0.5f * A[0] * iq;
+  // Y = Abar B^T, X = Kc^T Y
+  float Y[D][D];
+#pragma unroll
+  for (int d = 0; d < D; ++d)
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      float s = 0.f;
+#pragma unroll
+      for (int c = 0; c < D; ++c) s = fmaf(Ab[d][c], basis<K>(f, c, b), s);
+      Y[d][b] = s;
+    }
+#pragma unroll
+  for (int q = 0; q < n_rparam<K>(); ++q) {
+    const int a = rrow<K>(q), b = rcol<K>(q);
+    float s = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) s = fmaf(p.Kc[d][a], Y[d][b], s);
+    gr[q] = 2.f * s;
+  }
+}
+
+// psi-space Gram matrix of the cell weights:
+// out[k][l] = sum w dl/dpsi_k dl/dpsi_l (+ sum w d2l/dpsi_k dpsi_l if WITH_C).
+template <int K, bool WITH_C>
+__device__ __forceinline__ void psi_gram(const float *M, const float *G,
+                                         float (&B)[n_psi<K>()][n_psi<K>()]) {
+  if constexpr (K == 1) {
+    const float g = G[0];
+    B[0][0] = M[0];
+    B[0][1] = -30.f * M[2];
+    B[0][2] = 60.f * g * M[1];
+    B[1][1] = 900.f * M[4];
+    B[1][2] = -1800.f * g * M[3];
+    B[2][2] = 3600.f * g * g * M[2];
+    if (WITH_C) {
+      B[2][2] += -60.f * g * M[0];
+      B[1][2] += 60.f * M[1];
+    }
+  } else {
+    const float g0 = G[0], g1 = G[1], g2 = G[2];
+    B[0][0] = M[mi(0, 0)];
+    B[0][1] = -30.f * M[mi(2, 0)];
+    B[0][2] = -60.f * M[mi(1, 1)];
+    B[0][3] = -30.f * M[mi(0, 2)];
+    B[0][4] = 60.f * (g0 * M[mi(1, 0)] + g1 * M[mi(0, 1)]);
+    B[0][5] = 60.f * (g1 * M[mi(1, 0)] + g2 * M[mi(0, 1)]);
+    B[1][1] = 900.f * M[mi(4, 0)];
+    B[1][2] = 1800.f * M[mi(3, 1)];
+    B[1][3] = 900.f * M[mi(2, 2)];
+    B[1][4] = -1800.f * (g0 * M[mi(3, 0)] + g1 * M[mi(2, 1)]);
+    B[1][5] = -1800.f * (g1 * M[mi(3, 0)] + g2 * M[mi(2, 1)]);
+    B[2][2] = 3600.f * M[mi(2, 2)];
+    B[2][3] = 1800.f * M[mi(1, 3)];
+    B[2][4] = -3600.f * (g0 * M[mi(2, 1)] + g1 * M[mi(1, 2)]);
+    B[2][5] = -3600.f * (g1 * M[mi(2, 1)] + g2 * M[mi(1, 2)]);
+    B[3][3] = 900.f * M[mi(0, 4)];
+    B[3][4] = -1800.f * (g0 * M[mi(1, 2)] + g1 * M[mi(0, 3)]);
+    B[3][5] = -1800.f * (g1 * M[mi(1, 2)] + g2 * M[mi(0, 3)]);
+    B[4][4] = 3600.f * (g0 * g0 * M[mi(2, 0)] + 2.f * g0 * g1 * M[mi(1, 1)] +
+                        g1 * g1 * M[mi(0, 2)]);
+    B[4][5] = 3600.f * (g0 * g1 * M[mi(2, 0)] + (g0 * g2 + g1 * g1) * M[mi(1, 1)] +
+                        g1 * g2 * M[mi(0, 2)]);
+    B[5][5] = 3600.f * (g1 * g1 * M[mi(2, 0)] + 2.f * g1 * g2 * M[mi(1, 1)] +
+                        g2 * g2 * M[mi(0, 2)]);
+    if (WITH_C) {
+      B[4][4] += -60.f * g0 * M[0];
+      B[4][5] += -60.f * g1 * M[0];
+      B[5][5] += -60.f * g2 * M[0];
+      B[1][4] += 60.f * M[mi(1, 0)];
+      B[2][4] += 60.f * M[mi(0, 1)];
+      B[2][5] += 60.f * M[mi(1, 0)];
+      B[3][5] += 60.f * M[mi(0, 1)];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < n_psi<K>(); ++i)
+#pragma unroll
+    for (int j = 0; j < i; ++j) B[i][j] = B[j][i];
+}
+
+// Jacobian of (ln n, G params) with respect to r, and
+// sum_psi A_psi d2 psi / dr dr (Hr, packed upper triangle).
+template <int K>
+__device__ __forceinline__ void psi_r_derivs(
+    const Pair<K> &p, const Frame<K> &f, const float *A,
+    float (&Jr)[1 + K * (K + 1) / 2][n_rparam<K>()],
+    float (&Hr)[n_rparam<K>() * (n_rparam<K>() + 1) / 2]) {
+  constexpr int D = K + 1;
+  constexpr int PR = n_rparam<K>();
+  constexpr int NG = K * (K + 1) / 2;
+  const float w = p.Q[K][K], iq = 1.f / w;
+  // dQ_cd / dr_p for the entries used: (i,j) detector pairs, (i,T), (T,T)
+  auto dQ = [&](int c, int d, int q) -> float {
+    const int a = rrow<K>(q), b = rcol<K>(q);
+    return basis<K>(f, c, b) * p.Kc[d][a] + basis<K>(f, d, b) * p.Kc[c][a];
+  };
+  auto ddQ = [&](int c, int d, int q, int s) -> float {
+    if (rrow<K>(q) != rrow<K>(s)) return 0.f;
+    const int b = rcol<K>(q), b2 = rcol<K>(s);
+    return basis<K>(f, c, b) * basis<K>(f, d, b2) + basis<K>(f, d, b) * basis<K>(f, c, b2);
+  };
+  float wp[PR];
+#pragma unroll
+  for (int q = 0; q < PR; ++q) {
+    wp[q] = dQ(K, K, q);
+    Jr[0][q] = -0.5f * wp[q] * iq;
+  }
+  // G params in order (0,0), (0,1), (1,1) for K = 2
+  int gi[NG], gj[NG];
+  if constexpr (K == 1) {
+    gi[0] = 0; gj[0] = 0;
+  } else {
+    gi[0] = 0; gj[0] = 0;
+    gi[1] = 0; gj[1] = 1;
+    gi[2] = 1; gj[2] = 1;
+  }
+#pragma unroll
+  for (int k = 0; k < NG; ++k) {
+    const int i = gi[k], j = gj[k];
+    const float u = p.Q[i][K], v = p.Q[j][K];
+#pragma unroll
+    for (int q = 0; q < PR; ++q) {
+      const float up = dQ(i, K, q), vp = dQ(j, K, q);
+      Jr[1 + k][q] = dQ(i, j, q) - (up * v + u * vp) * iq + u * v * wp[q] * iq * iq;
+    }
+  }
+  int o = 0;
+#pragma unroll
+  for (int q = 0; q < PR; ++q)
+#pragma unroll
+    for (int s = q; s < PR; ++s, ++o) {
+      const float wpq = ddQ(K, K, q, s);
+      float h = A[0] * (-0.5f) * (wpq * iq - wp[q] * wp[s] * iq * iq);
+#pragma unroll
+      for (int k = 0; k < NG; ++k) {
+        const int i = gi[k], j = gj[k];
+        const float u = p.Q[i][K], v = p.Q[j][K];
+        const float up = dQ(i, K, q), us = dQ(i, K, s);
+        const float vp = dQ(j, K, q), vs = dQ(j, K, s);
+        const float ups = ddQ(i, K, q, s), vps = ddQ(j, K, q, s);
+        const float fqs = (ups * v + up * vs + us * vp + u * vps) * iq -
+                          (up * v + u * vp) * wp[s] * iq * iq -
+                          (us * v + u * vs) * wp[q] * iq * iq -
+                          u * v * wpq * iq * iq +
+                          2.f * u * v * wp[q] * wp[s] * iq * iq * iq;
+        h += A[1 + k] * (ddQ(i, j, q, s) - fqs);
+      }
+      Hr[o] = h;
+    }
+}
+
+template <int K, int ORDER>
+__global__ void __launch_bounds__(128)
+    gr_deriv_kernel(Atoms at, Geom g, DerivIn in, DerivCfg cfg, float *part) {
+  constexpr int D = K + 1;
+  constexpr int PR = n_rparam<K>();
+  constexpr int P = n_par<K>();
+  constexpr int NPSI = n_psi<K>();
+  constexpr int NG = K * (K + 1) / 2;
+  constexpr int DEG = ORDER == 1 ? 2 : 4;
+  constexpr int NH = P * (P + 1) / 2;
+  constexpr bool GN = ORDER > 1;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int warps_atoms = (at.n + cfg.ag - 1) / cfg.ag;
+  if (gw >= warps_atoms * cfg.nchunks) return;
+  const int chunk = gw / warps_atoms, wa = gw - chunk * warps_atoms;
+  const int j = wa * cfg.ag + (lane % cfg.ag);
+  const int sub = lane / cfg.ag;
+  const bool valid = j < at.n;
+  const int jj = valid ? j : 0;
+  const float I = at.I[jj];
+  const int a_lo = chunk * cfg.ch;
+  const int a_hi = min(g.n_angles, a_lo + cfg.ch);
+
+  float f = 0.f;
+  CAcc gacc[P];
+  float hacc[ORDER > 1 ? NH : 1];
+#pragma unroll
+  for (int i = 0; i < P; ++i) gacc[i].zero();
+#pragma unroll
+  for (int i = 0; i < (ORDER > 1 ? NH : 1); ++i) hacc[i] = 0.f;
+
+  for (int a = a_lo + sub; a < a_hi && valid; a += cfg.sg) {
+    Frame<K> fr;
+    load_frame<K>(g.frames, a, fr);
+    Pair<K> p;
+    pair_setup<K>(at, jj, fr, g, p);
+    PairMoments<K, DEG, GN> mo;
+    pair_moments<K, DEG, GN>(p, g, in, a, I, mo);
+    float Aa[NPSI];
+    first_psi<K, n_mom<K, DEG>()>(mo.Ma, p.G, Aa);
+    // value
+    if (in.mode == kModeInner) f += I * mo.Ma[0];
+    else if (in.mode == kModeL2Atom) f += I * (0.5f * I * mo.Y0 - mo.X0);
+    // gradient: g_I = sum alpha E, g_xi = I sum_psi A_psi dpsi/dxi
+    float gx[D], grr[PR];
+    psi_grad<K>(p, fr, Aa, gx, grr);
+    gacc[0].add(mo.Ma[0]);
+#pragma unroll
+    for (int c = 0; c < D; ++c) gacc[1 + c].add(I * gx[c]);
+#pragma unroll
+    for (int q = 0; q < PR; ++q) gacc[1 + D + q].add(I * grr[q]);
+    if constexpr (ORDER > 1) {
+      float Ab[NPSI];
+      first_psi<K, n_mom<K, DEG>()>(mo.Mb, p.G, Ab);
+      float Ba[NPSI][NPSI], Bb[NPSI][NPSI];
+      psi_gram<K, true>(mo.Ma, p.G, Ba);
+      psi_gram<K, false>(mo.Mb, p.G, Bb);
+      float X[NPSI][NPSI];
+#pragma unroll
+      for (int k = 0; k < NPSI; ++k)
+#pragma unroll
+        for (int l = 0; l < NPSI; ++l) X[k][l] = I * Ba[k][l] + I * I * Bb[k][l];
+      float Jr[1 + NG][PR];
+      float Hr[PR * (PR + 1) / 2];
+      psi_r_derivs<K>(p, fr, Aa, Jr, Hr);
+      // mixed first-order terms for the I row
+      float Am[NPSI];
+#pragma unroll
+      for (int k = 0; k < NPSI; ++k) Am[k] = Aa[k] + I * Ab[k];
+      float hx[D], hr[PR];
+      psi_grad<K>(p, fr, Am, hx, hr);
+      // packed upper triangle over (I, x, r)
+      int o = 0;
+      hacc[o++] += mo.Mb[0];  // (I, I)
+#pragma unroll
+      for (int c = 0; c < D; ++c) hacc[o++] += hx[c];
+#pragma unroll
+      for (int q = 0; q < PR; ++q) hacc[o++] += hr[q];
+      // x rows
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+#pragma unroll
+        for (int c2 = c; c2 < D; ++c2) {
+          float s = 0.f;
+#pragma unroll
+          for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int i2 = 0; i2 < K; ++i2)
+              s = fmaf(fr.wt[i][c] * X[1 + NG + i][1 + NG + i2], fr.wt[i2][c2], s);
+          hacc[o++] += s;
+        }
+#pragma unroll
+        for (int q = 0; q < PR; ++q) {
+          float s = 0.f;
+#pragma unroll
+          for (int i = 0; i < K; ++i) {
+            float t = 0.f;
+#pragma unroll
+            for (int k = 0; k < 1 + NG; ++k) t = fmaf(X[1 + NG + i][k], Jr[k][q], t);
+            s = fmaf(fr.wt[i][c], t, s);
+          }
+          hacc[o++] += s;
+        }
+      }
+      // r rows
+      int hro = 0;
+#pragma unroll
+      for (int q = 0; q < PR; ++q)
+#pragma unroll
+        for (int s2 = q; s2 < PR; ++s2, ++hro) {
+          float s = I * Hr[hro];
+#pragma unroll
+          for (int k = 0; k < 1 + NG; ++k) {
+            float t = 0.f;
+#pragma unroll
+            for (int l = 0; l < 1 + NG; ++l) t = fmaf(X[k][l], Jr[l][s2], t);
+            s = fmaf(Jr[k][q], t, s);
+          }
+          hacc[o++] += s;
+        }
+    }
+  }
+
+  // combine lanes sharing an atom (fixed butterfly order), then write
+  float vals_f = f;
+  float gv[P];
+#pragma unroll
+  for (int i = 0; i < P; ++i) gv[i] = gacc[i].get();
+  for (int off = cfg.ag; off < 32; off <<= 1) {
+    vals_f += __shfl_xor_sync(0xffffffffu, vals_f, off);
+#pragma unroll
+    for (int i = 0; i < P; ++i) gv[i] += __shfl_xor_sync(0xffffffffu, gv[i], off);
+    if constexpr (ORDER > 1) {
+#pragma unroll
+      for (int i = 0; i < NH; ++i) hacc[i] += __shfl_xor_sync(0xffffffffu, hacc[i], off);
+    }
+  }
+  if (!valid || sub != 0) return;
+  const size_t N = at.n;
+  float *dst = part + (size_t)chunk * cfg.qn * N + j;
+  dst[0] = vals_f;
+#pragma unroll
+  for (int i = 0; i < P; ++i) dst[(1 + i) * N] = gv[i];
+  if constexpr (ORDER > 1) {
+#pragma unroll
+    for (int i = 0; i < NH; ++i) dst[(1 + P + i) * N] = hacc[i];
+  }
+}
+
+// Sum chunk partials in chunk order (FP64), expand the packed Hessian, and
+// apply the isotropic chain rule r_aniso = (s, .., s, 0, ..).
+template <int K>
+__global__ void gr_deriv_finalize_kernel(const float *part, DerivCfg cfg, int n,
+                                         int order, int r_iso, DerivOut out,
+                                         const double *f_extra) {
+  constexpr int D = K + 1;
+  constexpr int P = n_par<K>();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double v[1 + P + P * (P + 1) / 2];
+  for (int q = 0; q < cfg.qn; ++q) {
+    double s = 0.0;
+    for (int c = 0; c < cfg.nchunks; ++c)
+      s += (double)part[((size_t)c * cfg.qn + q) * n + j];
+    v[q] = s;
+  }
+  double f = v[0] + (f_extra ? f_extra[0] : 0.0);
+  double H[P][P];
+  if (order > 1) {
+    int o = 1 + P;
+    for (int a = 0; a < P; ++a)
+      for (int b = a; b < P; ++b, ++o) {
+        H[a][b] = v[o];
+        H[b][a] = v[o];
+      }
+  }
+  out.f[j] = f;
+  if (!r_iso) {
+    for (int a = 0; a < P; ++a) out.g[(size_t)j * P + a] = v[1 + a];
+    if (order > 1)
+      for (int a = 0; a < P; ++a)
+        for (int b = 0; b < P; ++b) out.H[((size_t)j * P + a) * P + b] = H[a][b];
+    return;
+  }
+  // isotropic: parameters (I, x, s); s maps to the D diagonal r entries
+  constexpr int PI = 2 + D;
+  double gi[PI];
+  for (int a = 0; a <= D; ++a) gi[a] = v[1 + a];
+  gi[1 + D] = 0.0;
+  for (int q = 0; q < D; ++q) gi[1 + D] += v[1 + 1 + D + q];
+  for (int a = 0; a < PI; ++a) out.g[(size_t)j * PI + a] = gi[a];
+  if (order > 1) {
+    auto src = [&](int a, int q) { return a < 1 + D ? a : 1 + D + q; };
+    for (int a = 0; a < PI; ++a)
+      for (int b = 0; b < PI; ++b) {
+        const int na = a < 1 + D ? 1 : D, nb = b < 1 + D ? 1 : D;
+        double s = 0.0;
+        for (int qa = 0; qa < na; ++qa)
+          for (int qb = 0; qb < nb; ++qb) s += H[src(a, qa)][src(b, qb)];
+        out.H[((size_t)j * PI + a) * PI + b] = s;
+      }
+  }
+}
+
+// 1/2 sum C^2 helper: block partial sums (FP32 compensated per thread, FP64
+// across the block), then a fixed-order FP64 finalize.
+__global__ void gr_sumsq_kernel(const float *C, size_t n, double *part) {
+  __shared__ double sh[256];
+  CAcc acc;
+  acc.zero();
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float c = C[i];
+    acc.add(c * c);
+  }
+  sh[threadIdx.x] = (double)acc.s + (double)acc.c;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void gr_sumsq_finalize_kernel(const double *part, int n, double scale,
+                                         double *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += part[i];
+  out[0] = scale * s;
+}
+
+constexpr int kSumSqBlocks = 304;
+
+int launch_sum_squares(const float *C, size_t n, double *out, void *ws,
+                       size_t ws_bytes, cudaStream_t stream) {
+  if (ws_bytes < align_up(kSumSqBlocks * sizeof(double))) return kErrWorkspace;
+  double *part = static_cast<double *>(ws);
+  gr_sumsq_kernel<<<kSumSqBlocks, 256, 0, stream>>>(C, n, part);
+  gr_sumsq_finalize_kernel<<<1, 32, 0, stream>>>(part, kSumSqBlocks, 0.5, out);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
+size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order) {
+  DerivCfg c = deriv_cfg(K, n_atoms, n_angles, order);
+  size_t b = align_up((size_t)c.nchunks * c.qn * (size_t)n_atoms * sizeof(float));
+  b += align_up(kSumSqBlocks * sizeof(double)) + align_up(sizeof(double));
+  return b;
+}
+
+int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
+                  const DerivOut &out, void *ws, size_t ws_bytes,
+                  cudaStream_t stream) {
+  const int K = g.K;
+  if (at.n <= 0) return kOk;
+  if (in.order < 1 || in.order > 2) return kErrArg;
+  DerivCfg c = deriv_cfg(K, at.n, g.n_angles, in.order);
+  if (ws == nullptr || ws_bytes < derivs_workspace_bytes(K, at.n, g.n_angles, in.order))
+    return kErrWorkspace;
+  char *wp = static_cast<char *>(ws);
+  float *part = reinterpret_cast<float *>(wp);
+  wp += align_up((size_t)c.nchunks * c.qn * (size_t)at.n * sizeof(float));
+  double *sumsq_part = reinterpret_cast<double *>(wp);
+  wp += align_up(kSumSqBlocks * sizeof(double));
+  double *f_extra = reinterpret_cast<double *>(wp);
+  const double *fe = nullptr;
+  if (in.mode == kModeL2Atom) {
+    const size_t cells = (size_t)g.n_angles * g.ax[0].n * (K == 2 ? g.ax[1].n : 1);
+    int rc = launch_sum_squares(in.alpha, cells, f_extra, sumsq_part,
+                                align_up(kSumSqBlocks * sizeof(double)), stream);
+    if (rc != kOk) return rc;
+    fe = f_extra;
+  }
+  const int warps = ((at.n + c.ag - 1) / c.ag) * c.nchunks;
+  const int blocks = (warps + 3) / 4;
+  if (K == 1) {
+    if (in.order == 1) gr_deriv_kernel<1, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+    else gr_deriv_kernel<1, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+    gr_deriv_finalize_kernel<1><<<(at.n + 127) / 128, 128, 0, stream>>>(
+        part, c, at.n, in.order, at.r_iso, out, fe);
+  } else {
+    if (in.order == 1) gr_deriv_kernel<2, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+    else gr_deriv_kernel<2, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+    gr_deriv_finalize_kernel<2><<<(at.n + 127) / 128, 128, 0, stream>>>(
+        part, c, at.n, in.order, at.r_iso, out, fe);
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
+}  // namespace gr

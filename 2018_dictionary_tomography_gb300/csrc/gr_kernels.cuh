@@ -1,0 +1,72 @@
+// Declarations shared by the kernel translation units and the C ABI.
+#pragma once
+#include "gr_common.cuh"
+
+namespace gr {
+
+// ---- forward projection tiling -------------------------------------------
+constexpr int kProjWarps = 4;        // independent (angle, tile) warps per CTA
+constexpr int kTileDim0 = 32;        // 3D tile rows (detector axis 0)
+constexpr int kTileDim1 = 32;        // 3D tile cols (detector axis 1, contiguous)
+constexpr int kTile1D = 64;          // 2D tile length
+constexpr int kTileCells = 1024;     // shared-memory cell sums per warp
+constexpr int kListWords = 16;       // bitmap words compacted per pass
+constexpr int kProjWarpFloats =
+    2 * kTileCells + 64 + kTileDim1 + kListWords * 32;
+
+struct TileCfg {
+  int t0, t1;     // tile extent along detector axes 0 and 1
+  int nt0, nt1;   // tiles along each axis
+  int ntiles;
+};
+
+enum Epilogue : int { kEpiNone = 0, kEpiL2 = 1, kEpiKL = 2 };
+
+struct ProjOut {
+  float *R;            // sinogram (nullable)
+  int epilogue;
+  const float *data;   // data sinogram (L2 / KL)
+  float bg;            // KL background
+  float *alpha;        // first-order weight field (nullable)
+  float *beta;         // Gauss-Newton weight field (KL, nullable)
+  double *loss_part;   // per-(angle, tile) loss partials (set by the launcher)
+};
+
+// ---- derivatives -----------------------------------------------------------
+enum DerivMode : int {
+  kModeField = 0,    // alpha / beta fields given (fit derivatives)
+  kModeL2Atom = 1,   // alpha = R_atom - C, beta = 1 (per-atom L2 fit to C)
+  kModeInner = 2,    // alpha = C, beta = 0 (inner product <R_atom, C>)
+};
+
+struct DerivIn {
+  int mode;
+  int order;             // 1: value + gradient, 2: + Hessian
+  const float *alpha;    // field, or C for kModeL2Atom / kModeInner
+  const float *beta;     // field (nullable)
+  float beta_const;      // used when beta == nullptr
+};
+
+struct DerivOut {
+  double *f;   // (N)
+  double *g;   // (N, P_out)
+  double *H;   // (N, P_out, P_out), order 2
+};
+
+inline size_t align_up(size_t b) { return (b + 255) & ~(size_t)255; }
+
+TileCfg make_tiles(int K, int D0, int D1);
+size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1);
+int launch_project(const Atoms &at, const Geom &g, const ProjOut &o,
+                   double *loss_out, void *ws, size_t ws_bytes,
+                   cudaStream_t stream);
+
+size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order);
+int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
+                  const DerivOut &out, void *ws, size_t ws_bytes,
+                  cudaStream_t stream);
+
+int launch_sum_squares(const float *C, size_t n, double *out, void *ws,
+                       size_t ws_bytes, cudaStream_t stream);
+
+}  // namespace gr

@@ -1,0 +1,330 @@
+// Forward projection of Gaussian atoms (sm_103a).
+//
+// Replaces the reference's dense per-cell loops __RadProj
+// (GaussDictCode/bin/NewtonBases2D.py:286-296) and __RadProj_3D/_2p5D
+// (GaussDictCode/bin/NewtonBases.py:731-756), which evaluate every atom at
+// every detector cell.  Here:
+//   1. gr_bin_kernel: per (atom, angle) pair, compute the support box of
+//      m <= 1 and set the atom's bit in the bitmap of every detector tile the
+//      box touches (integer atomicOr, so the bitmap does not depend on the
+//      order in which pairs run).
+//   2. gr_project_kernel: one warp per (angle, tile).  The warp reads its
+//      bitmap, so it meets its atoms in increasing index order, computes the
+//      pair data of up to 32 atoms at once (one per lane), then evaluates each
+//      atom densely over its support box clipped to the tile, lanes spread
+//      over the box cells, accumulating into shared-memory cell sums with a
+//      compensated (Kahan/Neumaier) add.  Each cell therefore sums its atoms in
+//      atom-index order, with no float atomics: results are bitwise
+//      reproducible.  The epilogue writes the sinogram and, fused, the
+//      residual or KL weight fields and per-tile loss partials.
+//   3. gr_loss_finalize_kernel: fixed-order FP64 sum of the loss partials.
+#include "gr_kernels.cuh"
+
+namespace gr {
+
+template <int K>
+__global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
+                                                     TileCfg tc, uint32_t *bitmap,
+                                                     int W) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int a = blockIdx.y;
+  if (j >= at.n) return;
+  Frame<K> f;
+  load_frame<K>(g.frames, a, f);
+  Pair<K> p;
+  pair_setup<K>(at, j, f, g, p);
+  if (p.lo[0] > p.hi[0]) return;
+  const uint32_t bit = 1u << (j & 31);
+  const size_t base = (size_t)a * tc.ntiles;
+  const int wj = j >> 5;
+  if constexpr (K == 1) {
+    const int t_lo = p.lo[0] / tc.t0, t_hi = p.hi[0] / tc.t0;
+    for (int t = t_lo; t <= t_hi; ++t)
+      atomicOr(bitmap + (base + t) * W + wj, bit);
+  } else {
+    if (p.lo[1] > p.hi[1]) return;
+    const int r_lo = p.lo[0] / tc.t0, r_hi = p.hi[0] / tc.t0;
+    const int c_lo = p.lo[1] / tc.t1, c_hi = p.hi[1] / tc.t1;
+    for (int tr = r_lo; tr <= r_hi; ++tr)
+      for (int tcix = c_lo; tcix <= c_hi; ++tcix)
+        atomicOr(bitmap + (base + (size_t)tr * tc.nt1 + tcix) * W + wj, bit);
+  }
+}
+
+// Broadcast-ready pair data for the projection loop.
+struct PairLite {
+  float qh0, ql0, qh1, ql1, G0, G1, G2, l2amp;
+  int lo0, hi0, lo1, hi1;
+};
+
+__device__ __forceinline__ PairLite shfl_pair(const PairLite &v, int src) {
+  PairLite o;
+  const unsigned m = 0xffffffffu;
+  o.qh0 = __shfl_sync(m, v.qh0, src);
+  o.ql0 = __shfl_sync(m, v.ql0, src);
+  o.qh1 = __shfl_sync(m, v.qh1, src);
+  o.ql1 = __shfl_sync(m, v.ql1, src);
+  o.G0 = __shfl_sync(m, v.G0, src);
+  o.G1 = __shfl_sync(m, v.G1, src);
+  o.G2 = __shfl_sync(m, v.G2, src);
+  o.l2amp = __shfl_sync(m, v.l2amp, src);
+  o.lo0 = __shfl_sync(m, v.lo0, src);
+  o.hi0 = __shfl_sync(m, v.hi0, src);
+  o.lo1 = __shfl_sync(m, v.lo1, src);
+  o.hi1 = __shfl_sync(m, v.hi1, src);
+  return o;
+}
+
+// Per-cell KL term f log(f/g) - f + g = g h(u), u = f/g, h(u) = u log u - u + 1,
+// evaluated without cancellation: a series in e = u - 1 near u = 1.
+__device__ __forceinline__ float kl_term(float f, float g) {
+  if (!(f > 0.f)) return g;
+  const float e = (f - g) / g;
+  float h;
+  if (fabsf(e) < 0.125f) {
+    // h = sum_{k>=2} (-1)^k e^k / (k (k-1))
+    float e2 = e * e;
+    h = e2 * (0.5f + e * (-1.f / 6.f + e * (1.f / 12.f + e * (-1.f / 20.f +
+             e * (1.f / 30.f + e * (-1.f / 42.f + e * (1.f / 56.f)))))));
+  } else {
+    const float u = f / g;
+    h = u * logf(u) - u + 1.f;
+  }
+  return g * h;
+}
+
+template <int K, bool KAHAN>
+__global__ void __launch_bounds__(kProjWarps * 32)
+    gr_project_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
+                      int W, ProjOut out) {
+  extern __shared__ float smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * kProjWarps + warp;
+  const int n_items = g.n_angles * tc.ntiles;
+  if (item >= n_items) return;  // whole warp leaves together
+  const int cells = tc.t0 * tc.t1;
+  float *acc = smem + (size_t)warp * kProjWarpFloats;
+  float *cmp = acc + kTileCells;
+  float *pc0 = cmp + kTileCells;              // coordinates of tile rows
+  float *pc1 = pc0 + 64;                      // coordinates of tile cols
+  int *list = reinterpret_cast<int *>(pc1 + kTileDim1);
+
+  const int a = item / tc.ntiles, t = item - a * tc.ntiles;
+  const int tr = t / tc.nt1, tcix = t - tr * tc.nt1;
+  const int r0 = tr * tc.t0, c0 = tcix * tc.t1;
+  const int D0 = g.ax[0].n, D1 = (K == 1) ? 1 : g.ax[1].n;
+
+  for (int e = lane; e < cells; e += 32) {
+    acc[e] = 0.f;
+    if (KAHAN) cmp[e] = 0.f;
+  }
+  for (int e = lane; e < tc.t0; e += 32)
+    pc0[e] = (r0 + e < D0) ? g.ax[0].coords[r0 + e] : 0.f;
+  if constexpr (K == 2)
+    for (int e = lane; e < tc.t1; e += 32)
+      pc1[e] = (c0 + e < D1) ? g.ax[1].coords[c0 + e] : 0.f;
+  Frame<K> f;
+  load_frame<K>(g.frames, a, f);
+  __syncwarp();
+
+  const uint32_t *words = bitmap + (size_t)item * W;
+  for (int wb = 0; wb < W; wb += kListWords) {
+    // compact the set bits of kListWords bitmap words into list[] in order
+    const int wi = wb + (lane < kListWords ? lane : 0);
+    uint32_t wd = (lane < kListWords && wi < W) ? words[wi] : 0u;
+    int cnt = __popc(wd), incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int pos = incl - cnt;
+    while (wd) {
+      const int b = __ffs(wd) - 1;
+      list[pos++] = (wi << 5) + b;
+      wd &= wd - 1;
+    }
+    __syncwarp();
+    for (int bs = 0; bs < total; bs += 32) {
+      const int idx = bs + lane;
+      PairLite mine;
+      mine.lo0 = 1;
+      mine.hi0 = 0;
+      mine.lo1 = 1;
+      mine.hi1 = 0;
+      if (idx < total) {
+        Pair<K> p;
+        pair_setup<K>(at, list[idx], f, g, p);
+        mine.qh0 = p.qh[0];
+        mine.ql0 = p.ql[0];
+        mine.G0 = p.G[0];
+        mine.G1 = p.G[1];
+        mine.G2 = p.G[2];
+        mine.l2amp = p.l2amp;
+        mine.lo0 = max(p.lo[0], r0);
+        mine.hi0 = min(p.hi[0], r0 + tc.t0 - 1);
+        if constexpr (K == 2) {
+          mine.qh1 = p.qh[1];
+          mine.ql1 = p.ql[1];
+          mine.lo1 = max(p.lo[1], c0);
+          mine.hi1 = min(p.hi[1], c0 + tc.t1 - 1);
+        } else {
+          mine.qh1 = 0.f;
+          mine.ql1 = 0.f;
+          mine.lo1 = 0;
+          mine.hi1 = 0;
+        }
+      }
+      const int nb = min(32, total - bs);
+      for (int s = 0; s < nb; ++s) {
+        const PairLite q = shfl_pair(mine, s);
+        if (q.lo0 > q.hi0 || q.lo1 > q.hi1) continue;  // warp-uniform
+        const int bw = q.hi1 - q.lo1 + 1;
+        const int ncell = (q.hi0 - q.lo0 + 1) * bw;
+        const float inv_bw = 1.f / (float)bw;
+        for (int e = lane; e < ncell; e += 32) {
+          const int rr = (int)(((float)e + 0.5f) * inv_bw);
+          const int cc = e - rr * bw;
+          const int lr = q.lo0 - r0 + rr;        // tile-local row
+          const int lc = (K == 2) ? (q.lo1 - c0 + cc) : 0;
+          const float d0 = (pc0[lr] - q.qh0) - q.ql0;
+          float m;
+          if constexpr (K == 2) {
+            const float d1 = (pc1[lc] - q.qh1) - q.ql1;
+            m = fmaf(d0, fmaf(q.G0, d0, 2.f * q.G1 * d1), q.G2 * d1 * d1);
+          } else {
+            m = q.G0 * d0 * d0;
+          }
+          if (m <= 1.f) {
+            const float v = ex2_approx(fmaf(m, kNegThirtyLog2e, q.l2amp));
+            const int ci = lr * tc.t1 + lc;
+            if (KAHAN) {
+              const float s0 = acc[ci];
+              const float tt = s0 + v;
+              cmp[ci] += (fabsf(s0) >= v) ? ((s0 - tt) + v) : ((v - tt) + s0);
+              acc[ci] = tt;
+            } else {
+              acc[ci] += v;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+  }
+  __syncwarp();
+
+  // epilogue: write the tile, fused fit fields and loss partial
+  float lsum = 0.f, lcmp = 0.f;
+  for (int e = lane; e < cells; e += 32) {
+    const int lr = e / tc.t1, lc = e - lr * tc.t1;
+    const int row = r0 + lr, col = c0 + lc;
+    if (row >= D0 || col >= D1) continue;
+    const float v = KAHAN ? (acc[e] + cmp[e]) : acc[e];
+    const size_t gi = ((size_t)a * D0 + row) * D1 + col;
+    if (out.R) out.R[gi] = v;
+    float l = 0.f;
+    if (out.epilogue == kEpiL2) {
+      const float res = v - out.data[gi];
+      if (out.alpha) out.alpha[gi] = res;
+      l = 0.5f * res * res;
+    } else if (out.epilogue == kEpiKL) {
+      const float fo = out.data[gi];
+      const float gg = v + out.bg;
+      const float ig = 1.f / gg;
+      if (out.alpha) out.alpha[gi] = 1.f - fo * ig;
+      if (out.beta) out.beta[gi] = fo * ig * ig;
+      l = kl_term(fo, gg);
+    }
+    const float tt = lsum + l;
+    lcmp += (fabsf(lsum) >= fabsf(l)) ? ((lsum - tt) + l) : ((l - tt) + lsum);
+    lsum = tt;
+  }
+  if (out.loss_part) {
+    double d = warp_sum_d((double)lsum + (double)lcmp);
+    if (lane == 0) out.loss_part[item] = d;
+  }
+}
+
+__global__ void gr_loss_finalize_kernel(const double *part, int n, double *out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
+}
+
+TileCfg make_tiles(int K, int D0, int D1) {
+  TileCfg tc;
+  if (K == 1) {
+    tc.t0 = kTile1D;
+    tc.t1 = 1;
+    tc.nt0 = (D0 + tc.t0 - 1) / tc.t0;
+    tc.nt1 = 1;
+  } else {
+    tc.t0 = kTileDim0;
+    tc.t1 = kTileDim1;
+    tc.nt0 = (D0 + tc.t0 - 1) / tc.t0;
+    tc.nt1 = (D1 + tc.t1 - 1) / tc.t1;
+  }
+  tc.ntiles = tc.nt0 * tc.nt1;
+  return tc;
+}
+
+size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1) {
+  TileCfg tc = make_tiles(K, D0, D1);
+  const size_t W = (size_t)(n_atoms + 31) / 32;
+  const size_t items = (size_t)n_angles * tc.ntiles;
+  size_t bytes = align_up(items * W * sizeof(uint32_t));
+  bytes += align_up(items * sizeof(double));
+  return bytes;
+}
+
+int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
+                   double *loss_out, void *ws, size_t ws_bytes,
+                   cudaStream_t stream) {
+  const int K = g.K;
+  const int D0 = g.ax[0].n, D1 = K == 1 ? 1 : g.ax[1].n;
+  TileCfg tc = make_tiles(K, D0, D1);
+  const int W = (at.n + 31) / 32;
+  const size_t items = (size_t)g.n_angles * tc.ntiles;
+  const size_t need = project_workspace_bytes(K, at.n, g.n_angles, D0, D1);
+  if (ws_bytes < need || (ws == nullptr && need > 0)) return kErrWorkspace;
+  char *wp = static_cast<char *>(ws);
+  uint32_t *bitmap = reinterpret_cast<uint32_t *>(wp);
+  wp += align_up(items * W * sizeof(uint32_t));
+  double *loss_part = reinterpret_cast<double *>(wp);
+  ProjOut o = o_in;
+  o.loss_part = loss_out ? loss_part : nullptr;
+  if (W > 0) {
+    if (cudaMemsetAsync(bitmap, 0, items * W * sizeof(uint32_t), stream) != cudaSuccess)
+      return kErrLaunch;
+    dim3 bgrid((at.n + 127) / 128, g.n_angles);
+    if (K == 1)
+      gr_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W);
+    else
+      gr_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W);
+  }
+  const int blocks = (int)((items + kProjWarps - 1) / kProjWarps);
+  const size_t smem = (size_t)kProjWarps * kProjWarpFloats * sizeof(float);
+  if (K == 1) {
+    auto kern = gr_project_kernel<1, true>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o);
+  } else {
+    auto kern = gr_project_kernel<2, true>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o);
+  }
+  if (loss_out)
+    gr_loss_finalize_kernel<<<1, 256, 0, stream>>>(loss_part, (int)items, loss_out);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
+}  // namespace gr

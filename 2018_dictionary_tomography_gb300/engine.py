@@ -1,0 +1,194 @@
+"""Device-level API of the Gaussian-atom Radon engine (torch tensors in HBM).
+
+Every function here launches the hand-written sm_103a kernels of
+libgauss_radon.so through its C ABI on the current torch CUDA stream.  There
+is no CPU path: calls raise ``EngineError`` when the library or a CUDA device
+is missing.
+
+Atoms are ``(I (N,), x (N, d), r (N, P_r) or (N,) / (N, 1) isotropic)``;
+geometry is a :class:`DeviceGeometry`.
+"""
+import ctypes
+import threading
+
+import torch
+
+from . import _lib
+from .geometry import DeviceGeometry
+
+_ws_lock = threading.Lock()
+_workspaces = {}
+
+
+def _require_cuda(device):
+    if not torch.cuda.is_available():
+        raise _lib.EngineError("no CUDA device: the Gaussian-atom Radon engine "
+                               "runs only on the GPU")
+    if device.type != "cuda":
+        raise _lib.EngineError("engine tensors must live on a CUDA device, got %s" % device)
+
+
+def workspace(nbytes, device):
+    """Per-(device, stream) scratch buffer, grown on demand and reused."""
+    stream = torch.cuda.current_stream(device)
+    key = (device.index, stream.cuda_stream)
+    with _ws_lock:
+        buf = _workspaces.get(key)
+        if buf is None or buf.numel() < nbytes:
+            buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+            _workspaces[key] = buf
+    return buf
+
+
+def _stream_handle(device):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+class DeviceAtoms:
+    """Float32 device copies of atom parameters plus the C-ABI descriptor."""
+
+    def __init__(self, I, x, r, device=None):
+        device = torch.device(device or "cuda")
+        _require_cuda(device)
+        I = torch.as_tensor(I).to(device=device, dtype=torch.float32).reshape(-1).contiguous()
+        n = I.numel()
+        x = torch.as_tensor(x).to(device=device, dtype=torch.float32)
+        r = torch.as_tensor(r).to(device=device, dtype=torch.float32)
+        if n > 0:
+            x = x.reshape(n, -1).contiguous()
+            r = r.reshape(n, -1).contiguous()
+        else:
+            x = x.reshape(0, x.shape[-1] if x.dim() > 1 else 0)
+            r = r.reshape(0, r.shape[-1] if r.dim() > 1 else 1)
+        self.iso = r.shape[1] == 1
+        if self.iso:
+            r = r.reshape(n).contiguous()
+        self.I, self.x, self.r = I, x, r
+        self.n = n
+        self.dim = x.shape[1] if n > 0 else 0
+        s = _lib.GrAtoms()
+        s.n_atoms = n
+        s.I = I.data_ptr() if n else None
+        s.x = x.data_ptr() if n else None
+        s.r = r.data_ptr() if n else None
+        s.r_iso = 1 if self.iso else 0
+        self.struct = s
+
+    def n_params(self):
+        d = self.dim
+        if self.iso:
+            return 2 + d
+        return 1 + d + (3 if d == 2 else 6)
+
+
+def _check_dims(atoms, geom):
+    if atoms.n and atoms.dim != geom.dim:
+        raise ValueError("atoms are %dD but the geometry is %dD" % (atoms.dim, geom.dim))
+    if not atoms.iso and atoms.n:
+        want = 3 if geom.dim == 2 else 6
+        if atoms.r.shape[1] != want:
+            raise ValueError("anisotropic r must have %d entries per atom" % want)
+
+
+def _ws_for(op, atoms, geom):
+    lib = _lib.load()
+    n = lib.gr_workspace_bytes(op, ctypes.byref(atoms.struct), ctypes.byref(geom.struct))
+    return workspace(n, geom.device), n
+
+
+def radproj(atoms, geom, out=None):
+    """Forward projection R (A, D0[, D1]) float32 on the device."""
+    _check_dims(atoms, geom)
+    if out is None:
+        out = torch.empty(geom.shape, dtype=torch.float32, device=geom.device)
+    if tuple(out.shape) != tuple(geom.shape) or out.dtype != torch.float32 or not out.is_contiguous():
+        raise ValueError("output must be a contiguous float32 tensor of shape %s" % (geom.shape,))
+    ws, n = _ws_for(_lib.GR_OP_PROJECT, atoms, geom)
+    st = _lib.load().gr_radproj(ctypes.byref(atoms.struct), ctypes.byref(geom.struct),
+                                out.data_ptr(), ws.data_ptr(), n, _stream_handle(geom.device))
+    _lib.check(st, "gr_radproj")
+    return out
+
+
+def fit_forward(atoms, geom, data, fit="l2", background=0.0, want_R=False,
+                want_fields=True):
+    """Projection fused with an L2 or KL fit.
+
+    Returns dict with 'loss' (0-d float64 device tensor), 'alpha', 'beta'
+    (KL) and 'R' when requested.
+    """
+    _check_dims(atoms, geom)
+    data = torch.as_tensor(data, device=geom.device, dtype=torch.float32).contiguous()
+    if tuple(data.shape) != tuple(geom.shape):
+        raise ValueError("data shape %s does not match geometry %s" % (tuple(data.shape), geom.shape))
+    code = {"l2": _lib.GR_FIT_L2, "kl": _lib.GR_FIT_KL}[fit]
+    dev = geom.device
+    out = {"loss": torch.empty((), dtype=torch.float64, device=dev)}
+    R = torch.empty(geom.shape, dtype=torch.float32, device=dev) if want_R else None
+    alpha = torch.empty(geom.shape, dtype=torch.float32, device=dev) if want_fields else None
+    beta = (torch.empty(geom.shape, dtype=torch.float32, device=dev)
+            if (want_fields and fit == "kl") else None)
+    ws, n = _ws_for(_lib.GR_OP_PROJECT, atoms, geom)
+    p = lambda t: None if t is None else t.data_ptr()
+    st = _lib.load().gr_fit_forward(
+        ctypes.byref(atoms.struct), ctypes.byref(geom.struct), code, data.data_ptr(),
+        float(background), p(R), p(alpha), p(beta), out["loss"].data_ptr(),
+        ws.data_ptr(), n, _stream_handle(dev))
+    _lib.check(st, "gr_fit_forward")
+    out["R"], out["alpha"], out["beta"] = R, alpha, beta
+    return out
+
+
+MODES = {"field": _lib.GR_MODE_FIELD, "l2_atom": _lib.GR_MODE_L2_ATOM,
+         "inner": _lib.GR_MODE_INNER}
+
+
+def atom_derivs(atoms, geom, mode, field, beta_field=None, beta_const=1.0, order=2):
+    """Per-atom value (N,), gradient (N, P) and Hessian (N, P, P), float64.
+
+    mode 'inner' (field = C): derivatives of <R_j, C>;
+    mode 'l2_atom' (field = C): of 1/2 |R_j - C|^2, each atom alone;
+    mode 'field' (field = alpha, beta): g = sum alpha dR_j,
+    H = sum beta dR_j dR_j^T + alpha d2R_j, f = 0.
+    """
+    _check_dims(atoms, geom)
+    dev = geom.device
+    field = torch.as_tensor(field, device=dev, dtype=torch.float32).contiguous()
+    if tuple(field.shape) != tuple(geom.shape):
+        raise ValueError("field shape %s does not match geometry %s" % (tuple(field.shape), geom.shape))
+    if beta_field is not None:
+        beta_field = torch.as_tensor(beta_field, device=dev, dtype=torch.float32).contiguous()
+    P = atoms.n_params()
+    N = atoms.n
+    f = torch.empty(N, dtype=torch.float64, device=dev)
+    g = torch.empty((N, P), dtype=torch.float64, device=dev)
+    H = torch.empty((N, P, P), dtype=torch.float64, device=dev) if order == 2 else None
+    if N == 0:
+        return f, g, H
+    op = _lib.GR_OP_DERIVS_1 if order == 1 else _lib.GR_OP_DERIVS_2
+    ws, n = _ws_for(op, atoms, geom)
+    st = _lib.load().gr_atom_derivs(
+        ctypes.byref(atoms.struct), ctypes.byref(geom.struct), MODES[mode],
+        field.data_ptr(), None if beta_field is None else beta_field.data_ptr(),
+        float(beta_const), int(order), f.data_ptr(), g.data_ptr(),
+        None if H is None else H.data_ptr(), ws.data_ptr(), n, _stream_handle(dev))
+    _lib.check(st, "gr_atom_derivs")
+    return f, g, H
+
+
+def l2_fit_derivs(atoms, geom, data, order=2):
+    """Loss 1/2|R - data|^2 and, for every atom j, the gradient and Hessian of
+    the reference's L2derivs_RadProj(atom_j, data + R_j - R) (the Newton-loop
+    call, NewtonGaussian.py:59-60).  f_j equals the loss for every j."""
+    fw = fit_forward(atoms, geom, data, "l2")
+    f, g, H = atom_derivs(atoms, geom, "field", fw["alpha"], None, 1.0, order)
+    f.copy_(fw["loss"].expand_as(f))
+    return fw["loss"], g, H
+
+
+def kl_fit_derivs(atoms, geom, data, background, order=2):
+    """KL(data || R + b) with its per-atom gradient and Hessian."""
+    fw = fit_forward(atoms, geom, data, "kl", background)
+    f, g, H = atom_derivs(atoms, geom, "field", fw["alpha"], fw["beta"], 0.0, order)
+    f.copy_(fw["loss"].expand_as(f))
+    return fw["loss"], g, H

@@ -1,0 +1,143 @@
+/*
+ * gauss_radon.h -- C ABI of the GB300 Gaussian-atom Radon engine.
+ *
+ * Plain C types only: device pointers, sizes and a CUDA stream handle passed
+ * as void* (a cudaStream_t; NULL is the legacy default stream).  Every entry
+ * point is asynchronous on that stream, returns a status code (GR_OK = 0,
+ * negative on error) and never aborts the process.
+ *
+ * The entry points replace the four callables of the reference's kernel
+ * module, the plug-in point that GaussTomo._getOps returns
+ * (GaussDictCode/atomFuncs.py:106-113):
+ *   RadProj(atom, Rad, R)               -> gr_radproj
+ *   L2derivs_RadProj(atom, Rad, C, ord) -> gr_atom_derivs(GR_MODE_L2_ATOM)
+ *   derivs_RadProj(atom, Rad, C, ord)   -> gr_atom_derivs(GR_MODE_INNER)
+ * and add the fused forms the fitting loops need (gr_fit_forward and
+ * gr_atom_derivs(GR_MODE_FIELD)), which compute, for every atom at once, what
+ * the reference obtains with one L2derivs_RadProj launch per atom
+ * (NewtonGaussian.py:59-60).
+ *
+ * Conventions (reference GaussDictCode/bin/NewtonBases2D.py:17-72,
+ * GaussDictCode/bin/NewtonBases.py:239-310):
+ *   atom j = (I[j], x[j*d .. j*d+d-1], r[j*P_r ..]); d = kdet + 1;
+ *   r packed upper-triangular: 2D [r00 r11 r01], 3D [r00 r11 r22 r01 r12 r02],
+ *   or one radius per atom when r_iso != 0;
+ *   derivative order [I, x_0..x_{d-1}, r_0..r_{P_r-1}] (isotropic: [I, x, s]).
+ *   Sinograms are float32, C order, shape (n_angles, n_det[0]) for kdet = 1 or
+ *   (n_angles, n_det[0], n_det[1]) for kdet = 2.
+ */
+#ifndef GAUSS_RADON_H
+#define GAUSS_RADON_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    GR_OK = 0,
+    GR_ERR_ARG = -1,       /* invalid argument (null pointer, bad size) */
+    GR_ERR_WORKSPACE = -2, /* workspace missing or too small */
+    GR_ERR_LAUNCH = -3,    /* CUDA launch or runtime error */
+    GR_ERR_SHAPE = -4      /* geometry not supported (e.g. decreasing grid) */
+};
+
+/* Atoms in device memory (float32). */
+typedef struct {
+    int n_atoms;
+    const float *I;   /* (n_atoms) */
+    const float *x;   /* (n_atoms, d) */
+    const float *r;   /* (n_atoms, P_r) or (n_atoms) when r_iso */
+    int r_iso;
+} gr_atoms;
+
+/*
+ * Projection geometry in device memory.  frames holds one record per angle:
+ *   kdet = 1 (2D):  T(2) w0(2) wt0(2) pad(2)                 -> 8 floats
+ *   kdet = 2 (3D):  T(3) w0(3) w1(3) wt0(3) wt1(3) pad(1)    -> 16 floats
+ * T is the ray direction (ProjSpace.orientations), w0/w1 the detector axes
+ * (ProjSpace.ortho), wt0/wt1 the first kdet rows of inverse([w0 w1 T])
+ * (equal to w0/w1 for orthonormal frames).  The 2.5D single-axis tilt of the
+ * reference (NewtonBases.py:685-688) is the 3D case with T = (T0, T1, 0),
+ * w0 = (w00, w01, 0), w1 = (0, 0, 1).
+ * det[k] are the detector cell centres (ProjSpace.detector), uniformly spaced
+ * and increasing; det_first[k] = det[k][0], det_inv_step[k] = 1/spacing.
+ */
+typedef struct {
+    int kdet;
+    int n_angles;
+    const float *frames;
+    int n_det[2];
+    const float *det[2];
+    float det_first[2];
+    float det_inv_step[2];
+} gr_geometry;
+
+enum { GR_FIT_NONE = 0, GR_FIT_L2 = 1, GR_FIT_KL = 2 };
+enum { GR_MODE_FIELD = 0, GR_MODE_L2_ATOM = 1, GR_MODE_INNER = 2 };
+enum { GR_OP_PROJECT = 0, GR_OP_DERIVS_1 = 1, GR_OP_DERIVS_2 = 2 };
+
+/* Library version (major*10000 + minor*100 + patch). */
+int gr_version(void);
+
+/* Static description of a status code. */
+const char *gr_status_string(int status);
+
+/*
+ * Device workspace (bytes) an operation needs; the caller allocates it
+ * (256-byte aligned) and may reuse it across calls on the same stream.
+ */
+size_t gr_workspace_bytes(int op, const gr_atoms *atoms, const gr_geometry *geom);
+
+/*
+ * Forward projection: R = sum over atoms of I / |r T| exp(-30 m), m <= 1.
+ * Replaces RadProj (GaussDictCode/bin/NewtonBases2D.py:274-296,
+ * GaussDictCode/bin/NewtonBases.py:714-756); R is written in full.
+ */
+int gr_radproj(const gr_atoms *atoms, const gr_geometry *geom, float *R,
+               void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * Forward projection fused with a data fit.
+ *   GR_FIT_L2: alpha = R - data, *loss = 1/2 sum (R - data)^2
+ *              (GaussDictCode/transport_loss.py:569-585).
+ *   GR_FIT_KL: g = R + background, alpha = 1 - data/g, beta = data/g^2,
+ *              *loss = sum data log(data/g) - data + g
+ *              (KL_GaussRadon.py:52-54 with an explicit background).
+ * R, alpha, beta and loss may each be NULL when not wanted; loss is one
+ * double in device memory.
+ */
+int gr_fit_forward(const gr_atoms *atoms, const gr_geometry *geom, int fit,
+                   const float *data, float background, float *R, float *alpha,
+                   float *beta, double *loss, void *workspace,
+                   size_t workspace_bytes, void *stream);
+
+/*
+ * Per-atom value, gradient and Hessian of a data fit, all atoms in one call.
+ *   GR_MODE_INNER   (field = C): f = <R_j, C>, g = <dR_j, C>, H = <d2R_j, C>
+ *                   (derivs_RadProj, NewtonBases2D.py:415-515,
+ *                    NewtonBases.py:954-1069).
+ *   GR_MODE_L2_ATOM (field = C): f = 1/2 |R_j - C|^2 with its gradient and
+ *                   Hessian (L2derivs_RadProj, NewtonBases2D.py:299-401,
+ *                   NewtonBases.py:759-870), each atom fitted alone to C.
+ *   GR_MODE_FIELD   (field = alpha, beta_field or beta_const = beta):
+ *                   g = sum alpha dR_j, H = sum beta dR_j dR_j^T + alpha d2R_j,
+ *                   f = 0.  With alpha = R - data, beta = 1 this is the
+ *                   reference's L2derivs_RadProj(atom_j, data + R_j - R) for
+ *                   every j; with the KL fields of gr_fit_forward it is the
+ *                   KL fit's gradient and Gauss-Newton-plus-curvature Hessian.
+ * order 1: f and g; order 2: f, g and H.  Outputs are float64 in device
+ * memory: f (n_atoms), g (n_atoms, P), H (n_atoms, P, P) with P = 1 + d + P_r
+ * (isotropic: P = 2 + d, exact chain rule of r = (s, .., s, 0, ..)).
+ */
+int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
+                   const float *field, const float *beta_field, float beta_const,
+                   int order, double *f, double *g, double *H, void *workspace,
+                   size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GAUSS_RADON_H */

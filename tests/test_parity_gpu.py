@@ -1,0 +1,136 @@
+"""GPU parity of the CUDA engine against the FP64 oracle.
+
+Tolerance for the FP32 path: 1e-5 relative (sinograms and losses normwise;
+gradients and Hessians per parameter entry, scaled by that entry's largest
+magnitude over the atoms)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import gauss_oracle as go
+from problems import (engine_atoms, engine_geometry, entry_relerr, make_atoms,
+                      make_geometry, relerr)
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+CASES = {
+    "2d": dict(kind="2d", A=30, D0=96, N=24, dim=2),
+    "2p5d": dict(kind="2p5d", A=9, D0=40, D1=36, N=10, dim=3),
+    "3d": dict(kind="3d", A=9, D0=40, D1=44, N=10, dim=3),
+}
+
+
+def _setup(case, iso=False, seed=0):
+    c = CASES[case]
+    g = make_geometry(c["kind"], c["A"], c["D0"], c.get("D1"))
+    I, x, r = make_atoms(c["dim"], c["N"], seed, iso=iso)
+    return g, I, x, r
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("iso", [False, True])
+def test_forward_matches_oracle(eng, cuda_ready, case, iso):
+    g, I, x, r = _setup(case, iso)
+    R = eng.radproj(engine_atoms(I, x, r), engine_geometry(g)).cpu().numpy()
+    ref = go.radproj(I, x, r, g)
+    assert R.shape == ref.shape
+    assert relerr(R, ref) < TOL
+
+
+def test_forward_large_2d_matches_oracle(eng, cuda_ready):
+    """Config-0 sized 2D problem (64 atoms, 60 angles, 128 cells)."""
+    g = make_geometry("2d", 60, 128)
+    I, x, r = make_atoms(2, 64, 11, iso=True, rdiag=(1.61, 6.45), box=0.6)
+    R = eng.radproj(engine_atoms(I, x, r), engine_geometry(g)).cpu().numpy()
+    assert relerr(R, go.radproj(I, x, r, g)) < TOL
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("order", [1, 2])
+def test_inner_derivs_match_oracle(eng, cuda_ready, case, order):
+    g, I, x, r = _setup(case, seed=1)
+    C = np.random.default_rng(2).normal(size=g.shape).astype(np.float32).astype(np.float64)
+    f, gr_, H = eng.atom_derivs(engine_atoms(I, x, r), engine_geometry(g), "inner",
+                                torch.from_numpy(C).float(), order=order)
+    fo, go_, Ho = go.all_atom_derivs("ip", I, x, r, g, C, 2)
+    assert relerr(f.cpu().numpy(), fo) < TOL
+    assert entry_relerr(gr_.cpu().numpy(), go_) < TOL
+    if order == 2:
+        assert entry_relerr(H.cpu().numpy(), Ho) < TOL
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("iso", [False, True])
+def test_l2_fit_derivs_match_oracle(eng, cuda_ready, case, iso):
+    """All-atom L2 derivatives = reference L2derivs_RadProj(atom_j,
+    data + R_j - R) for every j (NewtonGaussian.py:59-60)."""
+    g, I, x, r = _setup(case, iso=iso, seed=3)
+    rng = np.random.default_rng(4)
+    data = (go.radproj(I * 0.9, x + 0.01, r, g) + rng.normal(0, 0.01, g.shape))
+    data = data.astype(np.float32).astype(np.float64)
+    loss, gr_, H = eng.l2_fit_derivs(engine_atoms(I, x, r), engine_geometry(g),
+                                     torch.from_numpy(data).float(), order=2)
+    fo, go_, Ho = go.all_atom_derivs("l2fit", I, x, r, g, data, 2)
+    assert abs(loss.item() - fo[0]) <= TOL * abs(fo[0])
+    assert entry_relerr(gr_.cpu().numpy(), go_) < TOL
+    assert entry_relerr(H.cpu().numpy(), Ho) < TOL
+
+
+@pytest.mark.parametrize("case", ["2d", "3d"])
+def test_l2_single_atom_mode_matches_oracle(eng, cuda_ready, case):
+    """Per-atom L2derivs_RadProj(atom, Rad, C): each atom fitted alone to C,
+    value includes 1/2 sum C^2 over the whole sinogram."""
+    g, I, x, r = _setup(case, seed=5)
+    C = go.radproj(I[:1] * 1.1, x[:1], r[:1], g) + 0.01
+    C = C.astype(np.float32).astype(np.float64)
+    f, gr_, H = eng.atom_derivs(engine_atoms(I, x, r), engine_geometry(g), "l2_atom",
+                                torch.from_numpy(C).float(), order=2)
+    fo, go_, Ho = [], [], []
+    for j in range(I.size):
+        a = go.atom_derivs("l2", I[j], x[j], r[j], g, C, 2)
+        fo.append(a[0]); go_.append(a[1]); Ho.append(a[2])
+    assert relerr(f.cpu().numpy(), np.array(fo)) < TOL
+    assert entry_relerr(gr_.cpu().numpy(), np.array(go_)) < TOL
+    assert entry_relerr(H.cpu().numpy(), np.array(Ho)) < TOL
+
+
+@pytest.mark.parametrize("case", ["2d", "3d"])
+def test_kl_fit_matches_oracle(eng, cuda_ready, case):
+    g, I, x, r = _setup(case, seed=6)
+    rng = np.random.default_rng(7)
+    b = 0.05
+    lam = go.radproj(I, x, r, g) * 200 + b * 200
+    counts = rng.poisson(lam).astype(np.float64) / 200
+    atoms = engine_atoms(I * 1.05, x, r)
+    loss, gr_, H = eng.kl_fit_derivs(atoms, engine_geometry(g),
+                                     torch.from_numpy(counts).float(), b, order=2)
+    R = go.radproj(I * 1.05, x, r, g)
+    assert abs(loss.item() - go.kl_value(counts, R, b)) <= TOL * go.kl_value(counts, R, b)
+    al, be = go.kl_fields(counts, R, b)
+    fo, go_, Ho = go.all_atom_derivs("field", I * 1.05, x, r, g, al, 2, beta=be)
+    assert entry_relerr(gr_.cpu().numpy(), go_) < TOL
+    assert entry_relerr(H.cpu().numpy(), Ho) < TOL
+
+
+def test_bitwise_deterministic(eng, cuda_ready):
+    g, I, x, r = _setup("3d", seed=9)
+    atoms, geom = engine_atoms(I, x, r), engine_geometry(g)
+    data = torch.from_numpy(go.radproj(I, x, r, g) * 0.95).float().cuda()
+    outs = []
+    for _ in range(2):
+        R = eng.radproj(atoms, geom)
+        loss, gg, H = eng.l2_fit_derivs(atoms, geom, data, order=2)
+        outs.append((R.clone(), loss.clone(), gg.clone(), H.clone()))
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
+
+
+def test_atoms_outside_detector_and_empty(eng, cuda_ready):
+    g = make_geometry("2d", 12, 64)
+    I, x, r = make_atoms(2, 5, 12)
+    x[0] = [5.0, 5.0]    # far outside: projects off the detector
+    R = eng.radproj(engine_atoms(I, x, r), engine_geometry(g)).cpu().numpy()
+    assert relerr(R, go.radproj(I, x, r, g)) < TOL
+    R0 = eng.radproj(engine_atoms(I[:0], x[:0], r[:0]), engine_geometry(g))
+    assert torch.count_nonzero(R0).item() == 0
