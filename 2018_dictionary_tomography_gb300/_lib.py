@@ -38,7 +38,8 @@ class EngineError(RuntimeError):
 
 
 EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
-           "gr_fit_forward", "gr_atom_derivs")
+           "gr_fit_forward", "gr_atom_derivs", "gr_count_support", "gr_probe_ex2",
+           "gr_launch_count")
 
 _lock = threading.Lock()
 _lib = None
@@ -83,6 +84,14 @@ def load(build_if_missing=True):
                                        ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_size_t, ctypes.c_void_p]
+        lib.gr_count_support.restype = ctypes.c_int
+        lib.gr_count_support.argtypes = [P(GrAtoms), P(GrGeometry), ctypes.c_void_p,
+                                         ctypes.c_void_p]
+        lib.gr_probe_ex2.restype = ctypes.c_int
+        lib.gr_probe_ex2.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_void_p, ctypes.c_void_p]
+        lib.gr_launch_count.restype = ctypes.c_ulonglong
+        lib.gr_launch_count.argtypes = []
         _lib = lib
         return lib
 

@@ -129,4 +129,22 @@ int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
                        static_cast<cudaStream_t>(stream));
 }
 
+int gr_count_support(const gr_atoms *atoms, const gr_geometry *geom,
+                     unsigned long long *count, void *stream) {
+  Atoms at;
+  Geom g;
+  int st;
+  if (!to_internal(atoms, geom, at, g, &st)) return st;
+  if (!count) return GR_ERR_ARG;
+  return launch_count(at, g, count, static_cast<cudaStream_t>(stream));
+}
+
+int gr_probe_ex2(int blocks, int threads, int iters, float *sink, void *stream) {
+  if (!sink) return GR_ERR_ARG;
+  return launch_ex2_probe(blocks, threads, iters, sink,
+                          static_cast<cudaStream_t>(stream));
+}
+
+unsigned long long gr_launch_count(void) { return g_launches.load(); }
+
 }  // extern "C"

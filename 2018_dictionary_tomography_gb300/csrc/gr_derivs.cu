@@ -59,7 +59,7 @@ inline DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order) {
   c.ag = next_pow2(n_atoms < 1 ? 1 : n_atoms);
   c.sg = 32 / c.ag;
   const int warps_atoms = (n_atoms + c.ag - 1) / c.ag;
-  int nch = (8192 + warps_atoms - 1) / warps_atoms;
+  int nch = (4096 + warps_atoms - 1) / warps_atoms;
   const int max_ch = (n_angles + c.sg - 1) / c.sg;
   if (nch > max_ch) nch = max_ch;
   if (nch < 1) nch = 1;
@@ -544,10 +544,35 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// Sum chunk partials in chunk order (FP64), expand the packed Hessian, and
-// apply the isotropic chain rule r_aniso = (s, .., s, 0, ..).
+// Sum chunk partials (FP64) in a fixed order: a block covers 32 atoms x 8
+// chunk slices; thread (atom, slice) sums chunks slice, slice + 8, ... (reads
+// of consecutive atoms are coalesced), then slice 0 adds the 8 slice sums in
+// slice order.
+constexpr int kRedSlices = 8;
+__global__ void __launch_bounds__(32 * kRedSlices)
+    gr_deriv_reduce_kernel(const float *part, DerivCfg cfg, int n, double *sums) {
+  __shared__ double sh[kRedSlices][32];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + tx;
+  const int q = blockIdx.y;
+  double s = 0.0;
+  if (j < n)
+    for (int c = ty; c < cfg.nchunks; c += kRedSlices)
+      s += (double)part[((size_t)c * cfg.qn + q) * n + j];
+  sh[ty][tx] = s;
+  __syncthreads();
+  if (ty == 0 && j < n) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < kRedSlices; ++k) t += sh[k][tx];
+    sums[(size_t)q * n + j] = t;
+  }
+}
+
+// Expand the packed Hessian and apply the isotropic chain rule
+// r_aniso = (s, .., s, 0, ..).
 template <int K>
-__global__ void gr_deriv_finalize_kernel(const float *part, DerivCfg cfg, int n,
+__global__ void gr_deriv_finalize_kernel(const double *sums, DerivCfg cfg, int n,
                                          int order, int r_iso, DerivOut out,
                                          const double *f_extra) {
   constexpr int D = K + 1;
@@ -555,12 +580,7 @@ __global__ void gr_deriv_finalize_kernel(const float *part, DerivCfg cfg, int n,
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   double v[1 + P + P * (P + 1) / 2];
-  for (int q = 0; q < cfg.qn; ++q) {
-    double s = 0.0;
-    for (int c = 0; c < cfg.nchunks; ++c)
-      s += (double)part[((size_t)c * cfg.qn + q) * n + j];
-    v[q] = s;
-  }
+  for (int q = 0; q < cfg.qn; ++q) v[q] = sums[(size_t)q * n + j];
   double f = v[0] + (f_extra ? f_extra[0] : 0.0);
   double H[P][P];
   if (order > 1) {
@@ -635,12 +655,14 @@ int launch_sum_squares(const float *C, size_t n, double *out, void *ws,
   double *part = static_cast<double *>(ws);
   gr_sumsq_kernel<<<kSumSqBlocks, 256, 0, stream>>>(C, n, part);
   gr_sumsq_finalize_kernel<<<1, 32, 0, stream>>>(part, kSumSqBlocks, 0.5, out);
+  note_launches(2);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
 size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order) {
   DerivCfg c = deriv_cfg(K, n_atoms, n_angles, order);
   size_t b = align_up((size_t)c.nchunks * c.qn * (size_t)n_atoms * sizeof(float));
+  b += align_up((size_t)c.qn * n_atoms * sizeof(double));
   b += align_up(kSumSqBlocks * sizeof(double)) + align_up(sizeof(double));
   return b;
 }
@@ -657,6 +679,8 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
   char *wp = static_cast<char *>(ws);
   float *part = reinterpret_cast<float *>(wp);
   wp += align_up((size_t)c.nchunks * c.qn * (size_t)at.n * sizeof(float));
+  double *sums = reinterpret_cast<double *>(wp);
+  wp += align_up((size_t)c.qn * at.n * sizeof(double));
   double *sumsq_part = reinterpret_cast<double *>(wp);
   wp += align_up(kSumSqBlocks * sizeof(double));
   double *f_extra = reinterpret_cast<double *>(wp);
@@ -670,17 +694,21 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
   }
   const int warps = ((at.n + c.ag - 1) / c.ag) * c.nchunks;
   const int blocks = (warps + 3) / 4;
+  const dim3 rgrid((at.n + 31) / 32, c.qn);
   if (K == 1) {
     if (in.order == 1) gr_deriv_kernel<1, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
     else gr_deriv_kernel<1, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+    gr_deriv_reduce_kernel<<<rgrid, 32 * kRedSlices, 0, stream>>>(part, c, at.n, sums);
     gr_deriv_finalize_kernel<1><<<(at.n + 127) / 128, 128, 0, stream>>>(
-        part, c, at.n, in.order, at.r_iso, out, fe);
+        sums, c, at.n, in.order, at.r_iso, out, fe);
   } else {
     if (in.order == 1) gr_deriv_kernel<2, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
     else gr_deriv_kernel<2, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+    gr_deriv_reduce_kernel<<<rgrid, 32 * kRedSlices, 0, stream>>>(part, c, at.n, sums);
     gr_deriv_finalize_kernel<2><<<(at.n + 127) / 128, 128, 0, stream>>>(
-        part, c, at.n, in.order, at.r_iso, out, fe);
+        sums, c, at.n, in.order, at.r_iso, out, fe);
   }
+  note_launches(3);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 

@@ -1,5 +1,7 @@
 // Declarations shared by the kernel translation units and the C ABI.
 #pragma once
+#include <atomic>
+
 #include "gr_common.cuh"
 
 namespace gr {
@@ -8,7 +10,7 @@ namespace gr {
 constexpr int kProjWarps = 4;        // independent (angle, tile) warps per CTA
 constexpr int kTileDim0 = 32;        // 3D tile rows (detector axis 0)
 constexpr int kTileDim1 = 32;        // 3D tile cols (detector axis 1, contiguous)
-constexpr int kTile1D = 64;          // 2D tile length
+constexpr int kTile1D = 32;          // 2D tile length (one cell per lane)
 constexpr int kTileCells = 1024;     // shared-memory cell sums per warp
 constexpr int kListWords = 16;       // bitmap words compacted per pass
 constexpr int kProjWarpFloats =
@@ -68,5 +70,14 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
 
 int launch_sum_squares(const float *C, size_t n, double *out, void *ws,
                        size_t ws_bytes, cudaStream_t stream);
+
+int launch_count(const Atoms &at, const Geom &g, unsigned long long *out,
+                 cudaStream_t stream);
+int launch_ex2_probe(int blocks, int threads, int iters, float *out,
+                     cudaStream_t stream);
+
+// host-side count of kernels launched by this library
+void note_launches(int n);
+extern std::atomic<unsigned long long> g_launches;
 
 }  // namespace gr

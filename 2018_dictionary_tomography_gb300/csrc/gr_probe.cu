@@ -1,0 +1,89 @@
+// Measurement helpers of the engine (sm_103a):
+//   * gr_count_kernel: exact number of in-support (atom, angle, cell)
+//     evaluations, i.e. triples with m <= 1 -- the unit of work of the
+//     throughput metric.  Integer sums only, so the count is exact.
+//   * gr_ex2_probe_kernel: MUFU ex2 throughput of this GPU (independent
+//     ex2.approx chains), the denominator of the SFU roofline.
+//   * a host-side counter of kernel launches made by this library.
+#include <atomic>
+
+#include "gr_kernels.cuh"
+
+namespace gr {
+
+std::atomic<unsigned long long> g_launches{0};
+
+void note_launches(int n) { g_launches.fetch_add((unsigned long long)n); }
+
+template <int K>
+__global__ void __launch_bounds__(128) gr_count_kernel(Atoms at, Geom g,
+                                                       unsigned long long *out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int a = blockIdx.y;
+  unsigned long long cnt = 0;
+  if (j < at.n) {
+    Frame<K> f;
+    load_frame<K>(g.frames, a, f);
+    Pair<K> p;
+    pair_setup<K>(at, j, f, g, p);
+    const int lo1 = K == 2 ? p.lo[1] : 0, hi1 = K == 2 ? p.hi[1] : 0;
+    for (int k0 = p.lo[0]; k0 <= p.hi[0]; ++k0) {
+      const float d0 = (g.ax[0].coords[k0] - p.qh[0]) - p.ql[0];
+      for (int k1 = lo1; k1 <= hi1; ++k1) {
+        float m;
+        if constexpr (K == 2) {
+          const float d1 = (g.ax[1].coords[k1] - p.qh[1]) - p.ql[1];
+          m = fmaf(d0, fmaf(p.G[0], d0, 2.f * p.G[1] * d1), p.G[2] * d1 * d1);
+        } else {
+          m = p.G[0] * d0 * d0;
+        }
+        cnt += (m <= 1.f) ? 1ull : 0ull;
+      }
+    }
+  }
+  // warp reduction then one integer atomic per warp (exact, order-free)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(out, cnt);
+}
+
+__global__ void gr_ex2_probe_kernel(int iters, float *out) {
+  float v0 = threadIdx.x * 1e-6f, v1 = v0 + 0.1f, v2 = v0 + 0.2f, v3 = v0 + 0.3f;
+  float v4 = v0 + 0.4f, v5 = v0 + 0.5f, v6 = v0 + 0.6f, v7 = v0 + 0.7f;
+  for (int i = 0; i < iters; ++i) {
+    // x -> 2^(-x) maps [0, 1] into [0.5, 1]: bounded, never denormal
+    v0 = ex2_approx(-v0);
+    v1 = ex2_approx(-v1);
+    v2 = ex2_approx(-v2);
+    v3 = ex2_approx(-v3);
+    v4 = ex2_approx(-v4);
+    v5 = ex2_approx(-v5);
+    v6 = ex2_approx(-v6);
+    v7 = ex2_approx(-v7);
+  }
+  const float s = ((v0 + v1) + (v2 + v3)) + ((v4 + v5) + (v6 + v7));
+  if (s == 12345.f) out[0] = s;  // keeps the chains alive
+}
+
+int launch_count(const Atoms &at, const Geom &g, unsigned long long *out,
+                 cudaStream_t stream) {
+  if (cudaMemsetAsync(out, 0, sizeof(unsigned long long), stream) != cudaSuccess)
+    return kErrLaunch;
+  if (at.n > 0) {
+    dim3 grid((at.n + 127) / 128, g.n_angles);
+    if (g.K == 1) gr_count_kernel<1><<<grid, 128, 0, stream>>>(at, g, out);
+    else gr_count_kernel<2><<<grid, 128, 0, stream>>>(at, g, out);
+    note_launches(1);
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
+int launch_ex2_probe(int blocks, int threads, int iters, float *out,
+                     cudaStream_t stream) {
+  if (blocks < 1 || threads < 32 || threads > 1024 || iters < 1) return kErrArg;
+  gr_ex2_probe_kernel<<<blocks, threads, 0, stream>>>(iters, out);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
+}  // namespace gr

@@ -247,6 +247,110 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   }
 }
 
+// 2D sinograms: atom footprints are a few cells wide, so a warp owns a tile
+// of 32 consecutive cells of one angle, one cell per lane, with the cell sum
+// in registers.  Pair data of up to 32 listed atoms is computed in parallel
+// (one atom per lane) and staged in shared memory; every lane then walks the
+// batch in atom order and adds the atoms whose support box holds its cell.
+template <bool KAHAN>
+__global__ void __launch_bounds__(kProjWarps * 32)
+    gr_project1d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
+                        int W, ProjOut out) {
+  __shared__ float4 prm[kProjWarps][32][2];
+  __shared__ int lists[kProjWarps][kListWords * 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * kProjWarps + warp;
+  const int n_items = g.n_angles * tc.ntiles;
+  if (item >= n_items) return;  // whole warp leaves together
+  int *list = lists[warp];
+  const int a = item / tc.ntiles, t = item - a * tc.ntiles;
+  const int D0 = g.ax[0].n;
+  const int cell = t * tc.t0 + lane;
+  const float pc = cell < D0 ? g.ax[0].coords[cell] : 0.f;
+  Frame<1> f;
+  load_frame<1>(g.frames, a, f);
+  float acc = 0.f, cmp = 0.f;
+
+  const uint32_t *words = bitmap + (size_t)item * W;
+  for (int wb = 0; wb < W; wb += kListWords) {
+    const int wi = wb + (lane < kListWords ? lane : 0);
+    uint32_t wd = (lane < kListWords && wi < W) ? words[wi] : 0u;
+    int cnt = __popc(wd), incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int pos = incl - cnt;
+    while (wd) {
+      const int b = __ffs(wd) - 1;
+      list[pos++] = (wi << 5) + b;
+      wd &= wd - 1;
+    }
+    __syncwarp();
+    for (int bs = 0; bs < total; bs += 32) {
+      const int idx = bs + lane;
+      float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 p1 = make_float4(__int_as_float(1), __int_as_float(0), 0.f, 0.f);
+      if (idx < total) {
+        Pair<1> p;
+        pair_setup<1>(at, list[idx], f, g, p);
+        p0 = make_float4(p.qh[0], p.ql[0], p.G[0], p.l2amp);
+        p1 = make_float4(__int_as_float(p.lo[0]), __int_as_float(p.hi[0]), 0.f, 0.f);
+      }
+      prm[warp][lane][0] = p0;
+      prm[warp][lane][1] = p1;
+      __syncwarp();
+      const int nb = min(32, total - bs);
+#pragma unroll 4
+      for (int s2 = 0; s2 < nb; ++s2) {
+        const float4 q0 = prm[warp][s2][0];
+        const float4 q1 = prm[warp][s2][1];
+        const int lo = __float_as_int(q1.x), hi = __float_as_int(q1.y);
+        if (cell >= lo && cell <= hi) {
+          const float d = (pc - q0.x) - q0.y;
+          const float m = q0.z * d * d;
+          if (m <= 1.f) {
+            const float v = ex2_approx(fmaf(m, kNegThirtyLog2e, q0.w));
+            if (KAHAN) {
+              const float tt = acc + v;
+              cmp += (fabsf(acc) >= v) ? ((acc - tt) + v) : ((v - tt) + acc);
+              acc = tt;
+            } else {
+              acc += v;
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+
+  float l = 0.f;
+  if (cell < D0) {
+    const float v = KAHAN ? acc + cmp : acc;
+    const size_t gi = (size_t)a * D0 + cell;
+    if (out.R) out.R[gi] = v;
+    if (out.epilogue == kEpiL2) {
+      const float res = v - out.data[gi];
+      if (out.alpha) out.alpha[gi] = res;
+      l = 0.5f * res * res;
+    } else if (out.epilogue == kEpiKL) {
+      const float fo = out.data[gi];
+      const float gg = v + out.bg;
+      const float ig = 1.f / gg;
+      if (out.alpha) out.alpha[gi] = 1.f - fo * ig;
+      if (out.beta) out.beta[gi] = fo * ig * ig;
+      l = kl_term(fo, gg);
+    }
+  }
+  if (out.loss_part) {
+    const double d = warp_sum_d((double)l);
+    if (lane == 0) out.loss_part[item] = d;
+  }
+}
+
 __global__ void gr_loss_finalize_kernel(const double *part, int n, double *out) {
   __shared__ double sh[256];
   double s = 0.0;
@@ -310,20 +414,22 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
       gr_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W);
     else
       gr_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W);
+    note_launches(1);
   }
   const int blocks = (int)((items + kProjWarps - 1) / kProjWarps);
   const size_t smem = (size_t)kProjWarps * kProjWarpFloats * sizeof(float);
   if (K == 1) {
-    auto kern = gr_project_kernel<1, true>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o);
+    gr_project1d_kernel<true><<<blocks, kProjWarps * 32, 0, stream>>>(at, g, tc, bitmap, W, o);
   } else {
     auto kern = gr_project_kernel<2, true>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o);
   }
-  if (loss_out)
+  note_launches(1);
+  if (loss_out) {
     gr_loss_finalize_kernel<<<1, 256, 0, stream>>>(loss_part, (int)items, loss_out);
+    note_launches(1);
+  }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 

@@ -192,3 +192,28 @@ def kl_fit_derivs(atoms, geom, data, background, order=2):
     f, g, H = atom_derivs(atoms, geom, "field", fw["alpha"], fw["beta"], 0.0, order)
     f.copy_(fw["loss"].expand_as(f))
     return fw["loss"], g, H
+
+
+def count_support(atoms, geom):
+    """Exact number of (atom, angle, cell) triples with m <= 1 (int)."""
+    _check_dims(atoms, geom)
+    out = torch.zeros(1, dtype=torch.int64, device=geom.device)
+    st = _lib.load().gr_count_support(ctypes.byref(atoms.struct), ctypes.byref(geom.struct),
+                                      out.data_ptr(), _stream_handle(geom.device))
+    _lib.check(st, "gr_count_support")
+    return int(out.item())
+
+
+def probe_ex2(blocks, threads, iters, device=None):
+    """Launch the ex2 throughput probe (blocks*threads*iters*8 operations)."""
+    device = torch.device(device or "cuda")
+    _require_cuda(device)
+    sink = torch.zeros(1, dtype=torch.float32, device=device)
+    st = _lib.load().gr_probe_ex2(int(blocks), int(threads), int(iters), sink.data_ptr(),
+                                  _stream_handle(device))
+    _lib.check(st, "gr_probe_ex2")
+
+
+def launch_count():
+    """Kernels launched by the engine library so far in this process."""
+    return int(_lib.load().gr_launch_count())

@@ -1,0 +1,434 @@
+"""Benchmark of the Gaussian-atom Radon hot path on GB300.
+
+Default workload (config 1): 2D anisotropic atoms, 512 atoms, 180 angles,
+256 detector cells, KL fit on Poisson counts (peak 1e4 photons).  One step is
+one Newton iteration's derivative work for every atom at once: the fused KL
+forward projection (sinogram, weight fields, loss) followed by the per-atom
+gradient and Hessian.
+
+Metric: atom-pixel fwd+grad evaluations per second, counting the useful
+(in-support, m <= 1) atom-cell pairs; each such pair is evaluated once by the
+forward and once by the derivative pass of a step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload config1|config2|config4]
+
+Multi-GPU (torchrun): replicas only -- every rank fits its own problem, no
+collective on the data path; value sums the ranks' work over the slowest
+rank's time.
+"""
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "2018_dictionary_tomography_gb300"
+
+METRIC = "atom-pixel fwd+grad evals/s (in-support, m<=1)"
+UNIT = "evals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config1",
+                    choices=["config1", "config2", "config4"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="budget of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        busy = sorted(sm)[len(sm) // 2:] if sm else []
+        return {"sm_mhz": statistics.median(busy) if busy else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+def build_workload(name):
+    wl = importlib.import_module(PKG + ".workloads")
+    return {"config1": wl.config1, "config2": wl.config2, "config4": wl.config4}[name]()
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    importlib.import_module("__graft_entry__").build()
+    engine = importlib.import_module(PKG + ".engine")
+    geometry = importlib.import_module(PKG + ".geometry")
+
+    W = build_workload(args.workload)
+    I0, x0, r0 = W.init
+    geom = geometry.DeviceGeometry(W.orientations, W.ortho, W.detector, dev)
+    atoms = engine.DeviceAtoms(I0, x0, r0, dev)
+    data_d = torch.as_tensor(W.data, dtype=torch.float32).to(dev).contiguous()
+    fit, bg = W.fit, W.background
+    order = 2 if args.workload == "config1" else 1
+    N = atoms.n
+    P = atoms.n_params()
+
+    S = engine.count_support(atoms, geom)           # in-support pairs per pass
+    dense = N * int(np.prod(geom.shape))
+
+    def step():
+        fw = engine.fit_forward(atoms, geom, data_d, fit, bg)
+        f, g, H = engine.atom_derivs(atoms, geom, "field", fw["alpha"], fw["beta"],
+                                     1.0 if fit == "l2" else 0.0, order)
+        return fw, g, H
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing (value) ------------------------------------
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = engine.launch_count()
+    sampler.start()
+    for i in range(args.steps):
+        flush.zero_()                                   # evict L2 between steps
+        e0, e1, e2 = ev[i]
+        e0.record(stream)
+        fw = engine.fit_forward(atoms, geom, data_d, fit, bg)
+        e1.record(stream)
+        engine.atom_derivs(atoms, geom, "field", fw["alpha"], fw["beta"],
+                           1.0 if fit == "l2" else 0.0, order)
+        e2.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = engine.launch_count() - l0
+    t_fwd = [a.elapsed_time(b) for a, b, _ in ev]
+    t_der = [b.elapsed_time(c) for _, b, c in ev]
+    total_ms = sum(t_fwd) + sum(t_der)
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = S * args.steps * ws / (total_ms * 1e-3)
+
+    # ---- end-to-end through the API with host buffers ----------------------
+    Ih = torch.as_tensor(I0, dtype=torch.float32).pin_memory()
+    xh = torch.as_tensor(x0, dtype=torch.float32).pin_memory()
+    rh = torch.as_tensor(r0, dtype=torch.float32).reshape(N, -1).pin_memory()
+    dh = torch.as_tensor(W.data, dtype=torch.float32).pin_memory()
+    Id = torch.empty_like(Ih, device=dev)
+    xd = torch.empty_like(xh, device=dev)
+    rd = torch.empty_like(rh, device=dev)
+    dd = torch.empty_like(dh, device=dev)
+    loss_h = torch.empty((), dtype=torch.float64).pin_memory()
+    g_h = torch.empty((N, P), dtype=torch.float64).pin_memory()
+    H_h = torch.empty((N, P, P), dtype=torch.float64).pin_memory() if order == 2 else None
+    h2d = sum(t.numel() * t.element_size() for t in (Ih, xh, rh, dh))
+    d2h = 8 + g_h.numel() * 8 + (H_h.numel() * 8 if H_h is not None else 0)
+    n_e2e = max(10, args.steps // 4)
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_ms = 0.0
+    for i in range(n_e2e + 3):
+        flush.zero_()
+        if i >= 3:
+            e_start.record(stream)
+        Id.copy_(Ih, non_blocking=True)
+        xd.copy_(xh, non_blocking=True)
+        rd.copy_(rh, non_blocking=True)
+        dd.copy_(dh, non_blocking=True)
+        at = engine.DeviceAtoms(Id, xd, rd, dev)
+        fw = engine.fit_forward(at, geom, dd, fit, bg)
+        f, g, H = engine.atom_derivs(at, geom, "field", fw["alpha"], fw["beta"],
+                                     1.0 if fit == "l2" else 0.0, order)
+        loss_h.copy_(fw["loss"], non_blocking=True)
+        g_h.copy_(g, non_blocking=True)
+        if H_h is not None:
+            H_h.copy_(H, non_blocking=True)
+        if i >= 3:
+            e_end.record(stream)
+            torch.cuda.synchronize()
+            e2e_ms += e_start.elapsed_time(e_end)
+    e2e_value = S * n_e2e * ws / (e2e_ms * 1e-3)
+
+    # ---- roofline ----------------------------------------------------------
+    peaks, src = measured_peaks()
+    ex2_rate = probe_ex2_rate(engine, dev)
+    fwd_ms = statistics.mean(t_fwd)
+    der_ms = statistics.mean(t_der)
+    dom = "derivatives" if der_ms >= fwd_ms else "forward"
+    dom_ms = max(fwd_ms, der_ms)
+    cells = int(np.prod(geom.shape))
+    # algorithmic bytes per launch of each call
+    atom_bytes = N * (1 + atoms.dim + (1 if atoms.iso else atoms.r.shape[1])) * 4
+    fields = 2 if fit == "kl" else 1
+    fwd_bytes = cells * 4 * (1 + fields) + atom_bytes
+    der_bytes = cells * 4 * fields + atom_bytes + N * (P + (P * P if order == 2 else 0)) * 8
+    dom_bytes = der_bytes if dom == "derivatives" else fwd_bytes
+    roofline = {
+        "bound": "sfu",
+        "kernel": "gr_deriv_kernel" if dom == "derivatives" else "gr_project_kernel",
+        "achieved": S / (dom_ms * 1e-3) / 1e9,
+        "peak": ex2_rate / 1e9,
+        "unit": "Gex2/s",
+        "frac": (S / (dom_ms * 1e-3)) / ex2_rate,
+        "peak_source": "measured ex2.approx probe on this GPU (gr_probe_ex2)",
+        "traffic": None,
+        "ms_per_launch": dom_ms,
+    }
+    roofline_hbm = {
+        "bound": "hbm",
+        "achieved": dom_bytes / (dom_ms * 1e-3) / 1e9,
+        "peak": peaks["hbm_gbs"],
+        "unit": "GB/s",
+        "frac": dom_bytes / (dom_ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
+        "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src,
+        "algorithmic_bytes": dom_bytes,
+    }
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (FP64 reductions)", "data": "synthetic (seeded; reference datasets absent)",
+        "config": {"workload": W.name, "atoms": N, "detector": list(geom.shape),
+                   "fit": fit, "order": order, "in_support_pairs_per_pass": S,
+                   "dense_pairs_per_pass": dense, "l2": "flushed between steps (256 MB write)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "dense_equiv_evals_per_s": dense * args.steps * ws / (total_ms * 1e-3),
+        "ms_forward": fwd_ms, "ms_derivatives": der_ms,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / n_e2e},
+        "gpu_launches": launches, "gpu_launches_per_step": launches / args.steps,
+        "roofline": roofline, "roofline_hbm": roofline_hbm,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(W, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def probe_ex2_rate(engine, dev):
+    import torch
+    blocks, threads, iters = 152 * 8, 256, 4096
+    engine.probe_ex2(blocks, threads, 64, dev)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        engine.probe_ex2(blocks, threads, iters, dev)
+        b.record()
+        torch.cuda.synchronize()
+        ops = blocks * threads * iters * 8
+        best = max(best, ops / (a.elapsed_time(b) * 1e-3))
+    return best
+
+
+# --------------------------------------------------------------------------
+# CPU baseline (oracle FP32 twin = restatement of the reference's dense
+# per-pixel kernels) on the host cores
+# --------------------------------------------------------------------------
+def oracle_geometry(W):
+    from oracle import gauss_oracle as go
+    T = np.asarray(W.orientations)
+    if T.shape[1] == 2 and len(W.detector) == 1:
+        return go.Geometry(2, T, W.ortho[0], W.detector[0])
+    if T.shape[1] == 2:
+        return go.Geometry(25, T, W.ortho[0], W.detector[0], None, W.detector[1])
+    return go.Geometry(3, T, W.ortho[0], W.detector[0], W.ortho[1], W.detector[1])
+
+
+def cpu_sample(W, budget_s, threads):
+    """Time the reference algorithm (dense forward + one single-atom
+    derivative evaluation per atom over the whole sinogram) on a sample of
+    atoms; returns (in-support pairs of the sample, seconds, n sampled)."""
+    from oracle import gauss_oracle as go
+    g = oracle_geometry(W)
+    I, x, r = W.init
+    r = go.to_aniso(np.asarray(r).reshape(len(I), -1), g.dim)
+    fit = W.fit
+    order = 2 if W.name.startswith("config1") else 1
+    # fields from the current sinogram (computed once, not timed: the
+    # reference computes them with host numpy between launches)
+    n_take, done_pairs, done_t, n_done = 1, 0, 0.0, 0
+    rng = np.random.default_rng(0)
+    idx = rng.permutation(len(I))
+    Rfull = None
+    while done_t < budget_s and n_done < len(I):
+        sel = idx[n_done:n_done + n_take]
+        if Rfull is None:
+            # approximate residual fields with the sampled atoms only
+            Rfull = np.zeros(g.shape)
+        if fit == "kl":
+            al, be = go.kl_fields(W.data, Rfull, W.background)
+        else:
+            al, be = Rfull - W.data, np.ones(g.shape)
+        t0 = time.perf_counter()
+        go.radproj(I[sel], x[sel], r[sel], g, dtype=np.float32, nthreads=threads)
+        for j in sel:
+            go.atom_derivs("field", I[j], x[j], r[j], g, al, order, dtype=np.float32,
+                           nthreads=threads, beta=be)
+        done_t += time.perf_counter() - t0
+        done_pairs += go.count_support(x[sel], r[sel], g, nthreads=threads)
+        n_done += len(sel)
+        n_take = min(2 * n_take, 64)
+    return done_pairs, done_t, n_done
+
+
+def cpu_baseline(W, budget_s):
+    threads = os.cpu_count() or 1
+    pairs, secs, n = cpu_sample(W, budget_s, threads)
+    return {"value": pairs / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of %d atoms: dense FP32 forward + per-atom derivative "
+                      "evaluation over the full sinogram (%s), %.1f s"
+                      % (n, len(W.init[0]), "order 2" if W.name.startswith("config1") else "order 1", secs)}
+
+
+# --------------------------------------------------------------------------
+# reference arm: the reference's algorithm on the host cores
+# --------------------------------------------------------------------------
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from oracle import build_oracle
+    build_oracle.build()
+    # the workload generator needs a GPU projection for the data; the
+    # reference arm rebuilds the same seeded inputs with the oracle instead
+    wl = importlib.import_module(PKG + ".workloads")
+    from oracle import gauss_oracle as go
+
+    def project(I, x, r, T, w, det):
+        g = (go.Geometry(2, T, w[0], det[0]) if len(det) == 1 else
+             go.Geometry(25 if T.shape[1] == 2 else 3, T, w[0], det[0],
+                         None if T.shape[1] == 2 else w[1], det[1]))
+        return go.radproj(I, x, r, g, dtype=np.float32).astype(np.float64)
+
+    gen = {"config1": wl.config1, "config2": wl.config2, "config4": wl.config4}[args.workload]
+    kw = {"n_orient": 64} if args.workload == "config4" else {}
+    W = gen(project=project, **kw)
+    threads = os.cpu_count() or 1
+    per_step = max(0.05, min(2.0, 120.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_sample(W, per_step * 0.25, threads)
+    pairs, secs = 0, 0.0
+    for _ in range(args.steps):
+        p, s, _n = cpu_sample(W, per_step, threads)
+        pairs += p
+        secs += s
+    value = pairs / secs
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": W.name},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "per step: sampled atoms, dense FP32 forward + per-atom "
+                                   "derivatives over the full sinogram (the reference's "
+                                   "Numba kernels restated in C, OpenMP)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -136,6 +136,23 @@ int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
                    int order, double *f, double *g, double *H, void *workspace,
                    size_t workspace_bytes, void *stream);
 
+/*
+ * Measurement helpers (no counterpart in the reference, which has no
+ * benchmarks).
+ * gr_count_support: *count (device, one unsigned 64-bit integer) = number of
+ *   (atom, angle, cell) triples inside the basis support m <= 1, the exact
+ *   count of useful atom-cell evaluations of one projection.
+ * gr_probe_ex2: runs blocks x threads x iters x 8 independent ex2.approx
+ *   operations (sink: one device float, not written in practice); timing it
+ *   gives the special-function-unit roofline of the GPU.
+ * gr_launch_count: number of kernels this library has launched so far in
+ *   the process (host-side counter).
+ */
+int gr_count_support(const gr_atoms *atoms, const gr_geometry *geom,
+                     unsigned long long *count, void *stream);
+int gr_probe_ex2(int blocks, int threads, int iters, float *sink, void *stream);
+unsigned long long gr_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

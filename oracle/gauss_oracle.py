@@ -37,6 +37,7 @@ def lib():
             getattr(_lib, "or_atom_derivs" + sfx).restype = ctypes.c_int
             getattr(_lib, "or_point_derivs" + sfx).restype = ctypes.c_int
             getattr(_lib, "or_volproj" + sfx).restype = ctypes.c_int
+            getattr(_lib, "or_count_support" + sfx).restype = ctypes.c_longlong
     return _lib
 
 
@@ -223,6 +224,18 @@ def all_atom_derivs(kind, I, x, r, geom, C, order=2, dtype=np.float64, nthreads=
         dfs.append(out[1])
         ddfs.append(out[2])
     return np.array(fs), np.array(dfs), np.array(ddfs)
+
+
+def count_support(x, r, geom, nthreads=None):
+    """Dense count of (atom, angle, cell) triples with m <= 1."""
+    dim = geom.dim
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, dim)
+    r = np.ascontiguousarray(to_aniso(r, dim), dtype=np.float64)
+    I = np.ones(x.shape[0])
+    D1 = 1 if dim == 2 else geom.p1.size
+    return int(lib().or_count_support_f64(
+        geom.gm, x.shape[0], _p(I), _p(x), _p(r), geom.A, _p(geom.T), _p(geom.w0),
+        _p(geom.w1), geom.p0.size, _p(geom.p0), D1, _p(geom.p1), _nthreads(nthreads)))
 
 
 def point_derivs(dim, lenT, I, x, r, y, T, order=2):

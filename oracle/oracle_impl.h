@@ -360,6 +360,36 @@ int FN(or_atom_derivs)(int kind, int gm, const REAL *I, const REAL *x,
 }
 
 /*
+ * Number of (atom, angle, cell) triples inside the basis support m <= 1,
+ * counted densely (the useful work of one projection).
+ */
+long long FN(or_count_support)(int gm, int N, const REAL *I, const REAL *x,
+                               const REAL *r, int A, const REAL *T, const REAL *w0,
+                               const REAL *w1, int D0, const REAL *p0, int D1,
+                               const REAL *p1, int nthreads)
+{
+    int dim, lenT;
+    if (FN(geom)(gm, &dim, &lenT)) return -1;
+    const int Pr = dim == 2 ? 3 : 6;
+    if (dim == 2) D1 = 1;
+    long long total = 0;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : total)
+    for (int a = 0; a < A; a++) {
+        REAL y[3] = {0, 0, 0};
+        for (int k0 = 0; k0 < D0; k0++)
+            for (int k1 = 0; k1 < D1; k1++) {
+                FN(tovec)(gm, a, w0, w1, p0[k0], dim == 2 ? 0 : p1[k1], y);
+                for (int j = 0; j < N; j++) {
+                    /* unit intensity: Rf > 0 exactly when m <= 1 */
+                    if (FN(Rf)(dim, lenT, 1, x + dim * j, r + Pr * j, y, T + lenT * a) > 0)
+                        total++;
+                }
+            }
+    }
+    return total;
+}
+
+/*
  * Per-pixel value/gradient/Hessian at explicit points, for known-answer and
  * finite-difference checks of the restatement itself.
  */
