@@ -52,6 +52,7 @@ const char *gr_status_string(int status) {
     case GR_ERR_WORKSPACE: return "workspace missing or too small";
     case GR_ERR_LAUNCH: return "CUDA launch or runtime error";
     case GR_ERR_SHAPE: return "unsupported geometry";
+    case GR_ERR_TOO_LARGE: return "problem exceeds the 4 MiB built-in scratch of gr_radproj_noalloc";
     default: return "unknown status";
   }
 }

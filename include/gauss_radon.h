@@ -40,7 +40,8 @@ enum {
     GR_ERR_ARG = -1,       /* invalid argument (null pointer, bad size) */
     GR_ERR_WORKSPACE = -2, /* workspace missing or too small */
     GR_ERR_LAUNCH = -3,    /* CUDA launch or runtime error */
-    GR_ERR_SHAPE = -4      /* geometry not supported (e.g. decreasing grid) */
+    GR_ERR_SHAPE = -4,     /* geometry not supported (e.g. decreasing grid) */
+    GR_ERR_TOO_LARGE = -5  /* problem needs more than the built-in scratch */
 };
 
 /* Atoms in device memory (float32). */
@@ -152,6 +153,26 @@ int gr_count_support(const gr_atoms *atoms, const gr_geometry *geom,
                      unsigned long long *count, void *stream);
 int gr_probe_ex2(int blocks, int threads, int iters, float *sink, void *stream);
 unsigned long long gr_launch_count(void);
+
+/*
+ * gr_radproj without a caller-supplied workspace.  No counterpart in the
+ * reference (its kernels are Numba launches that allocate as they please).
+ *
+ * For callers that cannot allocate device memory themselves: a host program
+ * that owns the whole GPU memory budget and gives plug-ins only the buffers
+ * they must fill, a binding that can pass device pointers but has no device
+ * allocator, or a loop that must avoid cudaMalloc/cudaFree because they
+ * synchronise the device.  The scratch is a 4 MiB array compiled into the
+ * library; every GPU that loads the library keeps it until the process exits.
+ * Problems whose projection workspace (gr_workspace_bytes(GR_OP_PROJECT, ..))
+ * exceeds 4 MiB are rejected with GR_ERR_TOO_LARGE.  The call allocates
+ * nothing.  The first call on a device looks up the scratch address on that
+ * device (make it before any stream capture there).  All calls share the
+ * scratch: calls whose GPU work overlaps in time race and must be serialised
+ * by the caller.  Results equal gr_radproj's.
+ */
+int gr_radproj_noalloc(const gr_atoms *atoms, const gr_geometry *geom, float *R,
+                       void *stream);
 
 #ifdef __cplusplus
 }
