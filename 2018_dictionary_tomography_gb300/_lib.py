@@ -12,7 +12,7 @@ from . import build_ext
 GR_OK = 0
 GR_FIT_NONE, GR_FIT_L2, GR_FIT_KL = 0, 1, 2
 GR_MODE_FIELD, GR_MODE_L2_ATOM, GR_MODE_INNER = 0, 1, 2
-GR_OP_PROJECT, GR_OP_DERIVS_1, GR_OP_DERIVS_2 = 0, 1, 2
+GR_OP_PROJECT, GR_OP_DERIVS_1, GR_OP_DERIVS_2, GR_OP_ATOM_STEP = 0, 1, 2, 3
 
 
 class GrAtoms(ctypes.Structure):
@@ -39,7 +39,7 @@ class EngineError(RuntimeError):
 
 EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
            "gr_fit_forward", "gr_atom_derivs", "gr_count_support", "gr_probe_ex2",
-           "gr_launch_count")
+           "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj")
 
 _lock = threading.Lock()
 _lib = None
@@ -90,6 +90,18 @@ def load(build_if_missing=True):
         lib.gr_probe_ex2.restype = ctypes.c_int
         lib.gr_probe_ex2.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_void_p, ctypes.c_void_p]
+        lib.gr_atom_step.restype = ctypes.c_int
+        lib.gr_atom_step.argtypes = [P(GrAtoms), P(GrAtoms), P(GrGeometry), ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                     ctypes.c_void_p]
+        lib.gr_newton_solve.restype = ctypes.c_int
+        lib.gr_newton_solve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int] + \
+            [ctypes.c_void_p] * 9
+        lib.gr_volproj.restype = ctypes.c_int
+        lib.gr_volproj.argtypes = [P(GrAtoms), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p]
         lib.gr_launch_count.restype = ctypes.c_ulonglong
         lib.gr_launch_count.argtypes = []
         _lib = lib

@@ -67,6 +67,7 @@ size_t gr_workspace_bytes(int op, const gr_atoms *atoms, const gr_geometry *geom
     return project_workspace_bytes(g.K, at.n, g.n_angles, g.ax[0].n, D1);
   if (op == GR_OP_DERIVS_1 || op == GR_OP_DERIVS_2)
     return derivs_workspace_bytes(g.K, at.n, g.n_angles, op == GR_OP_DERIVS_1 ? 1 : 2);
+  if (op == GR_OP_ATOM_STEP) return align_up((size_t)g.n_angles * sizeof(double));
   return 0;
 }
 
@@ -128,6 +129,50 @@ int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
   DerivOut out{f, g_out, H};
   return launch_derivs(at, g, in, out, workspace, workspace_bytes,
                        static_cast<cudaStream_t>(stream));
+}
+
+int gr_atom_step(const gr_atoms *old_atom, const gr_atoms *new_atom,
+                 const gr_geometry *geom, int fit, int apply, float *R,
+                 const float *data, float background, float *alpha, float *beta,
+                 double *dloss, void *workspace, size_t workspace_bytes, void *stream) {
+  Atoms ao, an;
+  Geom g;
+  int st;
+  if (!to_internal(old_atom, geom, ao, g, &st)) return st;
+  if (!to_internal(new_atom, geom, an, g, &st)) return st;
+  if (ao.n != 1 || an.n != 1 || ao.r_iso != an.r_iso) return GR_ERR_ARG;
+  if (fit != GR_FIT_L2 && fit != GR_FIT_KL) return GR_ERR_ARG;
+  if (!R || !alpha || !data || (!apply && !dloss)) return GR_ERR_ARG;
+  if (fit == GR_FIT_KL && !(background > 0.f)) return GR_ERR_ARG;
+  return launch_atom_update(ao, an, g, fit == GR_FIT_L2 ? kEpiL2 : kEpiKL, apply ? 1 : 0,
+                            R, data, background, alpha, beta, dloss, workspace,
+                            workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+int gr_newton_solve(int dim, int iso, int n_atoms, const double *g, const double *H,
+                    const double *lam, const double *theta, const unsigned char *mask,
+                    double *theta_new, double *step_norm, int *fail, void *stream) {
+  if ((dim != 2 && dim != 3) || n_atoms < 0) return GR_ERR_ARG;
+  if (n_atoms > 0 && (!g || !H || !lam || !theta || !theta_new || !step_norm))
+    return GR_ERR_ARG;
+  return launch_newton_solve(dim, iso ? 1 : 0, n_atoms, g, H, lam, theta, mask,
+                             theta_new, step_norm, fail, static_cast<cudaStream_t>(stream));
+}
+
+int gr_volproj(const gr_atoms *atoms, int dim, const int *n_vox, const float *const *coords,
+               float *u, void *stream) {
+  if (!atoms || !n_vox || !coords || !u || (dim != 2 && dim != 3)) return GR_ERR_ARG;
+  if (atoms->n_atoms < 0 || (atoms->n_atoms > 0 && (!atoms->I || !atoms->x || !atoms->r)))
+    return GR_ERR_ARG;
+  for (int k = 0; k < dim; ++k)
+    if (n_vox[k] < 1 || !coords[k]) return GR_ERR_ARG;
+  Atoms at;
+  at.n = atoms->n_atoms;
+  at.I = atoms->I;
+  at.x = atoms->x;
+  at.r = atoms->r;
+  at.r_iso = atoms->r_iso ? 1 : 0;
+  return launch_volproj(at, dim, n_vox, coords, u, static_cast<cudaStream_t>(stream));
 }
 
 int gr_count_support(const gr_atoms *atoms, const gr_geometry *geom,

@@ -188,7 +188,8 @@ struct Pair {
   float qh[K], ql[K];  // projection centre q* = hi + lo
   float G[3];          // G00, G01, G11 (K == 1: G00)
   float n;             // 1 / |r T|
-  float l2amp;         // log2(I n)
+  float l2amp;         // log2(|I| n)
+  float sgn;           // sign of I (+1 or -1)
   int lo[K], hi[K];    // inclusive support box in cell indices (empty: lo > hi)
   // quantities kept for the derivative assembly
   float Kc[K + 1][K + 1];  // Kc[c][a] = (r B_c)_a, c = 0..K-1 detector axes, K = T
@@ -253,7 +254,8 @@ __device__ __forceinline__ bool pair_setup(const Atoms &at, int j,
     p.G[2] = g11;
   }
   const float I = at.I[j];
-  p.l2amp = lg2_approx(I * p.n);
+  p.l2amp = lg2_approx(fabsf(I) * p.n);
+  p.sgn = I < 0.f ? -1.f : 1.f;
   float xv[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) xv[a] = at.x[(size_t)D * j + a];

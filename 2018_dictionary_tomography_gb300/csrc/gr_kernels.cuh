@@ -76,6 +76,18 @@ int launch_count(const Atoms &at, const Geom &g, unsigned long long *out,
 int launch_ex2_probe(int blocks, int threads, int iters, float *out,
                      cudaStream_t stream);
 
+int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int fit,
+                       int apply, float *R, const float *data, float bg, float *alpha,
+                       float *beta, double *dloss, void *ws, size_t ws_bytes,
+                       cudaStream_t stream);
+int launch_newton_solve(int dim, int iso, int n, const double *g, const double *H,
+                        const double *lam, const double *theta,
+                        const unsigned char *mask, double *theta_new,
+                        double *step_norm, int *fail, cudaStream_t stream);
+
+int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y,
+                   float *u, cudaStream_t stream);
+
 // host-side count of kernels launched by this library
 void note_launches(int n);
 extern std::atomic<unsigned long long> g_launches;

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
 
 // Broadcast-ready pair data for the projection loop.
 struct PairLite {
-  float qh0, ql0, qh1, ql1, G0, G1, G2, l2amp;
+  float qh0, ql0, qh1, ql1, G0, G1, G2, l2amp, sgn;
   int lo0, hi0, lo1, hi1;
 };
 
@@ -68,6 +68,7 @@ __device__ __forceinline__ PairLite shfl_pair(const PairLite &v, int src) {
   o.G1 = __shfl_sync(m, v.G1, src);
   o.G2 = __shfl_sync(m, v.G2, src);
   o.l2amp = __shfl_sync(m, v.l2amp, src);
+  o.sgn = __shfl_sync(m, v.sgn, src);
   o.lo0 = __shfl_sync(m, v.lo0, src);
   o.hi0 = __shfl_sync(m, v.hi0, src);
   o.lo1 = __shfl_sync(m, v.lo1, src);
@@ -162,6 +163,7 @@ __global__ void __launch_bounds__(kProjWarps * 32)
         mine.G1 = p.G[1];
         mine.G2 = p.G[2];
         mine.l2amp = p.l2amp;
+        mine.sgn = p.sgn;
         mine.lo0 = max(p.lo[0], r0);
         mine.hi0 = min(p.hi[0], r0 + tc.t0 - 1);
         if constexpr (K == 2) {
@@ -197,12 +199,12 @@ __global__ void __launch_bounds__(kProjWarps * 32)
             m = q.G0 * d0 * d0;
           }
           if (m <= 1.f) {
-            const float v = ex2_approx(fmaf(m, kNegThirtyLog2e, q.l2amp));
+            const float v = q.sgn * ex2_approx(fmaf(m, kNegThirtyLog2e, q.l2amp));
             const int ci = lr * tc.t1 + lc;
             if (KAHAN) {
               const float s0 = acc[ci];
               const float tt = s0 + v;
-              cmp[ci] += (fabsf(s0) >= v) ? ((s0 - tt) + v) : ((v - tt) + s0);
+              cmp[ci] += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
               acc[ci] = tt;
             } else {
               acc[ci] += v;
@@ -297,7 +299,7 @@ __global__ void __launch_bounds__(kProjWarps * 32)
         Pair<1> p;
         pair_setup<1>(at, list[idx], f, g, p);
         p0 = make_float4(p.qh[0], p.ql[0], p.G[0], p.l2amp);
-        p1 = make_float4(__int_as_float(p.lo[0]), __int_as_float(p.hi[0]), 0.f, 0.f);
+        p1 = make_float4(__int_as_float(p.lo[0]), __int_as_float(p.hi[0]), p.sgn, 0.f);
       }
       prm[warp][lane][0] = p0;
       prm[warp][lane][1] = p1;
@@ -312,10 +314,10 @@ __global__ void __launch_bounds__(kProjWarps * 32)
           const float d = (pc - q0.x) - q0.y;
           const float m = q0.z * d * d;
           if (m <= 1.f) {
-            const float v = ex2_approx(fmaf(m, kNegThirtyLog2e, q0.w));
+            const float v = q1.z * ex2_approx(fmaf(m, kNegThirtyLog2e, q0.w));
             if (KAHAN) {
               const float tt = acc + v;
-              cmp += (fabsf(acc) >= v) ? ((acc - tt) + v) : ((v - tt) + acc);
+              cmp += (fabsf(acc) >= fabsf(v)) ? ((acc - tt) + v) : ((v - tt) + acc);
               acc = tt;
             } else {
               acc += v;

@@ -217,3 +217,40 @@ def probe_ex2(blocks, threads, iters, device=None):
 def launch_count():
     """Kernels launched by the engine library so far in this process."""
     return int(_lib.load().gr_launch_count())
+
+
+def atom_step(old_atom, new_atom, geom, fit, apply, R, data, alpha, beta=None,
+              background=0.0, dloss=None):
+    """Trial (apply=False: returns the fit change as a 0-d float64 device
+    tensor) or application (apply=True) of one atom's move; see
+    gr_atom_step in include/gauss_radon.h."""
+    code = {"l2": _lib.GR_FIT_L2, "kl": _lib.GR_FIT_KL}[fit]
+    dev = geom.device
+    if dloss is None and not apply:
+        dloss = torch.empty((), dtype=torch.float64, device=dev)
+    ws, n = _ws_for(_lib.GR_OP_ATOM_STEP, old_atom, geom)
+    p = lambda t: None if t is None else t.data_ptr()
+    st = _lib.load().gr_atom_step(
+        ctypes.byref(old_atom.struct), ctypes.byref(new_atom.struct), ctypes.byref(geom.struct),
+        code, 1 if apply else 0, R.data_ptr(), data.data_ptr(), float(background),
+        alpha.data_ptr(), p(beta), p(dloss), ws.data_ptr(), n, _stream_handle(dev))
+    _lib.check(st, "gr_atom_step")
+    return dloss
+
+
+def newton_solve(dim, iso, g, H, lam, theta, mask=None):
+    """Batched damped Newton update (FP64) with the reference's clamps.
+    Returns (theta_new (N, P), step_norm (N,), fail (N,) int32)."""
+    n = theta.shape[0]
+    dev = theta.device
+    theta_new = torch.empty_like(theta)
+    step = torch.empty(n, dtype=torch.float64, device=dev)
+    fail = torch.empty(n, dtype=torch.int32, device=dev)
+    for t in (g, H, lam, theta):
+        assert t.dtype == torch.float64 and t.is_contiguous()
+    st = _lib.load().gr_newton_solve(
+        int(dim), 1 if iso else 0, int(n), g.data_ptr(), H.data_ptr(), lam.data_ptr(),
+        theta.data_ptr(), None if mask is None else mask.data_ptr(), theta_new.data_ptr(),
+        step.data_ptr(), fail.data_ptr(), _stream_handle(dev))
+    _lib.check(st, "gr_newton_solve")
+    return theta_new, step, fail

@@ -77,7 +77,7 @@ typedef struct {
 
 enum { GR_FIT_NONE = 0, GR_FIT_L2 = 1, GR_FIT_KL = 2 };
 enum { GR_MODE_FIELD = 0, GR_MODE_L2_ATOM = 1, GR_MODE_INNER = 2 };
-enum { GR_OP_PROJECT = 0, GR_OP_DERIVS_1 = 1, GR_OP_DERIVS_2 = 2 };
+enum { GR_OP_PROJECT = 0, GR_OP_DERIVS_1 = 1, GR_OP_DERIVS_2 = 2, GR_OP_ATOM_STEP = 3 };
 
 /* Library version (major*10000 + minor*100 + patch). */
 int gr_version(void);
@@ -136,6 +136,44 @@ int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
                    const float *field, const float *beta_field, float beta_const,
                    int order, double *f, double *g, double *H, void *workspace,
                    size_t workspace_bytes, void *stream);
+
+/*
+ * Render atoms on a voxel grid: u[i0, i1(, i2)] = sum_j I_j sqrt(30/pi)
+ * exp(-30 |r_j (y - x_j)|^2) where |r_j (y - x_j)| <= 1, y = (coords[0][i0],
+ * coords[1][i1](, coords[2][i2])).  Replaces VolProj / __VolProj
+ * (GaussDictCode/bin/NewtonBases2D.py:252-271, NewtonBases.py:691-711).
+ * dim 2 or 3; n_vox[k] voxels along axis k; coordinate vectors monotone;
+ * u float32 C order, written in full.  No workspace.
+ */
+int gr_volproj(const gr_atoms *atoms, int dim, const int *n_vox, const float *const *coords,
+               float *u, void *stream);
+
+/*
+ * One atom of a fit moves from old_atom to new_atom (both n_atoms = 1, same
+ * r_iso).  The sinogram R changes by R(new) - R(old) inside the union of the
+ * two supports.  apply = 0 (trial): *dloss = change of the data fit (L2:
+ * 1/2|R - data|^2, KL as in gr_fit_forward), nothing written.  apply = 1:
+ * R, alpha (and beta for KL) are updated there.  This is the per-atom step
+ * of the reference's fitting loops (GD_lib._step, GD_lib.py:492-536) without
+ * its full re-projection and restore.
+ */
+int gr_atom_step(const gr_atoms *old_atom, const gr_atoms *new_atom,
+                 const gr_geometry *geom, int fit, int apply, float *R,
+                 const float *data, float background, float *alpha, float *beta,
+                 double *dloss, void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * Batched damped Newton step, float64, all atoms in one call: solve
+ * (H_j + lam_j 1) d = -g_j (Cholesky; partial-pivoting LU when the damped
+ * block is indefinite, as numpy.linalg.solve in NewtonGaussian.py:74), then
+ * theta_new = theta + d with the reference's clamps: I >= 0 and sign flips
+ * keeping diag(r) >= 0 (GD_lib.py:504-522).  theta (n, P) is [I, x, r] per
+ * atom; mask (nullable) freezes atoms with mask[j] == 0; step_norm[j] = |d|;
+ * fail (nullable) flags singular blocks (their parameters are kept).
+ */
+int gr_newton_solve(int dim, int iso, int n_atoms, const double *g, const double *H,
+                    const double *lam, const double *theta, const unsigned char *mask,
+                    double *theta_new, double *step_norm, int *fail, void *stream);
 
 /*
  * Measurement helpers (no counterpart in the reference, which has no

@@ -1,0 +1,198 @@
+"""GPU tests of the drop-in operator API and the fitting loops against the
+FP64 oracle restatements."""
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import fit_oracle, gauss_oracle as go
+from problems import (engine_atoms, engine_geometry, entry_relerr, make_atoms,
+                      make_geometry, relerr)
+
+pytestmark = pytest.mark.gpu
+PKG = "2018_dictionary_tomography_gb300"
+sp = importlib.import_module(PKG + ".spaces")
+af = importlib.import_module(PKG + ".atomFuncs")
+fid = importlib.import_module(PKG + ".fidelity")
+regm = importlib.import_module(PKG + ".regularisation")
+solvers = importlib.import_module(PKG + ".solvers")
+NB2 = importlib.import_module(PKG + ".NewtonBases2D")
+NB3 = importlib.import_module(PKG + ".NewtonBases")
+
+
+def _tomo(dim, A, D, iso):
+    S = sp.AtomSpace(dim, isotropic=iso)
+    if dim == 2:
+        P = sp.ProjSpace(sp.uniform_partition(0, np.pi, A, nodes_on_bdry=True),
+                         sp.uniform_partition(-1.5, 1.5, D))
+    else:
+        P = sp.ProjSpace(sp.uniform_partition(-np.pi / 3, np.pi / 3, A, nodes_on_bdry=True),
+                         sp.uniform_partition([-1.5, -1.5], [1.5, 1.5], [D, D]))
+    V = sp.VolSpace(sp.uniform_partition([-1] * dim, [1] * dim, [16] * dim))
+    return S, P, af.GaussTomo(S, V, P)
+
+
+def _ogeom(P):
+    if len(P.detector) == 1:
+        return go.Geometry(2, P.orientations, P.ortho[0], P.detector[0])
+    return go.Geometry(25, P.orientations, P.ortho[0], P.detector[0], None, P.detector[1])
+
+
+@pytest.mark.parametrize("dim,iso", [(2, True), (2, False), (3, False)])
+def test_gausstomo_call_and_derivs(cuda_ready, dim, iso):
+    S, P, Radon = _tomo(dim, 12, 40, iso)
+    I, x, r = make_atoms(dim, 6, 31, iso=iso)
+    atoms = S.element(x, r, I)
+    R = Radon(atoms)
+    g = _ogeom(P)
+    ref = go.radproj(atoms.I, atoms.x, atoms.r, g)
+    assert relerr(R.data, ref) < 1e-5
+    C = np.random.default_rng(1).normal(size=P.shape).astype(np.float32)
+    f, df, ddf = Radon.derivs(atoms, P.element(C))
+    fo, dfo, ddfo = go.all_atom_derivs("ip", atoms.I, atoms.x, atoms.r, g, C, 2)
+    assert f.shape == (6, 1) and df.shape == dfo.shape and ddf.shape == ddfo.shape
+    assert entry_relerr(df, dfo) < 1e-5 and entry_relerr(ddf, ddfo) < 1e-5
+    f2, df2 = Radon.L2_derivs(atoms, C, order=1)
+    fo2, dfo2, _ = go.all_atom_derivs("l2", atoms.I, atoms.x, atoms.r, g, C, 1)
+    assert relerr(f2.ravel(), fo2) < 1e-5 and entry_relerr(df2, dfo2) < 1e-5
+
+
+def test_kernel_module_dropin_single_atom(cuda_ready):
+    """The four callables with the reference's signatures (NewtonBases2D.py)."""
+    S, P, Radon = _tomo(2, 10, 48, False)
+    I, x, r = make_atoms(2, 3, 32)
+    atoms = S.element(x, r, I)
+    R = np.zeros(P.shape, dtype=np.float32)
+    NB2.RadProj(atoms, Radon, R)
+    g = _ogeom(P)
+    assert relerr(R, go.radproj(atoms.I, atoms.x, atoms.r, g)) < 1e-5
+    C = R * 0.9
+    f, Df, DDf = NB2.L2derivs_RadProj(atoms, Radon, C)
+    fo, Dfo, DDfo = go.atom_derivs("l2", atoms.I[0], atoms.x[0], atoms.r[0], g, C, 2)
+    assert abs(f - fo) <= 1e-5 * abs(fo)
+    assert relerr(Df, Dfo) < 1e-5 and relerr(DDf, DDfo) < 1e-5
+    f, Df, DDf = NB2.derivs_RadProj(atoms, Radon, C, order=1)
+    fo, Dfo, _ = go.atom_derivs("ip", atoms.I[0], atoms.x[0], atoms.r[0], g, C, 1)
+    assert relerr(Df, Dfo) < 1e-5 and DDf.shape == (6, 6)
+
+
+def test_negative_intensity_forward(eng, cuda_ready):
+    g = make_geometry("3d", 6, 32)
+    I, x, r = make_atoms(3, 8, 33)
+    I[::2] *= -1
+    R = eng.radproj(engine_atoms(I, x, r), engine_geometry(g)).cpu().numpy()
+    assert relerr(R, go.radproj(I, x, r, g)) < 1e-5
+    g2 = make_geometry("2d", 10, 64)
+    I2, x2, r2 = make_atoms(2, 8, 34)
+    I2[1::2] *= -1
+    R2 = eng.radproj(engine_atoms(I2, x2, r2), engine_geometry(g2)).cpu().numpy()
+    assert relerr(R2, go.radproj(I2, x2, r2, g2)) < 1e-5
+
+
+@pytest.mark.parametrize("kind", ["l2", "kl"])
+def test_atom_step_trial_and_apply(eng, cuda_ready, kind):
+    g = make_geometry("2d", 16, 64)
+    I, x, r = make_atoms(2, 5, 35)
+    bg = 0.1 if kind == "kl" else 0.0
+    rng = np.random.default_rng(3)
+    data = go.radproj(I * 1.1, x, r, g) + (bg if kind == "kl" else 0) + rng.uniform(0, 0.02, g.shape)
+    data = data.astype(np.float32).astype(np.float64)
+    geom = engine_geometry(g)
+    dd = torch.from_numpy(data).float().cuda()
+    fw = eng.fit_forward(engine_atoms(I, x, r), geom, dd, kind, bg, want_R=True)
+    I2, x2, r2 = I.copy(), x.copy(), r.copy()
+    x2[2] += 0.03
+    r2[2, 0] *= 1.2
+    I2[2] *= 0.8
+    old = engine_atoms(I[2:3], x[2:3], r[2:3])
+    new = engine_atoms(I2[2:3], x2[2:3], r2[2:3])
+    dl = eng.atom_step(old, new, geom, kind, False, fw["R"], dd, fw["alpha"], fw["beta"], bg)
+    R1 = go.radproj(I, x, r, g)
+    R2 = go.radproj(I2, x2, r2, g)
+    L = (lambda R: go.l2_value(R, data)) if kind == "l2" else (lambda R: go.kl_value(data, R, bg))
+    ref = L(R2) - L(R1)
+    assert abs(dl.item() - ref) <= 1e-5 * abs(L(R1))
+    eng.atom_step(old, new, geom, kind, True, fw["R"], dd, fw["alpha"], fw["beta"], bg)
+    assert relerr(fw["R"].cpu().numpy(), R2) < 1e-5
+    fresh = eng.fit_forward(engine_atoms(I2, x2, r2), geom, dd, kind, bg, want_R=True)
+    assert relerr(fw["alpha"].cpu().numpy(), fresh["alpha"].cpu().numpy()) < 1e-5
+
+
+def test_newton_solve_matches_numpy(eng, cuda_ready):
+    rng = np.random.default_rng(4)
+    for dim, P, iso in ((2, 6, False), (3, 10, False), (2, 4, True), (3, 5, True)):
+        n = 7
+        A = rng.normal(size=(n, P, P))
+        H = A @ A.transpose(0, 2, 1) + 0.1 * np.eye(P)
+        H[3] -= 5 * np.eye(P)       # an indefinite block: LU path
+        gvec = rng.normal(size=(n, P))
+        lam = rng.uniform(0.1, 2, n)
+        theta = np.concatenate([rng.uniform(0.5, 1, (n, 1)), rng.normal(size=(n, P - 1))], 1)
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        th, step, fail = eng.newton_solve(dim, iso, t(gvec), t(H), t(lam), t(theta))
+        for j in range(n):
+            d = np.linalg.solve(H[j] + lam[j] * np.eye(P), -gvec[j])
+            I1, x1, r1 = solvers.step_params(theta[j, 0], theta[j, 1:1 + dim], theta[j, 1 + dim:],
+                                             d, dim, iso)
+            want = np.concatenate([[I1], x1, np.atleast_1d(r1)])
+            assert np.allclose(th[j].cpu().numpy(), want, rtol=1e-10, atol=1e-12)
+            assert np.isclose(step[j].item(), np.linalg.norm(d), rtol=1e-10)
+        assert int(fail.sum().item()) == 0
+
+
+def _fit_problem(kind):
+    S, P, Radon = _tomo(2, 20, 64, True)
+    I, x, r = make_atoms(2, 4, 36, iso=True, rdiag=(3, 5), box=0.4)
+    g = _ogeom(P)
+    bg = 0.5 if kind == "kl" else 0.0
+    truth = go.radproj(I, x, r, g)
+    rng = np.random.default_rng(5)
+    if kind == "kl":
+        # high counts and a close start keep the KL Hessian blocks positive
+        # definite along the path, so FP32 and FP64 runs take the same steps
+        data = rng.poisson((truth + bg) * 2000).astype(np.float64) / 2000
+        init = (I * rng.uniform(0.9, 1.1, I.size), x + rng.normal(0, 0.01, x.shape), r * 1.05)
+    else:
+        data = truth + rng.normal(0, 0.01 * truth.max(), truth.shape)
+        init = (I * rng.uniform(0.8, 1.2, I.size), x + rng.normal(0, 0.02, x.shape), r * 1.1)
+    data = data.astype(np.float32).astype(np.float64)
+    init = tuple(a.astype(np.float32).astype(np.float64) for a in init)
+    return S, P, Radon, g, data, init, bg
+
+
+@pytest.mark.parametrize("kind", ["l2", "kl"])
+def test_newton_loop_matches_oracle(cuda_ready, kind):
+    S, P, Radon, g, data, (I0, x0, r0), bg = _fit_problem(kind)
+    recon = S.element(x0, r0, I0)
+    fidelity = fid.l2_squared_loss(2) if kind == "l2" else fid.KL_loss(2, bg)
+    _, E, F = solvers.Newton_linesearch(recon, P.element(data), [4, 1], fidelity,
+                                        regm.null(2), Radon, resync=False)
+    (_, _, _), Eo, Fo = fit_oracle.newton(I0, x0, r0, g, data, [4, 1], kind, bg)
+    assert E.size == Eo.size
+    assert abs(E[-1] - Eo[-1]) <= 1e-4 * abs(Eo[-1])
+    assert Eo[-1] < Eo[0]
+
+
+def test_gd_block_loop_matches_oracle(cuda_ready):
+    S, P, Radon, g, data, (I0, x0, r0), bg = _fit_problem("l2")
+    recon = S.element(x0, r0, I0)
+    _, E, F = solvers.GD_linesearch_block(recon, P.element(data), [3, 1],
+                                          fid.l2_squared_loss(2), regm.null(2), Radon,
+                                          resync=False)
+    (_, _, _), Eo, Fo = fit_oracle.gd_block(I0, x0, r0, g, data, [3, 1])
+    assert E.size == Eo.size
+    assert abs(E[-1] - Eo[-1]) <= 1e-4 * abs(Eo[-1])
+
+
+@pytest.mark.parametrize("kind", ["l2", "kl"])
+def test_batched_newton_matches_oracle(eng, cuda_ready, kind):
+    S, P, Radon, g, data, (I0, x0, r0), bg = _fit_problem(kind)
+    geom = engine_geometry(g)
+    atoms = engine_atoms(I0, x0, r0)
+    dd = torch.from_numpy(data).float().cuda()
+    iters = 6 if kind == "l2" else 10
+    _, losses = solvers.newton_batched(atoms, geom, dd, iters, kind, bg)
+    _, lo = fit_oracle.newton_batched(I0, x0, r0, g, data, iters, kind, bg)
+    assert abs(losses[-1] - lo[-1]) <= 1e-4 * abs(lo[-1])
+    assert lo[-1] < lo[0]
