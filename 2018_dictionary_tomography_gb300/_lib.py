@@ -39,7 +39,7 @@ class EngineError(RuntimeError):
 
 EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
            "gr_fit_forward", "gr_atom_derivs", "gr_count_support", "gr_probe_ex2",
-           "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj")
+           "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj", "gr_newton_accept")
 
 _lock = threading.Lock()
 _lib = None
@@ -98,7 +98,11 @@ def load(build_if_missing=True):
                                      ctypes.c_void_p]
         lib.gr_newton_solve.restype = ctypes.c_int
         lib.gr_newton_solve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int] + \
-            [ctypes.c_void_p] * 9
+            [ctypes.c_void_p] * 12
+        lib.gr_newton_accept.restype = ctypes.c_int
+        lib.gr_newton_accept.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_void_p] * 5 +
+                                         [ctypes.c_double] * 2 + [ctypes.c_void_p] * 9 +
+                                         [ctypes.c_int, ctypes.c_void_p])
         lib.gr_volproj.restype = ctypes.c_int
         lib.gr_volproj.argtypes = [P(GrAtoms), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p]

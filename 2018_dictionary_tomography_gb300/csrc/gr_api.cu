@@ -151,12 +151,35 @@ int gr_atom_step(const gr_atoms *old_atom, const gr_atoms *new_atom,
 
 int gr_newton_solve(int dim, int iso, int n_atoms, const double *g, const double *H,
                     const double *lam, const double *theta, const unsigned char *mask,
-                    double *theta_new, double *step_norm, int *fail, void *stream) {
+                    double *theta_new, double *step_norm, int *fail, float *I_new,
+                    float *x_new, float *r_new, void *stream) {
   if ((dim != 2 && dim != 3) || n_atoms < 0) return GR_ERR_ARG;
   if (n_atoms > 0 && (!g || !H || !lam || !theta || !theta_new || !step_norm))
     return GR_ERR_ARG;
-  return launch_newton_solve(dim, iso ? 1 : 0, n_atoms, g, H, lam, theta, mask,
-                             theta_new, step_norm, fail, static_cast<cudaStream_t>(stream));
+  if ((I_new || x_new || r_new) && !(I_new && x_new && r_new)) return GR_ERR_ARG;
+  AtomOut ao{I_new, x_new, r_new};
+  return launch_newton_solve(dim, iso ? 1 : 0, n_atoms, g, H, lam, theta, mask, theta_new,
+                             step_norm, fail, ao, static_cast<cudaStream_t>(stream));
+}
+
+int gr_newton_accept(int dim, int iso, int n_atoms, double *loss_cur,
+                     const double *loss_trial, double *theta, const double *theta_trial,
+                     double *lam, double lam_min, double lam_max, float *I, float *x,
+                     float *r, const float *I_trial, const float *x_trial,
+                     const float *r_trial, double *hist, int *hist_accepted,
+                     int *counter, int hist_len, void *stream) {
+  if ((dim != 2 && dim != 3) || n_atoms < 0 || !loss_cur || !loss_trial || !counter)
+    return GR_ERR_ARG;
+  if (n_atoms > 0 && (!theta || !theta_trial || !lam || !I || !x || !r || !I_trial ||
+                      !x_trial || !r_trial))
+    return GR_ERR_ARG;
+  if (hist_len > 0 && (!hist || !hist_accepted)) return GR_ERR_ARG;
+  const int pr = iso ? 1 : (dim == 2 ? 3 : 6);
+  const int P = 1 + dim + pr;
+  return launch_newton_accept(n_atoms, P, pr, dim, loss_cur, loss_trial, theta, theta_trial,
+                              lam, lam_min, lam_max, AtomOut{I, x, r},
+                              AtomIn{I_trial, x_trial, r_trial}, hist, hist_accepted,
+                              counter, hist_len, static_cast<cudaStream_t>(stream));
 }
 
 int gr_volproj(const gr_atoms *atoms, int dim, const int *n_vox, const float *const *coords,

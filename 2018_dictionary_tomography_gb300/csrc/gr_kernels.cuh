@@ -80,10 +80,21 @@ int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int 
                        int apply, float *R, const float *data, float bg, float *alpha,
                        float *beta, double *dloss, void *ws, size_t ws_bytes,
                        cudaStream_t stream);
+struct AtomOut {
+  float *I, *x, *r;
+};
+struct AtomIn {
+  const float *I, *x, *r;
+};
 int launch_newton_solve(int dim, int iso, int n, const double *g, const double *H,
                         const double *lam, const double *theta,
                         const unsigned char *mask, double *theta_new,
-                        double *step_norm, int *fail, cudaStream_t stream);
+                        double *step_norm, int *fail, AtomOut ao, cudaStream_t stream);
+int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
+                         const double *loss_trial, double *theta,
+                         const double *theta_trial, double *lam, double lam_min,
+                         double lam_max, AtomOut cur, AtomIn trial, double *hist,
+                         int *hist_acc, int *counter, int hist_len, cudaStream_t stream);
 
 int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y,
                    float *u, cudaStream_t stream);

@@ -420,12 +420,13 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   }
   const int blocks = (int)((items + kProjWarps - 1) / kProjWarps);
   const size_t smem = (size_t)kProjWarps * kProjWarpFloats * sizeof(float);
+  // smem (kProjWarps * kProjWarpFloats floats) stays below the 48 KB that
+  // needs no opt-in, so no function attribute is set (safe under capture)
+  static_assert(kProjWarps * kProjWarpFloats * sizeof(float) <= 48 * 1024, "smem");
   if (K == 1) {
     gr_project1d_kernel<true><<<blocks, kProjWarps * 32, 0, stream>>>(at, g, tc, bitmap, W, o);
   } else {
-    auto kern = gr_project_kernel<2, true>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o);
+    gr_project_kernel<2, true><<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o);
   }
   note_launches(1);
   if (loss_out) {

@@ -228,7 +228,7 @@ template <int P, int D>
 __global__ void gr_newton_solve_kernel(int n, int iso, const double *g, const double *H,
                                        const double *lam, const double *theta,
                                        const unsigned char *mask, double *theta_new,
-                                       double *step_norm, int *fail) {
+                                       double *step_norm, int *fail, AtomOut ao) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   double A[P][P], b[P];
@@ -268,22 +268,77 @@ __global__ void gr_newton_solve_kernel(int n, int iso, const double *g, const do
   for (int a = 0; a < P; ++a) theta_new[(size_t)j * P + a] = t[a];
   step_norm[j] = sqrt(nrm);
   if (fail) fail[j] = (active && !ok) ? 1 : 0;
+  if (ao.I) {
+    constexpr int PR = P - 1 - D;
+    ao.I[j] = (float)t[0];
+    for (int c = 0; c < D; ++c) ao.x[(size_t)j * D + c] = (float)t[1 + c];
+    for (int q = 0; q < PR; ++q) ao.r[(size_t)j * PR + q] = (float)t[1 + D + q];
+  }
+}
+
+// Device-side accept/reject of a batched Newton trial (no host round trip):
+// one block; if loss_trial <= loss_cur the trial parameters (FP64 and the
+// float32 atom arrays) become current, loss_cur takes the trial loss and the
+// damping halves, else the damping grows tenfold (both clamped).  Appends
+// (loss_cur, accepted) to the history.
+__global__ void gr_newton_accept_kernel(int n, int P, int pr, int dim,
+                                        double *loss_cur, const double *loss_trial,
+                                        double *theta, const double *theta_trial,
+                                        double *lam, double lam_min, double lam_max,
+                                        AtomOut cur, AtomIn trial, double *hist,
+                                        int *hist_acc, int *counter, int hist_len) {
+  __shared__ int acc;
+  if (threadIdx.x == 0) acc = (*loss_trial <= *loss_cur) ? 1 : 0;
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * P; e += blockDim.x)
+    if (acc) theta[e] = theta_trial[e];
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double l = acc ? lam[j] * 0.5 : lam[j] * 10.0;
+    lam[j] = l < lam_min ? lam_min : (l > lam_max ? lam_max : l);
+    if (acc) {
+      cur.I[j] = trial.I[j];
+      for (int c = 0; c < dim; ++c) cur.x[(size_t)j * dim + c] = trial.x[(size_t)j * dim + c];
+      for (int q = 0; q < pr; ++q) cur.r[(size_t)j * pr + q] = trial.r[(size_t)j * pr + q];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (acc) *loss_cur = *loss_trial;
+    const int k = *counter;
+    if (k < hist_len) {
+      hist[k] = *loss_cur;
+      hist_acc[k] = acc;
+    }
+    *counter = k + 1;
+  }
+}
+
+int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
+                         const double *loss_trial, double *theta,
+                         const double *theta_trial, double *lam, double lam_min,
+                         double lam_max, AtomOut cur, AtomIn trial, double *hist,
+                         int *hist_acc, int *counter, int hist_len, cudaStream_t stream) {
+  gr_newton_accept_kernel<<<1, 256, 0, stream>>>(n, P, pr, dim, loss_cur, loss_trial, theta,
+                                                 theta_trial, lam, lam_min, lam_max, cur,
+                                                 trial, hist, hist_acc, counter, hist_len);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
 int launch_newton_solve(int dim, int iso, int n, const double *g, const double *H,
                         const double *lam, const double *theta,
                         const unsigned char *mask, double *theta_new,
-                        double *step_norm, int *fail, cudaStream_t stream) {
+                        double *step_norm, int *fail, AtomOut ao, cudaStream_t stream) {
   if (n <= 0) return kOk;
   const int blocks = (n + 63) / 64;
   if (dim == 2 && iso)
-    gr_newton_solve_kernel<4, 2><<<blocks, 64, 0, stream>>>(n, 1, g, H, lam, theta, mask, theta_new, step_norm, fail);
+    gr_newton_solve_kernel<4, 2><<<blocks, 64, 0, stream>>>(n, 1, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else if (dim == 2)
-    gr_newton_solve_kernel<6, 2><<<blocks, 64, 0, stream>>>(n, 0, g, H, lam, theta, mask, theta_new, step_norm, fail);
+    gr_newton_solve_kernel<6, 2><<<blocks, 64, 0, stream>>>(n, 0, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else if (iso)
-    gr_newton_solve_kernel<5, 3><<<blocks, 64, 0, stream>>>(n, 1, g, H, lam, theta, mask, theta_new, step_norm, fail);
+    gr_newton_solve_kernel<5, 3><<<blocks, 64, 0, stream>>>(n, 1, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else
-    gr_newton_solve_kernel<10, 3><<<blocks, 64, 0, stream>>>(n, 0, g, H, lam, theta, mask, theta_new, step_norm, fail);
+    gr_newton_solve_kernel<10, 3><<<blocks, 64, 0, stream>>>(n, 0, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }

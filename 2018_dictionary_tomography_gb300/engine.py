@@ -251,6 +251,56 @@ def newton_solve(dim, iso, g, H, lam, theta, mask=None):
     st = _lib.load().gr_newton_solve(
         int(dim), 1 if iso else 0, int(n), g.data_ptr(), H.data_ptr(), lam.data_ptr(),
         theta.data_ptr(), None if mask is None else mask.data_ptr(), theta_new.data_ptr(),
-        step.data_ptr(), fail.data_ptr(), _stream_handle(dev))
+        step.data_ptr(), fail.data_ptr(), None, None, None, _stream_handle(dev))
     _lib.check(st, "gr_newton_solve")
     return theta_new, step, fail
+
+
+# ---------------------------------------------------------------------------
+# allocation-free forms with caller-owned buffers (CUDA-graph capturable)
+# ---------------------------------------------------------------------------
+def workspace_bytes(op, atoms, geom):
+    return int(_lib.load().gr_workspace_bytes(op, ctypes.byref(atoms.struct),
+                                              ctypes.byref(geom.struct)))
+
+
+def _ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def fit_forward_into(atoms, geom, data, fit, background, R, alpha, beta, loss, ws):
+    code = {"l2": _lib.GR_FIT_L2, "kl": _lib.GR_FIT_KL}[fit]
+    st = _lib.load().gr_fit_forward(
+        ctypes.byref(atoms.struct), ctypes.byref(geom.struct), code, data.data_ptr(),
+        float(background), _ptr(R), _ptr(alpha), _ptr(beta), _ptr(loss), ws.data_ptr(),
+        ws.numel(), _stream_handle(geom.device))
+    _lib.check(st, "gr_fit_forward")
+
+
+def atom_derivs_into(atoms, geom, mode, field, beta_field, beta_const, order, f, g, H, ws):
+    st = _lib.load().gr_atom_derivs(
+        ctypes.byref(atoms.struct), ctypes.byref(geom.struct), MODES[mode], field.data_ptr(),
+        _ptr(beta_field), float(beta_const), int(order), f.data_ptr(), g.data_ptr(), _ptr(H),
+        ws.data_ptr(), ws.numel(), _stream_handle(geom.device))
+    _lib.check(st, "gr_atom_derivs")
+
+
+def newton_solve_into(dim, iso, g, H, lam, theta, theta_new, step, trial_atoms, device):
+    st = _lib.load().gr_newton_solve(
+        int(dim), 1 if iso else 0, int(theta.shape[0]), g.data_ptr(), H.data_ptr(),
+        lam.data_ptr(), theta.data_ptr(), None, theta_new.data_ptr(), step.data_ptr(), None,
+        trial_atoms.I.data_ptr(), trial_atoms.x.data_ptr(), trial_atoms.r.data_ptr(),
+        _stream_handle(device))
+    _lib.check(st, "gr_newton_solve")
+
+
+def newton_accept_into(dim, iso, loss_cur, loss_trial, theta, theta_trial, lam, lam_min,
+                       lam_max, cur_atoms, trial_atoms, hist, hist_acc, counter, device):
+    st = _lib.load().gr_newton_accept(
+        int(dim), 1 if iso else 0, int(theta.shape[0]), loss_cur.data_ptr(),
+        loss_trial.data_ptr(), theta.data_ptr(), theta_trial.data_ptr(), lam.data_ptr(),
+        float(lam_min), float(lam_max), cur_atoms.I.data_ptr(), cur_atoms.x.data_ptr(),
+        cur_atoms.r.data_ptr(), trial_atoms.I.data_ptr(), trial_atoms.x.data_ptr(),
+        trial_atoms.r.data_ptr(), hist.data_ptr(), hist_acc.data_ptr(), counter.data_ptr(),
+        int(hist.numel()), _stream_handle(device))
+    _lib.check(st, "gr_newton_accept")

@@ -174,3 +174,59 @@ def config4(seed=4, n_orient=20000, project=project_host, snr=0.1):
     init = (I * rng.uniform(0.9, 1.1, N), x + rng.normal(0, 0.005, x.shape), r.copy())
     return Workload("config4: single-particle, 8192 atoms, %d x 128x128" % n_orient,
                     (I, x, r), init, T, (w0, w1), det, data, "l2")
+
+
+def config3_requests(n=512, rate=200.0, seed=3, p2d=0.6, atoms=(16, 4096),
+                     angles=(30, 180), det=(64, 512), max_iter=100, tol=1e-6):
+    """Served stream: n fitting requests with Poisson arrivals at ``rate``/s;
+    each 2D (probability p2d, isotropic atoms as config 0) or 3D (single-axis
+    tilt series, anisotropic atoms as config 2); atom count log-uniform in
+    ``atoms``, angle count uniform in ``angles``, detector cells per side
+    uniform in ``det``; data = projection + N(0, (0.01 max)^2) with a
+    per-request seed; init = truth with jittered centres and intensities;
+    L2 Newton to relative loss change ``tol`` (at most ``max_iter``)."""
+    from .serving import FitRequest
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    reqs = []
+    for i in range(n):
+        rr = np.random.default_rng([seed, i])
+        is2d = rr.uniform() < p2d
+        N = int(round(np.exp(rr.uniform(np.log(atoms[0]), np.log(atoms[1])))))
+        A = int(rr.integers(angles[0], angles[1] + 1))
+        D = int(rr.integers(det[0], det[1] + 1))
+        if is2d:
+            x = rr.uniform(-0.6, 0.6, (N, 2))
+            I = rr.uniform(0.5, 1.5, N)
+            sd = rr.uniform(0.02, 0.08, N)
+            r = (1.0 / (np.sqrt(60.0) * sd)).reshape(N, 1)
+            th = np.linspace(0, np.pi, A, endpoint=False)
+            T, w = theta_to_vec([th]), perp([th])
+            detc = (cell_centres(-1.5, 1.5, D),)
+            jit = 0.1 * sd.reshape(N, 1)
+        else:
+            x = rr.uniform(-1.0, 1.0, (N, 3))
+            I = rr.uniform(0.2, 2.0, N)
+            r = aniso_r(rr, N, 3, (10.0, 50.0), 6.0)
+            th = angle_nodes(-np.pi / 3, np.pi / 3, A)
+            T, w = theta_to_vec([th]), perp([th])
+            c = cell_centres(-1.5, 1.5, D)
+            detc = (c, c.copy())
+            jit = 0.1 / (np.sqrt(60.0) * r[:, :3].max(axis=1, keepdims=True))
+        init = (I * rr.uniform(0.9, 1.1, N), x + rr.normal(0, 1, x.shape) * jit, r.copy())
+        truth = (I, x, r)
+        reqs.append(FitRequest(i, T, w, detc, init, _data_maker(truth, [seed, i]), "l2", 0.0,
+                               max_iter=max_iter, tol=tol, arrival=float(t[i])))
+    return reqs
+
+
+def _data_maker(truth, seed):
+    def make(geom, device, stream):
+        import torch
+        from . import engine
+        R = engine.radproj(engine.DeviceAtoms(*truth, device), geom)
+        gen = torch.Generator(device=device)
+        gen.manual_seed(int(np.random.default_rng(seed).integers(1 << 62)))
+        noise = torch.randn(R.shape, generator=gen, device=device, dtype=torch.float32)
+        return (R + noise * (0.01 * R.max())).contiguous()
+    return make

@@ -170,10 +170,31 @@ int gr_atom_step(const gr_atoms *old_atom, const gr_atoms *new_atom,
  * keeping diag(r) >= 0 (GD_lib.py:504-522).  theta (n, P) is [I, x, r] per
  * atom; mask (nullable) freezes atoms with mask[j] == 0; step_norm[j] = |d|;
  * fail (nullable) flags singular blocks (their parameters are kept).
+ * I_new/x_new/r_new (all or none): the new parameters also as float32 atom
+ * arrays, ready for gr_fit_forward.
  */
 int gr_newton_solve(int dim, int iso, int n_atoms, const double *g, const double *H,
                     const double *lam, const double *theta, const unsigned char *mask,
-                    double *theta_new, double *step_norm, int *fail, void *stream);
+                    double *theta_new, double *step_norm, int *fail, float *I_new,
+                    float *x_new, float *r_new, void *stream);
+
+/*
+ * Device-side accept test of a batched Newton trial, so that a whole
+ * iteration (gr_fit_forward, gr_atom_derivs, gr_newton_solve, gr_fit_forward
+ * of the trial, gr_newton_accept) runs without a host round trip and can be
+ * replayed as a CUDA graph.  If *loss_trial <= *loss_cur: theta, the float32
+ * atoms and *loss_cur take the trial's values and lam halves; else lam grows
+ * tenfold; lam is clamped to [lam_min, lam_max].  hist[*counter] = *loss_cur
+ * and hist_accepted[*counter] = accepted (when *counter < hist_len), then
+ * ++*counter.  The same backtracking rule as the reference's Newton loop
+ * (NewtonGaussian.py:81-92), applied to all atoms at once.
+ */
+int gr_newton_accept(int dim, int iso, int n_atoms, double *loss_cur,
+                     const double *loss_trial, double *theta, const double *theta_trial,
+                     double *lam, double lam_min, double lam_max, float *I, float *x,
+                     float *r, const float *I_trial, const float *x_trial,
+                     const float *r_trial, double *hist, int *hist_accepted,
+                     int *counter, int hist_len, void *stream);
 
 /*
  * Measurement helpers (no counterpart in the reference, which has no
