@@ -61,18 +61,18 @@ def _data(C):
     return C
 
 
-def radproj(atom, Rad, R, dim):
+def radproj(atom, Rad, R, dim, psf=False):
     geom = _space_geometry(Rad.range)
-    if geom.dim != dim:
+    if dim is not None and geom.dim != dim:
         raise ValueError("this kernel module handles %dD geometry" % dim)
     atoms = _atoms(atom)
     if isinstance(R, torch.Tensor) and R.is_cuda:
         if R.dtype == torch.float32 and R.is_contiguous():
-            engine.radproj(atoms, geom, out=R)
+            engine.radproj(atoms, geom, out=R, psf=psf)
         else:
-            R.copy_(engine.radproj(atoms, geom))
+            R.copy_(engine.radproj(atoms, geom, psf=psf))
         return
-    out = engine.radproj(atoms, geom)
+    out = engine.radproj(atoms, geom, psf=psf)
     host = out.cpu().numpy()
     if isinstance(R, torch.Tensor):
         R.copy_(torch.from_numpy(host))
@@ -80,28 +80,28 @@ def radproj(atom, Rad, R, dim):
         R[...] = host.reshape(np.shape(R))
 
 
-def _derivs(atom, Rad, C, order, mode, dim):
+def _derivs(atom, Rad, C, order, mode, dim, psf=False):
     geom = _space_geometry(Rad.range)
-    if geom.dim != dim:
+    if dim is not None and geom.dim != dim:
         raise ValueError("this kernel module handles %dD geometry" % dim)
     atoms = _atoms(atom, first_only=True)
     C = _tensor(_data(C))
     o = 2 if order > 1 else 1
-    f, g, H = engine.atom_derivs(atoms, geom, mode, C.reshape(geom.shape), order=o)
+    f, g, H = engine.atom_derivs(atoms, geom, mode, C.reshape(geom.shape), order=o, psf=psf)
     f = float(f[0].item())
     Df = g[0].cpu().numpy()
     DDf = H[0].cpu().numpy() if H is not None else np.zeros((Df.size, Df.size))
     return f, Df, DDf
 
 
-def l2derivs(atom, Rad, C, order, dim):
-    return _derivs(atom, Rad, C, order, "l2_atom", dim)
+def l2derivs(atom, Rad, C, order, dim, psf=False):
+    return _derivs(atom, Rad, C, order, "l2_atom", dim, psf)
 
 
-def derivs(atom, Rad, C, order, dim):
-    return _derivs(atom, Rad, C, order, "inner", dim)
+def derivs(atom, Rad, C, order, dim, psf=False):
+    return _derivs(atom, Rad, C, order, "inner", dim, psf)
 
 
-def volproj(atom, y, u, dim):
+def volproj(atom, y, u, dim, psf=False):
     from . import volume
-    volume.volproj_into(_atoms(atom), y, u, dim)
+    volume.volproj_into(_atoms(atom), y, u, dim, psf=psf)

@@ -39,7 +39,8 @@ class EngineError(RuntimeError):
 
 EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
            "gr_fit_forward", "gr_atom_derivs", "gr_count_support", "gr_probe_ex2",
-           "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj", "gr_newton_accept")
+           "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj", "gr_newton_accept",
+           "gr_psf_radproj", "gr_psf_fit_forward", "gr_psf_atom_derivs", "gr_psf_volproj")
 
 _lock = threading.Lock()
 _lib = None
@@ -106,6 +107,15 @@ def load(build_if_missing=True):
         lib.gr_volproj.restype = ctypes.c_int
         lib.gr_volproj.argtypes = [P(GrAtoms), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p]
+        lib.gr_psf_radproj.restype = ctypes.c_int
+        lib.gr_psf_radproj.argtypes = lib.gr_radproj.argtypes
+        lib.gr_psf_fit_forward.restype = ctypes.c_int
+        lib.gr_psf_fit_forward.argtypes = lib.gr_fit_forward.argtypes
+        lib.gr_psf_atom_derivs.restype = ctypes.c_int
+        lib.gr_psf_atom_derivs.argtypes = lib.gr_atom_derivs.argtypes
+        lib.gr_psf_volproj.restype = ctypes.c_int
+        lib.gr_psf_volproj.argtypes = [P(GrAtoms), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]
         lib.gr_launch_count.restype = ctypes.c_ulonglong
         lib.gr_launch_count.argtypes = []
         _lib = lib

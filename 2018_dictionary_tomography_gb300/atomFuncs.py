@@ -33,6 +33,8 @@ class GaussTomo:
          self._proj) = self._getOps(Atoms.dim)
         self._geom = None
 
+    _psf = False
+
     def _getOps(self, dim):
         pkg = __name__.rsplit(".", 1)[0]
         if dim == 2:
@@ -76,7 +78,7 @@ class GaussTomo:
             np.ascontiguousarray(C, dtype=np.float32))
         f, g, H = engine.atom_derivs(self.device_atoms(atoms), self.geometry, mode,
                                      field.reshape(self.geometry.shape),
-                                     order=2 if order > 1 else 1)
+                                     order=2 if order > 1 else 1, psf=self._psf)
         f = f.cpu().numpy().reshape(-1, 1)
         df = g.cpu().numpy()
         if order == 1:
@@ -105,6 +107,8 @@ class GaussTomo:
 class SingleParticleGaussTomo(GaussTomo):
     """GaussTomo with the pixel-integrated point-spread kernels
     (atomFuncs.py:161-172)."""
+
+    _psf = True
 
     def _getOps(self, dim):
         if dim not in (2, 3):

@@ -71,8 +71,8 @@ size_t gr_workspace_bytes(int op, const gr_atoms *atoms, const gr_geometry *geom
   return 0;
 }
 
-int gr_radproj(const gr_atoms *atoms, const gr_geometry *geom, float *R,
-               void *workspace, size_t workspace_bytes, void *stream) {
+static int radproj_impl(const gr_atoms *atoms, const gr_geometry *geom, float *R,
+                        void *workspace, size_t workspace_bytes, void *stream, int psf) {
   Atoms at;
   Geom g;
   int st;
@@ -81,14 +81,25 @@ int gr_radproj(const gr_atoms *atoms, const gr_geometry *geom, float *R,
   ProjOut o{};
   o.R = R;
   o.epilogue = kEpiNone;
+  o.psf = psf;
   return launch_project(at, g, o, nullptr, workspace, workspace_bytes,
                         static_cast<cudaStream_t>(stream));
 }
 
-int gr_fit_forward(const gr_atoms *atoms, const gr_geometry *geom, int fit,
-                   const float *data, float background, float *R, float *alpha,
-                   float *beta, double *loss, void *workspace,
-                   size_t workspace_bytes, void *stream) {
+int gr_radproj(const gr_atoms *atoms, const gr_geometry *geom, float *R,
+               void *workspace, size_t workspace_bytes, void *stream) {
+  return radproj_impl(atoms, geom, R, workspace, workspace_bytes, stream, 0);
+}
+
+int gr_psf_radproj(const gr_atoms *atoms, const gr_geometry *geom, float *R,
+                   void *workspace, size_t workspace_bytes, void *stream) {
+  return radproj_impl(atoms, geom, R, workspace, workspace_bytes, stream, 1);
+}
+
+static int fit_forward_impl(const gr_atoms *atoms, const gr_geometry *geom, int fit,
+                            const float *data, float background, float *R, float *alpha,
+                            float *beta, double *loss, void *workspace,
+                            size_t workspace_bytes, void *stream, int psf) {
   Atoms at;
   Geom g;
   int st;
@@ -104,14 +115,31 @@ int gr_fit_forward(const gr_atoms *atoms, const gr_geometry *geom, int fit,
   o.bg = background;
   o.alpha = alpha;
   o.beta = beta;
+  o.psf = psf;
   return launch_project(at, g, o, loss, workspace, workspace_bytes,
                         static_cast<cudaStream_t>(stream));
 }
 
-int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
-                   const float *field, const float *beta_field, float beta_const,
-                   int order, double *f, double *g_out, double *H, void *workspace,
+int gr_fit_forward(const gr_atoms *atoms, const gr_geometry *geom, int fit,
+                   const float *data, float background, float *R, float *alpha,
+                   float *beta, double *loss, void *workspace,
                    size_t workspace_bytes, void *stream) {
+  return fit_forward_impl(atoms, geom, fit, data, background, R, alpha, beta, loss,
+                          workspace, workspace_bytes, stream, 0);
+}
+
+int gr_psf_fit_forward(const gr_atoms *atoms, const gr_geometry *geom, int fit,
+                       const float *data, float background, float *R, float *alpha,
+                       float *beta, double *loss, void *workspace,
+                       size_t workspace_bytes, void *stream) {
+  return fit_forward_impl(atoms, geom, fit, data, background, R, alpha, beta, loss,
+                          workspace, workspace_bytes, stream, 1);
+}
+
+static int atom_derivs_impl(const gr_atoms *atoms, const gr_geometry *geom, int mode,
+                            const float *field, const float *beta_field, float beta_const,
+                            int order, double *f, double *g_out, double *H, void *workspace,
+                            size_t workspace_bytes, void *stream, int psf) {
   Atoms at;
   Geom g;
   int st;
@@ -126,9 +154,26 @@ int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
   in.alpha = field;
   in.beta = mode == GR_MODE_FIELD ? beta_field : nullptr;
   in.beta_const = mode == GR_MODE_FIELD ? beta_const : (mode == GR_MODE_L2_ATOM ? 1.f : 0.f);
+  in.psf = psf;
   DerivOut out{f, g_out, H};
   return launch_derivs(at, g, in, out, workspace, workspace_bytes,
                        static_cast<cudaStream_t>(stream));
+}
+
+int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
+                   const float *field, const float *beta_field, float beta_const,
+                   int order, double *f, double *g_out, double *H, void *workspace,
+                   size_t workspace_bytes, void *stream) {
+  return atom_derivs_impl(atoms, geom, mode, field, beta_field, beta_const, order, f, g_out,
+                          H, workspace, workspace_bytes, stream, 0);
+}
+
+int gr_psf_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
+                       const float *field, const float *beta_field, float beta_const,
+                       int order, double *f, double *g_out, double *H, void *workspace,
+                       size_t workspace_bytes, void *stream) {
+  return atom_derivs_impl(atoms, geom, mode, field, beta_field, beta_const, order, f, g_out,
+                          H, workspace, workspace_bytes, stream, 1);
 }
 
 int gr_atom_step(const gr_atoms *old_atom, const gr_atoms *new_atom,
@@ -182,8 +227,9 @@ int gr_newton_accept(int dim, int iso, int n_atoms, double *loss_cur,
                               counter, hist_len, static_cast<cudaStream_t>(stream));
 }
 
-int gr_volproj(const gr_atoms *atoms, int dim, const int *n_vox, const float *const *coords,
-               float *u, void *stream) {
+static int volproj_impl(const gr_atoms *atoms, int dim, const int *n_vox,
+                        const float *const *coords, float *u, void *stream, int psf,
+                        float s) {
   if (!atoms || !n_vox || !coords || !u || (dim != 2 && dim != 3)) return GR_ERR_ARG;
   if (atoms->n_atoms < 0 || (atoms->n_atoms > 0 && (!atoms->I || !atoms->x || !atoms->r)))
     return GR_ERR_ARG;
@@ -195,7 +241,19 @@ int gr_volproj(const gr_atoms *atoms, int dim, const int *n_vox, const float *co
   at.x = atoms->x;
   at.r = atoms->r;
   at.r_iso = atoms->r_iso ? 1 : 0;
-  return launch_volproj(at, dim, n_vox, coords, u, static_cast<cudaStream_t>(stream));
+  return launch_volproj(at, dim, n_vox, coords, u, psf, s, static_cast<cudaStream_t>(stream));
+}
+
+int gr_volproj(const gr_atoms *atoms, int dim, const int *n_vox, const float *const *coords,
+               float *u, void *stream) {
+  return volproj_impl(atoms, dim, n_vox, coords, u, stream, 0, 0.f);
+}
+
+int gr_psf_volproj(const gr_atoms *atoms, int dim, const int *n_vox,
+                   const float *const *coords, float voxel_half_width, float *u,
+                   void *stream) {
+  if (!(voxel_half_width > 0.f)) return GR_ERR_ARG;
+  return volproj_impl(atoms, dim, n_vox, coords, u, stream, 1, voxel_half_width);
 }
 
 int gr_count_support(const gr_atoms *atoms, const gr_geometry *geom,

@@ -32,6 +32,7 @@ struct ProjOut {
   float *alpha;        // first-order weight field (nullable)
   float *beta;         // Gauss-Newton weight field (KL, nullable)
   double *loss_part;   // per-(angle, tile) loss partials (set by the launcher)
+  int psf;             // 1: pixel-integrated values (point-spread operator)
 };
 
 // ---- derivatives -----------------------------------------------------------
@@ -47,6 +48,7 @@ struct DerivIn {
   const float *alpha;    // field, or C for kModeL2Atom / kModeInner
   const float *beta;     // field (nullable)
   float beta_const;      // used when beta == nullptr
+  int psf;               // 1: pixel-integrated operator
 };
 
 struct DerivOut {
@@ -97,7 +99,7 @@ int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
                          int *hist_acc, int *counter, int hist_len, cudaStream_t stream);
 
 int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y,
-                   float *u, cudaStream_t stream);
+                   float *u, int psf, float s, cudaStream_t stream);
 
 // host-side count of kernels launched by this library
 void note_launches(int n);

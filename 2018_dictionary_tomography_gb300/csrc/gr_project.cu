@@ -353,6 +353,219 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   }
 }
 
+// ---- pixel-integrated operator: binning and projection -------------------
+template <int K>
+__global__ void __launch_bounds__(128) gr_psf_bin_kernel(Atoms at, Geom g, TileCfg tc,
+                                                         uint32_t *bitmap, int W, float s) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int a = blockIdx.y;
+  if (j >= at.n) return;
+  Frame<K> f;
+  load_frame<K>(g.frames, a, f);
+  Pair<K> p;
+  const bool ok = pair_setup<K>(at, j, f, g, p);
+  PsfPair<K> q;
+  psf_setup<K>(at, j, g, p, ok, s, q);
+  if (q.lo[0] > q.hi[0]) return;
+  const uint32_t bit = 1u << (j & 31);
+  const size_t base = (size_t)a * tc.ntiles;
+  const int wj = j >> 5;
+  if constexpr (K == 1) {
+    for (int t = q.lo[0] / tc.t0; t <= q.hi[0] / tc.t0; ++t)
+      atomicOr(bitmap + (base + t) * W + wj, bit);
+  } else {
+    if (q.lo[1] > q.hi[1]) return;
+    for (int tr = q.lo[0] / tc.t0; tr <= q.hi[0] / tc.t0; ++tr)
+      for (int tcix = q.lo[1] / tc.t1; tcix <= q.hi[1] / tc.t1; ++tcix)
+        atomicOr(bitmap + (base + (size_t)tr * tc.nt1 + tcix) * W + wj, bit);
+  }
+}
+
+struct PsfLite {
+  float qh0, ql0, qh1, ql1, G0, G1, G2, l2amp, sgn, rr, total;
+  int lo0, hi0, lo1, hi1;
+};
+
+__device__ __forceinline__ PsfLite shfl_psf(const PsfLite &v, int src) {
+  PsfLite o;
+  const unsigned m = 0xffffffffu;
+  o.qh0 = __shfl_sync(m, v.qh0, src);
+  o.ql0 = __shfl_sync(m, v.ql0, src);
+  o.qh1 = __shfl_sync(m, v.qh1, src);
+  o.ql1 = __shfl_sync(m, v.ql1, src);
+  o.G0 = __shfl_sync(m, v.G0, src);
+  o.G1 = __shfl_sync(m, v.G1, src);
+  o.G2 = __shfl_sync(m, v.G2, src);
+  o.l2amp = __shfl_sync(m, v.l2amp, src);
+  o.sgn = __shfl_sync(m, v.sgn, src);
+  o.rr = __shfl_sync(m, v.rr, src);
+  o.total = __shfl_sync(m, v.total, src);
+  o.lo0 = __shfl_sync(m, v.lo0, src);
+  o.hi0 = __shfl_sync(m, v.hi0, src);
+  o.lo1 = __shfl_sync(m, v.lo1, src);
+  o.hi1 = __shfl_sync(m, v.hi1, src);
+  return o;
+}
+
+// Warp per (angle, tile), atoms in index order from the bitmap, lanes spread
+// over each atom's cell box clipped to the tile, each cell's value by the
+// quadrature rule; compensated shared-memory cell sums (deterministic).
+template <int K>
+__global__ void __launch_bounds__(kProjWarps * 32)
+    gr_psf_project_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap, int W,
+                          float s, ProjOut out) {
+  extern __shared__ float smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * kProjWarps + warp;
+  if (item >= g.n_angles * tc.ntiles) return;
+  const int cells = tc.t0 * tc.t1;
+  float *acc = smem + (size_t)warp * kProjWarpFloats;
+  float *cmp = acc + kTileCells;
+  float *pc0 = cmp + kTileCells;
+  float *pc1 = pc0 + 64;
+  int *list = reinterpret_cast<int *>(pc1 + kTileDim1);
+  const int a = item / tc.ntiles, t = item - a * tc.ntiles;
+  const int tr = t / tc.nt1, tcix = t - tr * tc.nt1;
+  const int r0 = tr * tc.t0, c0 = tcix * tc.t1;
+  const int D0 = g.ax[0].n, D1 = (K == 1) ? 1 : g.ax[1].n;
+  for (int e = lane; e < cells; e += 32) {
+    acc[e] = 0.f;
+    cmp[e] = 0.f;
+  }
+  for (int e = lane; e < tc.t0; e += 32)
+    pc0[e] = (r0 + e < D0) ? g.ax[0].coords[r0 + e] : 0.f;
+  if constexpr (K == 2)
+    for (int e = lane; e < tc.t1; e += 32)
+      pc1[e] = (c0 + e < D1) ? g.ax[1].coords[c0 + e] : 0.f;
+  Frame<K> f;
+  load_frame<K>(g.frames, a, f);
+  __syncwarp();
+  const uint32_t *words = bitmap + (size_t)item * W;
+  for (int wb = 0; wb < W; wb += kListWords) {
+    const int wi = wb + (lane < kListWords ? lane : 0);
+    uint32_t wd = (lane < kListWords && wi < W) ? words[wi] : 0u;
+    int cnt = __popc(wd), incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int pos = incl - cnt;
+    while (wd) {
+      const int b = __ffs(wd) - 1;
+      list[pos++] = (wi << 5) + b;
+      wd &= wd - 1;
+    }
+    __syncwarp();
+    for (int bs = 0; bs < total; bs += 32) {
+      const int idx = bs + lane;
+      PsfLite mine{};
+      mine.lo0 = 1;
+      mine.hi0 = 0;
+      mine.lo1 = 1;
+      mine.hi1 = 0;
+      if (idx < total) {
+        const int j = list[idx];
+        Pair<K> p;
+        const bool ok = pair_setup<K>(at, j, f, g, p);
+        PsfPair<K> q;
+        psf_setup<K>(at, j, g, p, ok, s, q);
+        mine.qh0 = p.qh[0];
+        mine.ql0 = p.ql[0];
+        mine.G0 = p.G[0];
+        mine.G1 = p.G[1];
+        mine.G2 = p.G[2];
+        mine.l2amp = p.l2amp;
+        mine.sgn = p.sgn;
+        mine.rr = q.rr;
+        mine.total = q.total;
+        mine.lo0 = max(q.lo[0], r0);
+        mine.hi0 = min(q.hi[0], r0 + tc.t0 - 1);
+        if constexpr (K == 2) {
+          mine.qh1 = p.qh[1];
+          mine.ql1 = p.ql[1];
+          mine.lo1 = max(q.lo[1], c0);
+          mine.hi1 = min(q.hi[1], c0 + tc.t1 - 1);
+        } else {
+          mine.lo1 = 0;
+          mine.hi1 = 0;
+        }
+      }
+      const int nb = min(32, total - bs);
+      for (int s2 = 0; s2 < nb; ++s2) {
+        const PsfLite qq = shfl_psf(mine, s2);
+        if (qq.lo0 > qq.hi0 || qq.lo1 > qq.hi1) continue;
+        Pair<K> p;
+        p.qh[0] = qq.qh0;
+        p.ql[0] = qq.ql0;
+        p.G[0] = qq.G0;
+        p.G[1] = qq.G1;
+        p.G[2] = qq.G2;
+        p.l2amp = qq.l2amp;
+        if constexpr (K == 2) {
+          p.qh[1] = qq.qh1;
+          p.ql[1] = qq.ql1;
+        }
+        PsfPair<K> q;
+        q.rr = qq.rr;
+        q.total = qq.total;
+        const int bw = qq.hi1 - qq.lo1 + 1;
+        const int ncell = (qq.hi0 - qq.lo0 + 1) * bw;
+        const float inv_bw = 1.f / (float)bw;
+        for (int e = lane; e < ncell; e += 32) {
+          const int rr_ = (int)(((float)e + 0.5f) * inv_bw);
+          const int cc = e - rr_ * bw;
+          const int lr = qq.lo0 - r0 + rr_;
+          const int lc = (K == 2) ? (qq.lo1 - c0 + cc) : 0;
+          float dc[K], base[K], step[K];
+          dc[0] = (pc0[lr] - qq.qh0) - qq.ql0;
+          if constexpr (K == 2) dc[1] = (pc1[lc] - qq.qh1) - qq.ql1;
+          const int kind = psf_cell_kind<K>(q, dc, s, base, step);
+          if (kind == 0) continue;
+          const float v = kind == 1 ? qq.total : qq.sgn * psf_quadrature<K>(p, base, step);
+          const int ci = lr * tc.t1 + lc;
+          const float s0 = acc[ci];
+          const float tt = s0 + v;
+          cmp[ci] += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
+          acc[ci] = tt;
+        }
+        __syncwarp();
+      }
+    }
+  }
+  __syncwarp();
+  float lsum = 0.f, lcmp = 0.f;
+  for (int e = lane; e < cells; e += 32) {
+    const int lr = e / tc.t1, lc = e - lr * tc.t1;
+    const int row = r0 + lr, col = c0 + lc;
+    if (row >= D0 || col >= D1) continue;
+    const float v = acc[e] + cmp[e];
+    const size_t gi = ((size_t)a * D0 + row) * D1 + col;
+    if (out.R) out.R[gi] = v;
+    float l = 0.f;
+    if (out.epilogue == kEpiL2) {
+      const float res = v - out.data[gi];
+      if (out.alpha) out.alpha[gi] = res;
+      l = 0.5f * res * res;
+    } else if (out.epilogue == kEpiKL) {
+      const float fo = out.data[gi];
+      const float gg = v + out.bg;
+      const float ig = 1.f / gg;
+      if (out.alpha) out.alpha[gi] = 1.f - fo * ig;
+      if (out.beta) out.beta[gi] = fo * ig * ig;
+      l = kl_term(fo, gg);
+    }
+    const float tt = lsum + l;
+    lcmp += (fabsf(lsum) >= fabsf(l)) ? ((lsum - tt) + l) : ((l - tt) + lsum);
+    lsum = tt;
+  }
+  if (out.loss_part) {
+    double d = warp_sum_d((double)lsum + (double)lcmp);
+    if (lane == 0) out.loss_part[item] = d;
+  }
+}
+
 __global__ void gr_loss_finalize_kernel(const double *part, int n, double *out) {
   __shared__ double sh[256];
   double s = 0.0;
@@ -408,14 +621,20 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   double *loss_part = reinterpret_cast<double *>(wp);
   ProjOut o = o_in;
   o.loss_part = loss_out ? loss_part : nullptr;
+  // half-width of the (square) cells of the pixel-integrated operator
+  const float psf_s = 0.5f / g.ax[0].inv_step;
   if (W > 0) {
     if (cudaMemsetAsync(bitmap, 0, items * W * sizeof(uint32_t), stream) != cudaSuccess)
       return kErrLaunch;
     dim3 bgrid((at.n + 127) / 128, g.n_angles);
-    if (K == 1)
+    if (o.psf) {
+      if (K == 1) gr_psf_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, psf_s);
+      else gr_psf_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, psf_s);
+    } else if (K == 1) {
       gr_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W);
-    else
+    } else {
       gr_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W);
+    }
     note_launches(1);
   }
   const int blocks = (int)((items + kProjWarps - 1) / kProjWarps);
@@ -423,7 +642,12 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   // smem (kProjWarps * kProjWarpFloats floats) stays below the 48 KB that
   // needs no opt-in, so no function attribute is set (safe under capture)
   static_assert(kProjWarps * kProjWarpFloats * sizeof(float) <= 48 * 1024, "smem");
-  if (K == 1) {
+  if (o.psf) {
+    if (K == 1)
+      gr_psf_project_kernel<1><<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, psf_s, o);
+    else
+      gr_psf_project_kernel<2><<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, psf_s, o);
+  } else if (K == 1) {
     gr_project1d_kernel<true><<<blocks, kProjWarps * 32, 0, stream>>>(at, g, tc, bitmap, W, o);
   } else {
     gr_project_kernel<2, true><<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o);

@@ -21,9 +21,53 @@ struct VolGrid {
   const float *y[3];
 };
 
+// Voxel-integrated value of one atom (point_spread_functions.py __if2 :425,
+// __if3 :459): 11^D-point rule over the voxel of half-width s clipped to the
+// box +-rr (rr = 1 / min diag r) around the atom, points at lo + t (hi-lo)/10
+// (t = 1..11), no cut-off; total mass inside, zero beyond rr + s.
 template <int D>
+__device__ __forceinline__ float psf_voxel(float Iv, const float *X, const float (&M)[3][3],
+                                           float rr, float total, float s) {
+  float n2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) n2 = fmaf(X[i], X[i], n2);
+  const float n = sqrtf(n2);
+  if (n + rr < s) return total;
+  if (n - rr > s) return 0.f;
+  float lo[3], st[3];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    const float l = fmaxf(X[i] - rr, -s), h = fminf(X[i] + rr, s);
+    st[i] = 0.1f * (h - l);
+    lo[i] = l;
+  }
+  float sum = 0.f;
+  for (int a = 1; a <= 11; ++a) {
+    const float Y0 = fmaf((float)a, st[0], lo[0]) - X[0];
+    for (int b = 1; b <= 11; ++b) {
+      const float Y1 = fmaf((float)b, st[1], lo[1]) - X[1];
+      if (D == 2) {
+        const float p0 = M[0][0] * Y0 + M[0][1] * Y1, p1 = M[1][1] * Y1;
+        sum += ex2_approx((p0 * p0 + p1 * p1) * kNegThirtyLog2e);
+      } else {
+#pragma unroll
+        for (int c = 1; c <= 11; ++c) {
+          const float Y2 = fmaf((float)c, st[2], lo[2]) - X[2];
+          const float p0 = M[0][0] * Y0 + M[0][1] * Y1 + M[0][2] * Y2;
+          const float p1 = M[1][1] * Y1 + M[1][2] * Y2, p2 = M[2][2] * Y2;
+          sum += ex2_approx((p0 * p0 + p1 * p1 + p2 * p2) * kNegThirtyLog2e);
+        }
+      }
+    }
+  }
+  constexpr float kNorm = 3.0901936161855166f;  // sqrt(30 / pi)
+  return D == 2 ? Iv * kNorm * sum * (100.f * st[0] * st[1] / 121.f)
+                : Iv * kNorm * sum * (1000.f * st[0] * st[1] * st[2] / 1331.f);
+}
+
+template <int D, bool PSF>
 __global__ void __launch_bounds__(kVolThreads)
-    gr_volproj_kernel(Atoms at, VolGrid vg, int t0, int t1, int t2, float *u) {
+    gr_volproj_kernel(Atoms at, VolGrid vg, int t0, int t1, int t2, float s, float *u) {
   __shared__ float sI[kVolThreads], sx[3][kVolThreads], sr[6][kVolThreads];
   __shared__ int wcount[kVolThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -94,12 +138,16 @@ __global__ void __launch_bounds__(kVolThreads)
           }
         }
         hit = true;
+        float rr = M[0][0];
+#pragma unroll
+        for (int i = 1; i < D; ++i) rr = fminf(rr, M[i][i]);
+        rr = 1.f / rr;
 #pragma unroll
         for (int i = 0; i < D; ++i) {
           float e = 0.f;
 #pragma unroll
           for (int k = 0; k < D; ++k) e += inv[i][k] * inv[i][k];
-          e = sqrtf(e) * 1.0001f;
+          e = PSF ? (rr + s) * 1.0001f : sqrtf(e) * 1.0001f;
           hit = hit && (xj[i] + e >= blo[i]) && (xj[i] - e <= bhi[i]);
         }
       }
@@ -143,7 +191,22 @@ __global__ void __launch_bounds__(kVolThreads)
           const float d = sr[2][k] * Y2;
           nn = a * a + c * c + d * d;
         }
-        if (nn <= 1.f) acc += sI[k] * ex2_approx(nn * kNegThirtyLog2e);
+        if (!PSF && nn <= 1.f) acc += sI[k] * ex2_approx(nn * kNegThirtyLog2e);
+        if (PSF) {
+          float Mk[3][3] = {{sr[0][k], D == 2 ? sr[2][k] : sr[3][k], D == 2 ? 0.f : sr[5][k]},
+                            {0.f, sr[1][k], D == 2 ? 0.f : sr[4][k]},
+                            {0.f, 0.f, D == 2 ? 0.f : sr[2][k]}};
+          float X[3] = {sx[0][k] - yv[0], sx[1][k] - yv[1], D == 3 ? sx[2][k] - yv[2] : 0.f};
+          float mn = Mk[0][0];
+#pragma unroll
+          for (int i = 1; i < D; ++i) mn = fminf(mn, Mk[i][i]);
+          const float rr = 1.f / mn;
+          constexpr float kNormV = 3.0901936161855166f;
+          const float Iv = sI[k] / kNormV;
+          const float det = D == 2 ? Mk[0][0] * Mk[1][1] : Mk[0][0] * Mk[1][1] * Mk[2][2];
+          const float total = D == 2 ? Iv / det * 0.32360019f : Iv / det * 0.10471976f;
+          acc += psf_voxel<D>(Iv, X, Mk, rr, total, s);
+        }
       }
     }
     __syncthreads();
@@ -156,7 +219,7 @@ __global__ void __launch_bounds__(kVolThreads)
 }
 
 int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y,
-                   float *u, cudaStream_t stream) {
+                   float *u, int psf, float s, cudaStream_t stream) {
   VolGrid vg;
   for (int k = 0; k < 3; ++k) {
     vg.n[k] = k < dim ? n[k] : 1;
@@ -165,12 +228,14 @@ int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y
   if (dim == 2) {
     const int t0 = 16, t1 = 16;
     const int blocks = ((vg.n[0] + t0 - 1) / t0) * ((vg.n[1] + t1 - 1) / t1);
-    gr_volproj_kernel<2><<<blocks, kVolThreads, 0, stream>>>(at, vg, t0, t1, 1, u);
+    if (psf) gr_volproj_kernel<2, true><<<blocks, kVolThreads, 0, stream>>>(at, vg, t0, t1, 1, s, u);
+    else gr_volproj_kernel<2, false><<<blocks, kVolThreads, 0, stream>>>(at, vg, t0, t1, 1, s, u);
   } else {
     const int t0 = 4, t1 = 8, t2 = 8;
     const int blocks = ((vg.n[0] + t0 - 1) / t0) * ((vg.n[1] + t1 - 1) / t1) *
                        ((vg.n[2] + t2 - 1) / t2);
-    gr_volproj_kernel<3><<<blocks, kVolThreads, 0, stream>>>(at, vg, t0, t1, t2, u);
+    if (psf) gr_volproj_kernel<3, true><<<blocks, kVolThreads, 0, stream>>>(at, vg, t0, t1, t2, s, u);
+    else gr_volproj_kernel<3, false><<<blocks, kVolThreads, 0, stream>>>(at, vg, t0, t1, t2, s, u);
   }
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;

@@ -96,22 +96,24 @@ def _ws_for(op, atoms, geom):
     return workspace(n, geom.device), n
 
 
-def radproj(atoms, geom, out=None):
-    """Forward projection R (A, D0[, D1]) float32 on the device."""
+def radproj(atoms, geom, out=None, psf=False):
+    """Forward projection R (A, D0[, D1]) float32 on the device; psf=True
+    gives the pixel-integrated (single-particle) projection."""
     _check_dims(atoms, geom)
     if out is None:
         out = torch.empty(geom.shape, dtype=torch.float32, device=geom.device)
     if tuple(out.shape) != tuple(geom.shape) or out.dtype != torch.float32 or not out.is_contiguous():
         raise ValueError("output must be a contiguous float32 tensor of shape %s" % (geom.shape,))
     ws, n = _ws_for(_lib.GR_OP_PROJECT, atoms, geom)
-    st = _lib.load().gr_radproj(ctypes.byref(atoms.struct), ctypes.byref(geom.struct),
-                                out.data_ptr(), ws.data_ptr(), n, _stream_handle(geom.device))
+    fn = _lib.load().gr_psf_radproj if psf else _lib.load().gr_radproj
+    st = fn(ctypes.byref(atoms.struct), ctypes.byref(geom.struct),
+            out.data_ptr(), ws.data_ptr(), n, _stream_handle(geom.device))
     _lib.check(st, "gr_radproj")
     return out
 
 
 def fit_forward(atoms, geom, data, fit="l2", background=0.0, want_R=False,
-                want_fields=True):
+                want_fields=True, psf=False):
     """Projection fused with an L2 or KL fit.
 
     Returns dict with 'loss' (0-d float64 device tensor), 'alpha', 'beta'
@@ -130,7 +132,8 @@ def fit_forward(atoms, geom, data, fit="l2", background=0.0, want_R=False,
             if (want_fields and fit == "kl") else None)
     ws, n = _ws_for(_lib.GR_OP_PROJECT, atoms, geom)
     p = lambda t: None if t is None else t.data_ptr()
-    st = _lib.load().gr_fit_forward(
+    fn = _lib.load().gr_psf_fit_forward if psf else _lib.load().gr_fit_forward
+    st = fn(
         ctypes.byref(atoms.struct), ctypes.byref(geom.struct), code, data.data_ptr(),
         float(background), p(R), p(alpha), p(beta), out["loss"].data_ptr(),
         ws.data_ptr(), n, _stream_handle(dev))
@@ -143,7 +146,8 @@ MODES = {"field": _lib.GR_MODE_FIELD, "l2_atom": _lib.GR_MODE_L2_ATOM,
          "inner": _lib.GR_MODE_INNER}
 
 
-def atom_derivs(atoms, geom, mode, field, beta_field=None, beta_const=1.0, order=2):
+def atom_derivs(atoms, geom, mode, field, beta_field=None, beta_const=1.0, order=2,
+                psf=False):
     """Per-atom value (N,), gradient (N, P) and Hessian (N, P, P), float64.
 
     mode 'inner' (field = C): derivatives of <R_j, C>;
@@ -167,7 +171,8 @@ def atom_derivs(atoms, geom, mode, field, beta_field=None, beta_const=1.0, order
         return f, g, H
     op = _lib.GR_OP_DERIVS_1 if order == 1 else _lib.GR_OP_DERIVS_2
     ws, n = _ws_for(op, atoms, geom)
-    st = _lib.load().gr_atom_derivs(
+    fn = _lib.load().gr_psf_atom_derivs if psf else _lib.load().gr_atom_derivs
+    st = fn(
         ctypes.byref(atoms.struct), ctypes.byref(geom.struct), MODES[mode],
         field.data_ptr(), None if beta_field is None else beta_field.data_ptr(),
         float(beta_const), int(order), f.data_ptr(), g.data_ptr(),
@@ -268,17 +273,20 @@ def _ptr(t):
     return None if t is None else t.data_ptr()
 
 
-def fit_forward_into(atoms, geom, data, fit, background, R, alpha, beta, loss, ws):
+def fit_forward_into(atoms, geom, data, fit, background, R, alpha, beta, loss, ws, psf=False):
     code = {"l2": _lib.GR_FIT_L2, "kl": _lib.GR_FIT_KL}[fit]
-    st = _lib.load().gr_fit_forward(
+    fn = _lib.load().gr_psf_fit_forward if psf else _lib.load().gr_fit_forward
+    st = fn(
         ctypes.byref(atoms.struct), ctypes.byref(geom.struct), code, data.data_ptr(),
         float(background), _ptr(R), _ptr(alpha), _ptr(beta), _ptr(loss), ws.data_ptr(),
         ws.numel(), _stream_handle(geom.device))
     _lib.check(st, "gr_fit_forward")
 
 
-def atom_derivs_into(atoms, geom, mode, field, beta_field, beta_const, order, f, g, H, ws):
-    st = _lib.load().gr_atom_derivs(
+def atom_derivs_into(atoms, geom, mode, field, beta_field, beta_const, order, f, g, H, ws,
+                     psf=False):
+    fn = _lib.load().gr_psf_atom_derivs if psf else _lib.load().gr_atom_derivs
+    st = fn(
         ctypes.byref(atoms.struct), ctypes.byref(geom.struct), MODES[mode], field.data_ptr(),
         _ptr(beta_field), float(beta_const), int(order), f.data_ptr(), g.data_ptr(), _ptr(H),
         ws.data_ptr(), ws.numel(), _stream_handle(geom.device))

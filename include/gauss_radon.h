@@ -149,6 +149,33 @@ int gr_volproj(const gr_atoms *atoms, int dim, const int *n_vox, const float *co
                float *u, void *stream);
 
 /*
+ * Pixel-integrated ("point spread") operator: the same calls for the
+ * single-particle kernel module (GaussDictCode/bin/point_spread_functions.py,
+ * selected by SingleParticleGaussTomo._getOps, atomFuncs.py:168-172): RadProj
+ * (:371), L2derivs_RadProj (:1077), derivs_RadProj (:1314), VolProj (:168).
+ * A cell's value is the integral of the projection over the square cell
+ * (half-width s = spacing/2 of detector axis 0) by the reference's 11-point
+ * (2D) / 11 x 11 (3D) rule over the cell clipped to +-1/min(diag r) around the
+ * atom; cells holding a whole atom get its total mass (with zero
+ * derivatives, as the reference).  Arguments and outputs as gr_radproj,
+ * gr_fit_forward and gr_atom_derivs.  gr_psf_volproj integrates over voxels
+ * of half-width voxel_half_width (11^dim rule, __if2/__if3 :425-495).
+ */
+int gr_psf_radproj(const gr_atoms *atoms, const gr_geometry *geom, float *R,
+                   void *workspace, size_t workspace_bytes, void *stream);
+int gr_psf_fit_forward(const gr_atoms *atoms, const gr_geometry *geom, int fit,
+                       const float *data, float background, float *R, float *alpha,
+                       float *beta, double *loss, void *workspace,
+                       size_t workspace_bytes, void *stream);
+int gr_psf_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
+                       const float *field, const float *beta_field, float beta_const,
+                       int order, double *f, double *g, double *H, void *workspace,
+                       size_t workspace_bytes, void *stream);
+int gr_psf_volproj(const gr_atoms *atoms, int dim, const int *n_vox,
+                   const float *const *coords, float voxel_half_width, float *u,
+                   void *stream);
+
+/*
  * One atom of a fit moves from old_atom to new_atom (both n_atoms = 1, same
  * r_iso).  The sinogram R changes by R(new) - R(old) inside the union of the
  * two supports.  apply = 0 (trial): *dloss = change of the data fit (L2:

@@ -38,6 +38,9 @@ def lib():
             getattr(_lib, "or_point_derivs" + sfx).restype = ctypes.c_int
             getattr(_lib, "or_volproj" + sfx).restype = ctypes.c_int
             getattr(_lib, "or_count_support" + sfx).restype = ctypes.c_longlong
+            getattr(_lib, "or_psf_radproj" + sfx).restype = ctypes.c_int
+            getattr(_lib, "or_psf_atom_derivs" + sfx).restype = ctypes.c_int
+            getattr(_lib, "or_psf_volproj" + sfx).restype = ctypes.c_int
     return _lib
 
 
@@ -295,3 +298,66 @@ def kl_fields(f, R, b):
     f = np.asarray(f, dtype=np.float64)
     g = np.asarray(R, dtype=np.float64) + b
     return 1.0 - f / g, f / (g * g)
+
+
+# --------------------------------------------------------------------------
+# single-particle (pixel-integrated) operator
+# --------------------------------------------------------------------------
+def psf_radproj(I, x, r, geom, dtype=np.float64, nthreads=None):
+    """Pixel-integrated projection (point_spread_functions.RadProj)."""
+    dim = geom.dim
+    g = geom.cast(dtype)
+    I = np.ascontiguousarray(I, dtype=dtype).reshape(-1)
+    x = np.ascontiguousarray(x, dtype=dtype).reshape(-1, dim)
+    r = np.ascontiguousarray(to_aniso(r, dim), dtype=dtype)
+    out = np.zeros(geom.shape, dtype=dtype)
+    fn = lib().or_psf_radproj_f64 if dtype == np.float64 else lib().or_psf_radproj_f32
+    D1 = 1 if dim == 2 else g.p1.size
+    rc = fn(g.gm, I.size, _p(I), _p(x), _p(r), g.A, _p(g.T), _p(g.w0), _p(g.w1),
+            g.p0.size, _p(g.p0), D1, _p(g.p1), _p(out), _nthreads(nthreads))
+    assert rc == 0
+    return out
+
+
+def psf_atom_derivs(kind, I, x, r, geom, C, order=2, nthreads=None):
+    """Single-atom derivatives of the pixel-integrated projection:
+    kind "l2" (L2derivs_RadProj) or "ip" (derivs_RadProj); isotropic r uses
+    the exact chain rule."""
+    dim = geom.dim
+    r_in = np.asarray(r, dtype=np.float64).reshape(-1)
+    iso = r_in.size == 1
+    ra = np.ascontiguousarray(to_aniso(r_in.reshape(1, -1), dim).reshape(-1))
+    I = np.ascontiguousarray(np.reshape(I, -1)[:1], dtype=np.float64)
+    x = np.ascontiguousarray(np.reshape(x, -1)[:dim], dtype=np.float64)
+    C = np.ascontiguousarray(C, dtype=np.float64).reshape(geom.shape)
+    _, P = _dims(dim)
+    f = np.zeros(1)
+    Df = np.zeros(P)
+    DDf = np.zeros(P * P)
+    D1 = 1 if dim == 2 else geom.p1.size
+    rc = lib().or_psf_atom_derivs_f64(0 if kind == "l2" else 1, geom.gm, _p(I), _p(x), _p(ra),
+                                      geom.A, _p(geom.T), _p(geom.w0), _p(geom.w1),
+                                      geom.p0.size, _p(geom.p0), D1, _p(geom.p1), _p(C),
+                                      int(order), _p(f), _p(Df), _p(DDf), _nthreads(nthreads))
+    assert rc == 0
+    DDf = DDf.reshape(P, P)
+    if iso:
+        Df, DDf = collapse_iso(Df, DDf, dim)
+    return f[0], Df, DDf
+
+
+def psf_volproj(I, x, r, coords, nthreads=None):
+    """Voxel-integrated rendering (point_spread_functions.VolProj)."""
+    dim = len(coords)
+    I = np.ascontiguousarray(I, dtype=np.float64).reshape(-1)
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, dim)
+    r = np.ascontiguousarray(to_aniso(r, dim), dtype=np.float64)
+    ys = [np.ascontiguousarray(c, dtype=np.float64).reshape(-1) for c in coords]
+    if dim == 2:
+        ys.append(np.zeros(1))
+    out = np.zeros([y.size for y in ys[:dim]])
+    rc = lib().or_psf_volproj_f64(dim, I.size, _p(I), _p(x), _p(r), ys[0].size, _p(ys[0]),
+                                  ys[1].size, _p(ys[1]), ys[2].size, _p(ys[2]), _p(out),
+                                  _nthreads(nthreads))
+    assert rc == 0
+    return out

@@ -84,8 +84,8 @@ static void FN(tovec)(int gm, int a, const REAL *w0, const REAL *w1, REAL p0,
  * Follows NewtonBases2D.py:39-72 (dim 2) and NewtonBases.py:262-310 (dim 3,
  * lenT 2 or 3).
  */
-static REAL FN(Rf)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
-                   const REAL *y, const REAL *T)
+static REAL FN(Rf_gen)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
+                       const REAL *y, const REAL *T, int cut)
 {
     REAL M[3][3], Y[3] = {0, 0, 0}, rY[3] = {0, 0, 0}, rT[3] = {0, 0, 0},
                   T3[3] = {0, 0, 0};
@@ -108,8 +108,20 @@ static REAL FN(Rf)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
         REAL MY = rY[i] - rT[i] * IP;
         m += MY * MY;
     }
-    if (m > 1) return 0;
+    if (cut && m > 1) return 0;
     return I * RX_EXP(-30 * m) * n;
+}
+
+static REAL FN(Rf)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
+                   const REAL *y, const REAL *T)
+{
+    return FN(Rf_gen)(dim, lenT, I, x, r, y, T, 1);
+}
+
+static REAL FN(Rf_nocut)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
+                         const REAL *y, const REAL *T)
+{
+    return FN(Rf_gen)(dim, lenT, I, x, r, y, T, 0);
 }
 
 /*
@@ -119,9 +131,9 @@ static REAL FN(Rf)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
  * intermediate quantities dJdy, dJdT, ddJdyy, ddJdyT, ddJdTT.  P = 1+dim+Pr.
  * ddR is P x P row-major.  With order 1 only R and dR are filled.
  */
-static void FN(dRf)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
-                    const REAL *y, const REAL *T, REAL *R, REAL *dR, REAL *ddR,
-                    int order)
+static void FN(dRf_gen)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
+                        const REAL *y, const REAL *T, REAL *R, REAL *dR, REAL *ddR,
+                        int order, int cut)
 {
     const int Pr = dim == 2 ? 3 : 6, P = 1 + dim + Pr;
     REAL M[3][3], Y[3] = {0, 0, 0}, rY[3] = {0, 0, 0}, rT[3] = {0, 0, 0},
@@ -151,7 +163,13 @@ static void FN(dRf)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
         dMydT[i][i] -= IP;
     }
     REAL dg[3];
-    FN(dRg)(m, dg);
+    if (cut) {
+        FN(dRg)(m, dg);
+    } else {
+        dg[0] = RX_EXP(-30 * m);
+        dg[1] = -30 * dg[0];
+        dg[2] = 900 * dg[0];
+    }
     for (int i = 0; i < P; i++) {
         dR[i] = 0;
         if (order > 1)
@@ -243,6 +261,20 @@ static void FN(dRf)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
         }
     for (int i = 0; i < P; i++)
         for (int j = 0; j < i; j++) ddR[i * P + j] = ddR[j * P + i];
+}
+
+static void FN(dRf)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
+                    const REAL *y, const REAL *T, REAL *R, REAL *dR, REAL *ddR,
+                    int order)
+{
+    FN(dRf_gen)(dim, lenT, I, x, r, y, T, R, dR, ddR, order, 1);
+}
+
+static void FN(dRf_nocut)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
+                          const REAL *y, const REAL *T, REAL *R, REAL *dR, REAL *ddR,
+                          int order)
+{
+    FN(dRf_gen)(dim, lenT, I, x, r, y, T, R, dR, ddR, order, 0);
 }
 
 static int FN(geom)(int gm, int *dim, int *lenT)
@@ -431,6 +463,313 @@ int FN(or_volproj)(int dim, int N, const REAL *I, const REAL *x, const REAL *r,
                     }
                     if (nn <= 1)
                         acc += I[j] * RX_EXP(-30 * nn) * (REAL)c0;
+                }
+                u[((size_t)i0 * V1 + i1) * V2 + i2] = acc;
+            }
+    return 0;
+}
+
+
+/* ------------------------------------------------------------------------
+ * Single-particle ("point spread") operator: pixel-integrated projections.
+ * Restates GaussDictCode/bin/point_spread_functions.py: __Radius (:24),
+ * __total (:60), __projnorm (:75), __Rf (:386, no m > 1 cut-off), __rf2 (:413),
+ * __rf3 (:462), __dRf2/__dRf3 (:594, :738), __drf2 (:924), __drf3 (:1002),
+ * the bin ranges of __RadProj_2D/_3D (:530-588) and the L2 / inner-product
+ * accumulations (:1119-1313, :1354-1523).  Square pixels of half-width
+ * s = |p0[1] - p0[0]| / 2, as the reference assumes.
+ * ------------------------------------------------------------------------ */
+static REAL FN(psf_radius)(int dim, const REAL *r)
+{
+    REAL R = r[0] < r[1] ? r[0] : r[1];
+    if (dim == 3 && r[2] < R) R = r[2];
+    return (REAL)1 / R;
+}
+
+static REAL FN(psf_total)(int dim, REAL I, const REAL *r)
+{
+    if (dim == 2) return I / (r[0] * r[1]) * RX_SQRT((REAL)(3.14159265358979323846 / 30));
+    return I / (r[0] * r[1] * r[2]) * (REAL)(3.14159265358979323846 / 30);
+}
+
+/* value (and, with want_d, derivatives) of the pixel integral at pixel
+ * centre y for one atom; T, W0, W1 padded to 3 components */
+static void FN(psf_pixel)(int dim, int lenT, REAL I, const REAL *x, const REAL *r,
+                          const REAL *y, const REAL *T, const REAL *W0, const REAL *W1,
+                          REAL s, int want_d, int order, REAL *R, REAL *dR, REAL *ddR)
+{
+    const int Pr = dim == 2 ? 3 : 6, P = 1 + dim + Pr;
+    REAL X[3] = {0, 0, 0};
+    for (int i = 0; i < dim; i++) X[i] = x[i] - y[i];
+    *R = 0;
+    if (want_d)
+        for (int i = 0; i < P; i++) {
+            dR[i] = 0;
+            for (int j = 0; j < P; j++) ddR[i * P + j] = 0;
+        }
+    REAL rr = FN(psf_radius)(dim, r);
+    REAL t0 = 0, t1 = 0;
+    for (int i = 0; i < dim; i++) t0 += X[i] * X[i];
+    for (int i = 0; i < lenT; i++) t1 += X[i] * T[i];
+    t0 = t0 - t1 * t1;
+    REAL n = t0 > 0 ? RX_SQRT(t0) : 0;
+    if (n + rr < s) {
+        *R = FN(psf_total)(dim, I, r);
+        return;
+    } else if (n - rr > s) {
+        return;
+    }
+    REAL lim[2][2];
+    REAL Wv[2][3] = {{W0[0], W0[1], W0[2]}, {W1[0], W1[1], W1[2]}};
+    const int K = dim - 1;
+    for (int k = 0; k < K; k++) {
+        REAL c = 0;
+        for (int i = 0; i < dim; i++) c += X[i] * Wv[k][i];
+        lim[k][1] = c + rr < s ? c + rr : s;
+        lim[k][0] = c - rr > -s ? c - rr : -s;
+    }
+    REAL Ys[3] = {0, 0, 0};
+    for (int i = 0; i < dim; i++) {
+        Ys[i] = lim[0][0] * Wv[0][i];
+        if (K == 2) Ys[i] += lim[1][0] * Wv[1][i];
+    }
+    REAL step[2];
+    for (int k = 0; k < K; k++) step[k] = (REAL)0.1 * (lim[k][1] - lim[k][0]);
+    REAL Rv, dRv[10], ddRv[100];
+    int count = 0;
+    REAL sum = 0;
+    for (int a = 0; a < 11; a++) {
+        for (int i = 0; i < dim; i++) Ys[i] += step[0] * Wv[0][i];
+        int nb = K == 2 ? 11 : 1;
+        for (int b = 0; b < nb; b++) {
+            if (K == 2)
+                for (int i = 0; i < dim; i++) Ys[i] += step[1] * Wv[1][i];
+            /* point value at volume point y + Ys: the per-point basis has no
+             * cut-off in this module */
+            REAL Yp[3];
+            for (int i = 0; i < dim; i++) Yp[i] = y[i] + Ys[i];
+            if (want_d) {
+                FN(dRf_nocut)(dim, lenT, I, x, r, Yp, T, &Rv, dRv, ddRv, order);
+                sum += Rv;
+                for (int i = 0; i < P; i++) {
+                    dR[i] += dRv[i];
+                    if (order > 1)
+                        for (int j = 0; j < P; j++) ddR[i * P + j] += ddRv[i * P + j];
+                }
+            } else {
+                sum += FN(Rf_nocut)(dim, lenT, I, x, r, Yp, T);
+            }
+            count++;
+        }
+        if (K == 2)
+            for (int i = 0; i < dim; i++) Ys[i] -= 11 * step[1] * Wv[1][i];
+    }
+    REAL scale = K == 1 ? 10 * step[0] / count : 100 * step[0] * step[1] / count;
+    *R = sum * scale;
+    if (want_d)
+        for (int i = 0; i < P; i++) {
+            dR[i] *= scale;
+            for (int j = 0; j < P; j++) ddR[i * P + j] *= scale;
+        }
+}
+
+static void FN(psf_frame)(int gm, int a, const REAL *T, const REAL *w0, const REAL *w1,
+                          REAL *T3, REAL *W0, REAL *W1, int *lenT)
+{
+    for (int i = 0; i < 3; i++) { T3[i] = 0; W0[i] = 0; W1[i] = 0; }
+    if (gm == 2) {
+        *lenT = 2;
+        for (int i = 0; i < 2; i++) { T3[i] = T[2 * a + i]; W0[i] = w0[2 * a + i]; }
+    } else if (gm == 3) {
+        *lenT = 3;
+        for (int i = 0; i < 3; i++) {
+            T3[i] = T[3 * a + i]; W0[i] = w0[3 * a + i]; W1[i] = w1[3 * a + i];
+        }
+    } else {
+        *lenT = 2;
+        for (int i = 0; i < 2; i++) { T3[i] = T[2 * a + i]; W0[i] = w0[2 * a + i]; }
+        W1[2] = 1;
+    }
+}
+
+/* pixel-integrated forward projection (bin ranges of __RadProj_2D/_3D) */
+int FN(or_psf_radproj)(int gm, int N, const REAL *I, const REAL *x, const REAL *r,
+                       int A, const REAL *T, const REAL *w0, const REAL *w1, int D0,
+                       const REAL *p0, int D1, const REAL *p1, REAL *R, int nthreads)
+{
+    int dim, lenT;
+    if (FN(geom)(gm, &dim, &lenT)) return -1;
+    const int Pr = dim == 2 ? 3 : 6;
+    if (dim == 2) D1 = 1;
+    const REAL s = (REAL)fabs((double)(p0[1] - p0[0])) / 2;
+    const REAL dp = 1 / (p0[1] - p0[0]);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int a = 0; a < A; a++) {
+        REAL T3[3], W0[3], W1[3], y[3];
+        int lt;
+        FN(psf_frame)(gm, a, T, w0, w1, T3, W0, W1, &lt);
+        REAL *out = R + (size_t)a * D0 * D1;
+        for (int k = 0; k < D0 * D1; k++) out[k] = 0;
+        for (int j = 0; j < N; j++) {
+            const REAL *xj = x + dim * j, *rj = r + Pr * j;
+            REAL rr = FN(psf_radius)(dim, rj);
+            REAL IP = 0;
+            for (int i = 0; i < dim; i++) IP += xj[i] * W0[i];
+            int b00 = (int)((IP - rr - p0[0]) * dp);
+            if (b00 < 0) b00 = 0;
+            int b01 = (int)((IP + rr - p0[0]) * dp) + 2;
+            if (b01 > D0) b01 = D0;
+            int b10 = 0, b11 = 1;
+            if (dim == 3) {
+                IP = 0;
+                for (int i = 0; i < 3; i++) IP += xj[i] * W1[i];
+                b10 = (int)((IP - rr - p1[0]) * dp);
+                if (b10 < 0) b10 = 0;
+                b11 = (int)((IP + rr - p1[0]) * dp) + 2;
+                if (b11 > D1) b11 = D1;
+            }
+            for (int k0 = b00; k0 < b01; k0++)
+                for (int k1 = b10; k1 < b11; k1++) {
+                    for (int i = 0; i < 3; i++)
+                        y[i] = p0[k0] * W0[i] + (dim == 3 ? p1[k1] * W1[i] : 0);
+                    REAL v;
+                    FN(psf_pixel)(dim, lt, I[j], xj, rj, y, T3, W0, W1, s, 0, 0, &v, 0, 0);
+                    out[(size_t)k0 * D1 + k1] += v;
+                }
+        }
+    }
+    return 0;
+}
+
+/* single-atom derivatives of the pixel-integrated projection, summed over
+ * all cells: kind 0 (L2, C^2 for cells outside the bins), kind 1 (inner) */
+int FN(or_psf_atom_derivs)(int kind, int gm, const REAL *I, const REAL *x, const REAL *r,
+                           int A, const REAL *T, const REAL *w0, const REAL *w1, int D0,
+                           const REAL *p0, int D1, const REAL *p1, const REAL *C, int order,
+                           double *f, double *Df, double *DDf, int nthreads)
+{
+    int dim, lenT;
+    if (FN(geom)(gm, &dim, &lenT)) return -1;
+    const int Pr = dim == 2 ? 3 : 6, P = 1 + dim + Pr;
+    if (dim == 2) D1 = 1;
+    const int stride = 1 + P + P * P;
+    double *part = (double *)calloc((size_t)A * stride, sizeof(double));
+    if (!part) return -2;
+    const REAL s = (REAL)fabs((double)(p0[1] - p0[0])) / 2;
+    const REAL dp = 1 / (p0[1] - p0[0]);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int a = 0; a < A; a++) {
+        double *acc = part + (size_t)a * stride;
+        REAL T3[3], W0[3], W1[3], y[3], Rv, dR[10], ddR[100];
+        int lt;
+        FN(psf_frame)(gm, a, T, w0, w1, T3, W0, W1, &lt);
+        REAL rr = FN(psf_radius)(dim, r);
+        REAL IP = 0;
+        for (int i = 0; i < dim; i++) IP += x[i] * W0[i];
+        int b00 = (int)((IP - rr - s - p0[0]) * dp);
+        if (b00 < 0) b00 = 0;
+        int b01 = (int)((IP + rr + s - p0[0]) * dp) + 1;
+        if (b01 > D0) b01 = D0;
+        int b10 = 0, b11 = 1;
+        if (dim == 3) {
+            IP = 0;
+            for (int i = 0; i < 3; i++) IP += x[i] * W1[i];
+            b10 = (int)((IP - rr - s - p1[0]) * dp) - 1;
+            if (b10 < 0) b10 = 0;
+            b11 = (int)((IP + rr + s - p1[0]) * dp) + 1;
+            if (b11 > D1) b11 = D1;
+        }
+        for (int k0 = 0; k0 < D0; k0++)
+            for (int k1 = 0; k1 < D1; k1++) {
+                double c = C[((size_t)a * D0 + k0) * D1 + k1];
+                int in = k0 >= b00 && k0 < b01 && k1 >= b10 && k1 < b11;
+                if (!in) {
+                    if (kind == 0) acc[0] += c * c;
+                    continue;
+                }
+                for (int i = 0; i < 3; i++)
+                    y[i] = p0[k0] * W0[i] + (dim == 3 ? p1[k1] * W1[i] : 0);
+                FN(psf_pixel)(dim, lt, I[0], x, r, y, T3, W0, W1, s, 1, order, &Rv, dR, ddR);
+                if (kind == 0) {
+                    double res = (double)Rv - c;
+                    acc[0] += res * res;
+                    for (int i = 0; i < P; i++) acc[1 + i] += res * dR[i];
+                    if (order > 1)
+                        for (int i = 0; i < P; i++)
+                            for (int j = 0; j < P; j++)
+                                acc[1 + P + i * P + j] +=
+                                    (double)dR[i] * dR[j] + res * ddR[i * P + j];
+                } else {
+                    acc[0] += (double)Rv * c;
+                    for (int i = 0; i < P; i++) acc[1 + i] += c * dR[i];
+                    if (order > 1)
+                        for (int i = 0; i < P * P; i++) acc[1 + P + i] += c * ddR[i];
+                }
+            }
+    }
+    double tot[1 + 10 + 100];
+    for (int i = 0; i < stride; i++) tot[i] = 0;
+    for (int a = 0; a < A; a++)
+        for (int i = 0; i < stride; i++) tot[i] += part[(size_t)a * stride + i];
+    free(part);
+    *f = kind == 0 ? 0.5 * tot[0] : tot[0];
+    for (int i = 0; i < P; i++) Df[i] = tot[1 + i];
+    for (int i = 0; i < P * P; i++) DDf[i] = order > 1 ? tot[1 + P + i] : 0.0;
+    return 0;
+}
+
+/* voxel-integrated rendering (point_spread_functions.py __if2/__if3,
+ * __dense_VolProj2/3): 11^dim rule, half-width s = |y1[1] - y1[0]| / 2 */
+int FN(or_psf_volproj)(int dim, int N, const REAL *I, const REAL *x, const REAL *r,
+                       int V0, const REAL *y0, int V1, const REAL *y1, int V2,
+                       const REAL *y2, REAL *u, int nthreads)
+{
+    const int Pr = dim == 2 ? 3 : 6;
+    if (dim == 2) V2 = 1;
+    const REAL s = (REAL)fabs((double)(y1[1] - y1[0])) / 2;
+    const REAL c0 = RX_SQRT((REAL)(30.0 / 3.14159265358979323846));
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int i0 = 0; i0 < V0; i0++)
+        for (int i1 = 0; i1 < V1; i1++)
+            for (int i2 = 0; i2 < V2; i2++) {
+                REAL y[3] = {y0[i0], y1[i1], dim == 3 ? y2[i2] : 0};
+                REAL acc = 0;
+                for (int j = 0; j < N; j++) {
+                    REAL M[3][3], X[3] = {0, 0, 0};
+                    FN(rmat)(dim, r + Pr * j, M);
+                    const REAL *rj = r + Pr * j;
+                    for (int i = 0; i < dim; i++) X[i] = x[dim * j + i] - y[i];
+                    REAL rr = FN(psf_radius)(dim, rj), nn = 0;
+                    for (int i = 0; i < dim; i++) nn += X[i] * X[i];
+                    nn = RX_SQRT(nn);
+                    if (nn + rr < s) { acc += FN(psf_total)(dim, I[j], rj); continue; }
+                    if (nn - rr > s) continue;
+                    REAL lo[3], st[3], Y[3];
+                    for (int i = 0; i < dim; i++) {
+                        REAL l = X[i] - rr > -s ? X[i] - rr : -s;
+                        REAL h = X[i] + rr < s ? X[i] + rr : s;
+                        lo[i] = l;
+                        st[i] = (REAL)0.1 * (h - l);
+                    }
+                    REAL sum = 0;
+                    int count = 0;
+                    for (int a = 1; a <= 11; a++)
+                        for (int b = 1; b <= 11; b++)
+                            for (int c = 1; c <= (dim == 3 ? 11 : 1); c++) {
+                                Y[0] = lo[0] + a * st[0] - X[0];
+                                Y[1] = lo[1] + b * st[1] - X[1];
+                                Y[2] = dim == 3 ? lo[2] + c * st[2] - X[2] : 0;
+                                REAL n2 = 0;
+                                for (int q = 0; q < dim; q++) {
+                                    REAL v = 0;
+                                    for (int k = q; k < dim; k++) v += M[q][k] * Y[k];
+                                    n2 += v * v;
+                                }
+                                sum += RX_EXP(-30 * n2) * c0;
+                                count++;
+                            }
+                    acc += I[j] * sum / count *
+                           (dim == 2 ? 100 * st[0] * st[1] : 1000 * st[0] * st[1] * st[2]);
                 }
                 u[((size_t)i0 * V1 + i1) * V2 + i2] = acc;
             }

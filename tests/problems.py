@@ -80,3 +80,15 @@ def entry_relerr(a, ref):
     scale = np.max(np.abs(ref), axis=0)
     scale = np.where(scale > 1e-9 * tot, scale, tot)
     return float(np.max(np.abs(a - ref) / scale))
+
+
+def atom_normwise_relerr(a, ref):
+    """Max over atoms of max|a_j - ref_j| / max|ref_j| (each atom's matrix
+    scaled by its own largest entry)."""
+    a = np.asarray(a, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    n = ref.shape[0]
+    d = np.abs(a - ref).reshape(n, -1).max(axis=1)
+    sc = np.abs(ref).reshape(n, -1).max(axis=1)
+    sc = np.where(sc > 0, sc, 1.0)
+    return float(np.max(d / sc))
