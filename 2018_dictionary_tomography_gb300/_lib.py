@@ -20,7 +20,8 @@ class GrAtoms(ctypes.Structure):
                 ("I", ctypes.c_void_p),
                 ("x", ctypes.c_void_p),
                 ("r", ctypes.c_void_p),
-                ("r_iso", ctypes.c_int)]
+                ("r_iso", ctypes.c_int),
+                ("order", ctypes.c_void_p)]
 
 
 class GrGeometry(ctypes.Structure):
@@ -40,7 +41,8 @@ class EngineError(RuntimeError):
 EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
            "gr_fit_forward", "gr_atom_derivs", "gr_count_support", "gr_probe_ex2",
            "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj", "gr_newton_accept",
-           "gr_psf_radproj", "gr_psf_fit_forward", "gr_psf_atom_derivs", "gr_psf_volproj")
+           "gr_psf_radproj", "gr_psf_fit_forward", "gr_psf_atom_derivs", "gr_psf_volproj",
+           "gr_set_tuning", "gr_get_tuning")
 
 _lock = threading.Lock()
 _lib = None
@@ -116,6 +118,10 @@ def load(build_if_missing=True):
         lib.gr_psf_volproj.restype = ctypes.c_int
         lib.gr_psf_volproj.argtypes = [P(GrAtoms), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]
+        lib.gr_set_tuning.restype = ctypes.c_int
+        lib.gr_set_tuning.argtypes = [ctypes.c_int, ctypes.c_int]
+        lib.gr_get_tuning.restype = ctypes.c_int
+        lib.gr_get_tuning.argtypes = [ctypes.c_int]
         lib.gr_launch_count.restype = ctypes.c_ulonglong
         lib.gr_launch_count.argtypes = []
         _lib = lib

@@ -25,6 +25,7 @@ bool to_internal(const gr_atoms *a, const gr_geometry *g, Atoms &at, Geom &ge,
   at.x = a->x;
   at.r = a->r;
   at.r_iso = a->r_iso ? 1 : 0;
+  at.order = a->order;
   ge.K = g->kdet;
   ge.n_angles = g->n_angles;
   ge.frames = g->frames;
@@ -241,6 +242,7 @@ static int volproj_impl(const gr_atoms *atoms, int dim, const int *n_vox,
   at.x = atoms->x;
   at.r = atoms->r;
   at.r_iso = atoms->r_iso ? 1 : 0;
+  at.order = nullptr;
   return launch_volproj(at, dim, n_vox, coords, u, psf, s, static_cast<cudaStream_t>(stream));
 }
 
@@ -273,5 +275,9 @@ int gr_probe_ex2(int blocks, int threads, int iters, float *sink, void *stream) 
 }
 
 unsigned long long gr_launch_count(void) { return g_launches.load(); }
+
+int gr_set_tuning(int key, int value) { return set_tuning(key, value); }
+
+int gr_get_tuning(int key) { return get_tuning(key); }
 
 }  // extern "C"

@@ -113,6 +113,7 @@ struct Atoms {
   const float *x;
   const float *r;
   int r_iso;
+  const int *order;  // optional processing order of the derivative kernels
 };
 
 template <int K>

@@ -43,13 +43,22 @@ inline int next_pow2(int v) {
   return p;
 }
 
+constexpr int kRowChunk = 8;
+
+// Work split of the derivative kernels (tunable through gr_set_tuning):
+// about g_deriv_target_warps warps in total, each angle chunk holding at
+// least g_deriv_min_angles angles per lane group.
+int g_deriv_target_warps = 32768;
+int g_deriv_min_angles = 1;
+
 inline DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order) {
   DerivCfg c;
   c.ag = next_pow2(n_atoms < 1 ? 1 : n_atoms);
   c.sg = 32 / c.ag;
   const int warps_atoms = (n_atoms + c.ag - 1) / c.ag;
-  int nch = (4096 + warps_atoms - 1) / warps_atoms;
-  const int max_ch = (n_angles + c.sg - 1) / c.sg;
+  int nch = (g_deriv_target_warps + warps_atoms - 1) / warps_atoms;
+  const int per = c.sg * (g_deriv_min_angles < 1 ? 1 : g_deriv_min_angles);
+  const int max_ch = (n_angles + per - 1) / per;
   if (nch > max_ch) nch = max_ch;
   if (nch < 1) nch = 1;
   c.ch = (n_angles + nch - 1) / nch;
@@ -127,31 +136,45 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
         if (GN) Sb[q] = 0.f;
       }
       const size_t rbase = abase + (size_t)k0 * D1;
-      for (int k1 = p.lo[1]; k1 <= p.hi[1]; ++k1) {
-        const float d1 = (__ldg(g.ax[1].coords + k1) - p.qh[1]) - p.ql[1];
-        const float m = fmaf(d1, fmaf(p.G[2], d1, u), t0);
-        if (m <= 1.f) {
-          const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
-          const float c = __ldg(field + rbase + k1);
-          const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
-          float w = al * E;
+      // the row is walked in chunks of kRowChunk cells whose field values
+      // and coordinates are loaded together first, so the loads overlap
+      // instead of each cell waiting for its own
+      for (int kb = p.lo[1]; kb <= p.hi[1]; kb += kRowChunk) {
+        float cv[kRowChunk], pv[kRowChunk], bv[GN ? kRowChunk : 1];
 #pragma unroll
-          for (int q = 0; q <= DEG; ++q) {
-            Sa[q] += w;
-            w *= d1;
-          }
-          if (GN) {
-            const float be = bfield ? __ldg(bfield + rbase + k1) : in.beta_const;
-            float wb = be * E * E;
+        for (int i = 0; i < kRowChunk; ++i) {
+          const int k1 = min(kb + i, p.hi[1]);
+          cv[i] = __ldg(field + rbase + k1);
+          pv[i] = __ldg(g.ax[1].coords + k1);
+          if (GN) bv[i] = bfield ? __ldg(bfield + rbase + k1) : in.beta_const;
+        }
+#pragma unroll
+        for (int i = 0; i < kRowChunk; ++i) {
+          if (kb + i > p.hi[1]) break;
+          const float d1 = (pv[i] - p.qh[1]) - p.ql[1];
+          const float m = fmaf(d1, fmaf(p.G[2], d1, u), t0);
+          if (m <= 1.f) {
+            const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
+            const float c = cv[i];
+            const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
+            float w = al * E;
 #pragma unroll
             for (int q = 0; q <= DEG; ++q) {
-              Sb[q] += wb;
-              wb *= d1;
+              Sa[q] += w;
+              w *= d1;
             }
-          }
-          if (in.mode == kModeL2Atom) {
-            mo.X0 = fmaf(E, c, mo.X0);
-            mo.Y0 = fmaf(E, E, mo.Y0);
+            if (GN) {
+              float wb = bv[i] * E * E;
+#pragma unroll
+              for (int q = 0; q <= DEG; ++q) {
+                Sb[q] += wb;
+                wb *= d1;
+              }
+            }
+            if (in.mode == kModeL2Atom) {
+              mo.X0 = fmaf(E, c, mo.X0);
+              mo.Y0 = fmaf(E, E, mo.Y0);
+            }
           }
         }
       }
@@ -170,7 +193,7 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
 }
 
 template <int K, int ORDER>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, ORDER == 1 ? 5 : 1)
     gr_deriv_kernel(Atoms at, Geom g, DerivIn in, DerivCfg cfg, float *part) {
   constexpr int D = K + 1;
   constexpr int PR = n_rparam<K>();
@@ -185,10 +208,10 @@ __global__ void __launch_bounds__(128)
   const int warps_atoms = (at.n + cfg.ag - 1) / cfg.ag;
   if (gw >= warps_atoms * cfg.nchunks) return;
   const int chunk = gw / warps_atoms, wa = gw - chunk * warps_atoms;
-  const int j = wa * cfg.ag + (lane % cfg.ag);
+  const int j = wa * cfg.ag + (lane % cfg.ag);   // slot
   const int sub = lane / cfg.ag;
   const bool valid = j < at.n;
-  const int jj = valid ? j : 0;
+  const int jj = valid ? (at.order ? at.order[j] : j) : 0;  // atom of the slot
   const float I = at.I[jj];
   const int a_lo = chunk * cfg.ch;
   const int a_hi = min(g.n_angles, a_lo + cfg.ch);
@@ -271,10 +294,10 @@ __global__ void __launch_bounds__(128)
   const int warps_atoms = (at.n + cfg.ag - 1) / cfg.ag;
   if (gw >= warps_atoms * cfg.nchunks) return;
   const int chunk = gw / warps_atoms, wa = gw - chunk * warps_atoms;
-  const int j = wa * cfg.ag + (lane % cfg.ag);
+  const int j = wa * cfg.ag + (lane % cfg.ag);   // slot
   const int sub = lane / cfg.ag;
   const bool valid = j < at.n;
-  const int jj = valid ? j : 0;
+  const int jj = valid ? (at.order ? at.order[j] : j) : 0;  // atom of the slot
   const float I = at.I[jj];
   const int a_lo = chunk * cfg.ch;
   const int a_hi = min(g.n_angles, a_lo + cfg.ch);
@@ -457,17 +480,18 @@ __global__ void __launch_bounds__(32 * kRedSlices)
 // r_aniso = (s, .., s, 0, ..).
 template <int K>
 __global__ void gr_deriv_finalize_kernel(const double *sums, DerivCfg cfg, int n,
-                                         int order, int r_iso, DerivOut out,
-                                         const double *f_extra) {
+                                         int deriv_order, int r_iso, DerivOut out,
+                                         const double *f_extra, const int *order) {
   constexpr int D = K + 1;
   constexpr int P = n_par<K>();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= n) return;
   double v[1 + P + P * (P + 1) / 2];
-  for (int q = 0; q < cfg.qn; ++q) v[q] = sums[(size_t)q * n + j];
+  for (int q = 0; q < cfg.qn; ++q) v[q] = sums[(size_t)q * n + slot];
+  const int j = order ? order[slot] : slot;  // atom of the slot
   double f = v[0] + (f_extra ? f_extra[0] : 0.0);
   double H[P][P];
-  if (order > 1) {
+  if (deriv_order > 1) {
     int o = 1 + P;
     for (int a = 0; a < P; ++a)
       for (int b = a; b < P; ++b, ++o) {
@@ -478,7 +502,7 @@ __global__ void gr_deriv_finalize_kernel(const double *sums, DerivCfg cfg, int n
   out.f[j] = f;
   if (!r_iso) {
     for (int a = 0; a < P; ++a) out.g[(size_t)j * P + a] = v[1 + a];
-    if (order > 1)
+    if (deriv_order > 1)
       for (int a = 0; a < P; ++a)
         for (int b = 0; b < P; ++b) out.H[((size_t)j * P + a) * P + b] = H[a][b];
     return;
@@ -490,7 +514,7 @@ __global__ void gr_deriv_finalize_kernel(const double *sums, DerivCfg cfg, int n
   gi[1 + D] = 0.0;
   for (int q = 0; q < D; ++q) gi[1 + D] += v[1 + 1 + D + q];
   for (int a = 0; a < PI; ++a) out.g[(size_t)j * PI + a] = gi[a];
-  if (order > 1) {
+  if (deriv_order > 1) {
     auto src = [&](int a, int q) { return a < 1 + D ? a : 1 + D + q; };
     for (int a = 0; a < PI; ++a)
       for (int b = 0; b < PI; ++b) {
@@ -543,6 +567,22 @@ int launch_sum_squares(const float *C, size_t n, double *out, void *ws,
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
+int set_tuning(int key, int value) {
+  if (key == 0 && value >= 32 && value <= (1 << 22)) {
+    g_deriv_target_warps = value;
+    return kOk;
+  }
+  if (key == 1 && value >= 1 && value <= 65536) {
+    g_deriv_min_angles = value;
+    return kOk;
+  }
+  return kErrArg;
+}
+
+int get_tuning(int key) {
+  return key == 0 ? g_deriv_target_warps : key == 1 ? g_deriv_min_angles : -1;
+}
+
 size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order) {
   DerivCfg c = deriv_cfg(K, n_atoms, n_angles, order);
   size_t b = align_up((size_t)c.nchunks * c.qn * (size_t)n_atoms * sizeof(float));
@@ -590,21 +630,21 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
     }
     gr_deriv_reduce_kernel<<<rgrid, 32 * kRedSlices, 0, stream>>>(part, c, at.n, sums);
     if (K == 1)
-      gr_deriv_finalize_kernel<1><<<(at.n + 127) / 128, 128, 0, stream>>>(sums, c, at.n, in.order, at.r_iso, out, fe);
+      gr_deriv_finalize_kernel<1><<<(at.n + 127) / 128, 128, 0, stream>>>(sums, c, at.n, in.order, at.r_iso, out, fe, at.order);
     else
-      gr_deriv_finalize_kernel<2><<<(at.n + 127) / 128, 128, 0, stream>>>(sums, c, at.n, in.order, at.r_iso, out, fe);
+      gr_deriv_finalize_kernel<2><<<(at.n + 127) / 128, 128, 0, stream>>>(sums, c, at.n, in.order, at.r_iso, out, fe, at.order);
   } else if (K == 1) {
     if (in.order == 1) gr_deriv_kernel<1, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
     else gr_deriv_kernel<1, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
     gr_deriv_reduce_kernel<<<rgrid, 32 * kRedSlices, 0, stream>>>(part, c, at.n, sums);
     gr_deriv_finalize_kernel<1><<<(at.n + 127) / 128, 128, 0, stream>>>(
-        sums, c, at.n, in.order, at.r_iso, out, fe);
+        sums, c, at.n, in.order, at.r_iso, out, fe, at.order);
   } else {
     if (in.order == 1) gr_deriv_kernel<2, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
     else gr_deriv_kernel<2, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
     gr_deriv_reduce_kernel<<<rgrid, 32 * kRedSlices, 0, stream>>>(part, c, at.n, sums);
     gr_deriv_finalize_kernel<2><<<(at.n + 127) / 128, 128, 0, stream>>>(
-        sums, c, at.n, in.order, at.r_iso, out, fe);
+        sums, c, at.n, in.order, at.r_iso, out, fe, at.order);
   }
   note_launches(3);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;

@@ -101,6 +101,9 @@ int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
 int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y,
                    float *u, int psf, float s, cudaStream_t stream);
 
+int set_tuning(int key, int value);
+int get_tuning(int key);
+
 // host-side count of kernels launched by this library
 void note_launches(int n);
 extern std::atomic<unsigned long long> g_launches;

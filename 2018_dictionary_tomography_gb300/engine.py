@@ -44,10 +44,30 @@ def _stream_handle(device):
     return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 
 
-class DeviceAtoms:
-    """Float32 device copies of atom parameters plus the C-ABI descriptor."""
+def morton_order(x):
+    """Permutation visiting atom centres x (N, d) along a Morton (Z-order)
+    curve of a 2^10-per-axis grid over their bounding box, so consecutive
+    atoms are spatially close."""
+    import numpy as np
+    x = np.asarray(x, dtype=np.float64)
+    n, d = x.shape
+    lo, hi = x.min(axis=0), x.max(axis=0)
+    q = ((x - lo) / np.maximum(hi - lo, 1e-12) * 1023).astype(np.uint64)
+    code = np.zeros(n, dtype=np.uint64)
+    for bit in range(10):
+        for k in range(d):
+            code |= ((q[:, k] >> np.uint64(bit)) & np.uint64(1)) << np.uint64(bit * d + k)
+    return np.argsort(code, kind="stable").astype(np.int32)
 
-    def __init__(self, I, x, r, device=None):
+
+class DeviceAtoms:
+    """Float32 device copies of atom parameters plus the C-ABI descriptor.
+
+    order: None (index order), "spatial" (Morton order of the centres, better
+    cache locality in the derivative kernels for large atom sets), or a
+    permutation; results do not depend on it."""
+
+    def __init__(self, I, x, r, device=None, order=None):
         device = torch.device(device or "cuda")
         _require_cuda(device)
         I = torch.as_tensor(I).to(device=device, dtype=torch.float32).reshape(-1).contiguous()
@@ -72,6 +92,14 @@ class DeviceAtoms:
         s.x = x.data_ptr() if n else None
         s.r = r.data_ptr() if n else None
         s.r_iso = 1 if self.iso else 0
+        self.order = None
+        if isinstance(order, str) and order == "spatial" and n > 1:
+            order = morton_order(x.detach().cpu().numpy())
+        if order is not None and not isinstance(order, str):
+            self.order = torch.as_tensor(order, dtype=torch.int32).to(device).contiguous()
+            if self.order.numel() != n:
+                raise ValueError("order must be a permutation of the atoms")
+        s.order = self.order.data_ptr() if self.order is not None else None
         self.struct = s
 
     def n_params(self):

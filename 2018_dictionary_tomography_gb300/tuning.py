@@ -1,0 +1,72 @@
+"""Autotuner for the derivative kernels' work split.
+
+The derivative launch splits (atoms x angle chunks) into about
+``GR_TUNE_DERIV_WARPS`` warps with at least ``GR_TUNE_DERIV_MIN_ANGLES`` angles
+per lane group; the best split depends on the atom count, angle count,
+support sizes and derivative order.  ``autotune_derivs`` times candidate
+splits on the actual problem with CUDA events and keeps the fastest; results
+are cached per shape class (detector dims, log2 atom count, log2 angle count,
+order, pixel-integrated or not) and reapplied by ``apply_for``.
+Results do not depend on the split beyond FP rounding of the chunk sums.
+"""
+import math
+
+import torch
+
+from . import _lib, engine
+
+WARPS = (1024, 2048, 4096, 8192, 16384, 32768)
+MIN_ANGLES = (1, 2, 4, 8)
+_cache = {}
+
+
+def set_split(target_warps, min_angles):
+    lib = _lib.load()
+    _lib.check(lib.gr_set_tuning(0, int(target_warps)), "gr_set_tuning")
+    _lib.check(lib.gr_set_tuning(1, int(min_angles)), "gr_set_tuning")
+
+
+def get_split():
+    lib = _lib.load()
+    return int(lib.gr_get_tuning(0)), int(lib.gr_get_tuning(1))
+
+
+def shape_key(atoms, geom, order, psf=False):
+    return (geom.kdet, int(math.log2(max(1, atoms.n))), int(math.log2(max(1, geom.n_angles))),
+            int(order), bool(psf))
+
+
+def autotune_derivs(atoms, geom, field, beta_field=None, beta_const=1.0, order=1,
+                    psf=False, reps=5, candidates=None):
+    """Time every candidate split on this problem; apply and return the best
+    (target_warps, min_angles, ms)."""
+    key = shape_key(atoms, geom, order, psf)
+    cands = candidates or [(w, m) for w in WARPS for m in MIN_ANGLES]
+    saved = get_split()
+    best = None
+    for w, m in cands:
+        set_split(w, m)
+        engine.atom_derivs(atoms, geom, "field", field, beta_field, beta_const, order, psf=psf)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            engine.atom_derivs(atoms, geom, "field", field, beta_field, beta_const, order, psf=psf)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        if best is None or ms < best[2]:
+            best = (w, m, ms)
+    if best is None:
+        set_split(*saved)
+        return None
+    _cache[key] = best[:2]
+    set_split(best[0], best[1])
+    return best
+
+
+def apply_for(atoms, geom, order, psf=False):
+    """Apply the cached split for this shape class, if any; returns it."""
+    v = _cache.get(shape_key(atoms, geom, order, psf))
+    if v is not None:
+        set_split(*v)
+    return v

@@ -44,13 +44,17 @@ enum {
     GR_ERR_TOO_LARGE = -5  /* problem needs more than the built-in scratch */
 };
 
-/* Atoms in device memory (float32). */
+/* Atoms in device memory (float32).  order (nullable): a permutation of
+ * 0..n_atoms-1 giving the order in which the derivative kernels visit the
+ * atoms (spatially clustered orders read the weight fields with better cache
+ * locality); outputs stay indexed by atom and do not depend on it. */
 typedef struct {
     int n_atoms;
     const float *I;   /* (n_atoms) */
     const float *x;   /* (n_atoms, d) */
     const float *r;   /* (n_atoms, P_r) or (n_atoms) when r_iso */
     int r_iso;
+    const int *order; /* (n_atoms) or NULL */
 } gr_atoms;
 
 /*
@@ -239,6 +243,21 @@ int gr_count_support(const gr_atoms *atoms, const gr_geometry *geom,
                      unsigned long long *count, void *stream);
 int gr_probe_ex2(int blocks, int threads, int iters, float *sink, void *stream);
 unsigned long long gr_launch_count(void);
+
+/*
+ * Work-split knobs of the derivative kernels, process-wide (no counterpart
+ * in the reference).  GR_TUNE_DERIV_WARPS: about this many warps per
+ * derivative launch (atoms x angle chunks; default 4096);
+ * GR_TUNE_DERIV_MIN_ANGLES: at least this many angles per lane group in a
+ * chunk (default 1).  Set them before gr_workspace_bytes and keep them fixed
+ * while launches that used the old values are in flight.  Results do not
+ * depend on them beyond FP rounding of the chunk sums.  gr_set_tuning returns
+ * GR_ERR_ARG for an unknown key or out-of-range value; gr_get_tuning returns
+ * the current value (-1 for an unknown key).
+ */
+enum { GR_TUNE_DERIV_WARPS = 0, GR_TUNE_DERIV_MIN_ANGLES = 1 };
+int gr_set_tuning(int key, int value);
+int gr_get_tuning(int key);
 
 /*
  * gr_radproj without a caller-supplied workspace.  No counterpart in the

@@ -5,6 +5,8 @@ import importlib
 import os
 import re
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -48,3 +50,14 @@ def test_workspace_query_and_argument_errors_without_gpu():
     assert lib.gr_workspace_bytes(0, ctypes.byref(at), ctypes.byref(g)) == 0
     rc = lib.gr_radproj(ctypes.byref(at), ctypes.byref(g), None, None, 0, None)
     assert rc == lib_mod.GR_OK - 1  # GR_ERR_ARG
+
+
+def test_morton_order_is_permutation():
+    eng = importlib.import_module("2018_dictionary_tomography_gb300.engine")
+    x = np.random.default_rng(0).uniform(-1, 1, (1000, 3))
+    p = eng.morton_order(x)
+    assert sorted(p.tolist()) == list(range(1000))
+    # consecutive atoms along the curve are closer than in index order
+    d_curve = np.linalg.norm(np.diff(x[p], axis=0), axis=1).mean()
+    d_index = np.linalg.norm(np.diff(x, axis=0), axis=1).mean()
+    assert d_curve < 0.5 * d_index

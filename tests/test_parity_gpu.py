@@ -134,3 +134,23 @@ def test_atoms_outside_detector_and_empty(eng, cuda_ready):
     assert relerr(R, go.radproj(I, x, r, g)) < TOL
     R0 = eng.radproj(engine_atoms(I[:0], x[:0], r[:0]), engine_geometry(g))
     assert torch.count_nonzero(R0).item() == 0
+
+
+@pytest.mark.parametrize("case", ["2d", "3d"])
+@pytest.mark.parametrize("psf", [False, True])
+def test_atom_order_does_not_change_results(eng, cuda_ready, case, psf):
+    """A processing order (spatial or any permutation) changes only which lane
+    visits an atom; outputs stay indexed by atom."""
+    g, I, x, r = _setup(case, seed=21)
+    geom = engine_geometry(g)
+    field = torch.from_numpy(go.radproj(I, x, r, g) * 0.9).float().cuda()
+    base = eng.DeviceAtoms(I, x, r)
+    f0, g0, H0 = eng.atom_derivs(base, geom, "inner", field, order=2, psf=psf)
+    perm = np.random.default_rng(3).permutation(len(I)).astype(np.int32)
+    for order in ("spatial", perm):
+        atoms = eng.DeviceAtoms(I, x, r, order=order)
+        f1, g1, H1 = eng.atom_derivs(atoms, geom, "inner", field, order=2, psf=psf)
+        assert entry_relerr(g1.cpu().numpy(), g0.cpu().numpy()) < 1e-6
+        assert entry_relerr(H1.cpu().numpy(), H0.cpu().numpy()) < 1e-6
+        assert relerr(f1.cpu().numpy(), f0.cpu().numpy()) < 1e-6
+
