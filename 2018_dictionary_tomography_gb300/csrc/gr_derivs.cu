@@ -48,12 +48,21 @@ constexpr int kRowChunk = 8;
 // Work split of the derivative kernels (tunable through gr_set_tuning):
 // about g_deriv_target_warps warps in total, each angle chunk holding at
 // least g_deriv_min_angles angles per lane group.
-int g_deriv_target_warps = 32768;
+int g_deriv_target_warps = 131072;
 int g_deriv_min_angles = 1;
+// Atoms per warp (power of two up to 32; 0 = automatic): with fewer atoms per
+// warp the lanes of a warp take different angles of one atom, whose support
+// boxes are of similar size, so fewer lanes idle.  Automatic: one atom per
+// warp for Hessians and for long angle series, else four (so each lane still
+// has a few angles to amortise the warp's closing reduction).
+int g_deriv_atoms_per_warp = 0;
 
 inline DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order) {
   DerivCfg c;
   c.ag = next_pow2(n_atoms < 1 ? 1 : n_atoms);
+  const int ag_cap = g_deriv_atoms_per_warp > 0 ? g_deriv_atoms_per_warp
+                     : (order > 1 || n_angles >= 1024) ? 1 : 4;
+  if (c.ag > ag_cap) c.ag = ag_cap;
   c.sg = 32 / c.ag;
   const int warps_atoms = (n_atoms + c.ag - 1) / c.ag;
   int nch = (g_deriv_target_warps + warps_atoms - 1) / warps_atoms;
@@ -98,6 +107,14 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
   const float *__restrict__ field = in.alpha;
   const float *__restrict__ bfield = in.beta;
   const size_t abase = (size_t)a * D0 * D1;
+  // per row, m <= 1 holds for d1 within hw(d0) = sqrt(G2 - d0^2 det)/G2 of
+  // -G1 d0/G2: the row loop visits that range (widened like the support box)
+  // instead of the whole box; the m <= 1 test still decides every cell
+  float det = 0.f, iG2 = 0.f;
+  if constexpr (K == 2) {
+    det = p.G[0] * p.G[2] - p.G[1] * p.G[1];
+    iG2 = 1.f / p.G[2];
+  }
   for (int k0 = p.lo[0]; k0 <= p.hi[0]; ++k0) {
     const float d0 = (__ldg(g.ax[0].coords + k0) - p.qh[0]) - p.ql[0];
     if constexpr (K == 1) {
@@ -136,21 +153,27 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
         if (GN) Sb[q] = 0.f;
       }
       const size_t rbase = abase + (size_t)k0 * D1;
+      const float rem = fmaf(-d0 * d0, det, p.G[2]);
+      const float rc = (p.qh[1] - p.G[1] * d0 * iG2 - g.ax[1].first) * g.ax[1].inv_step;
+      const float rh = sqrtf(fmaxf(rem, 0.f)) * iG2 * g.ax[1].inv_step * 1.0001f + 1e-3f;
+      const float rlo = ceilf(rc - rh), rhi = floorf(rc + rh);
+      const int c_lo = (int)fminf(fmaxf(rlo, (float)p.lo[1]), (float)p.hi[1] + 1.f);
+      const int c_hi = (int)fmaxf(fminf(rhi, (float)p.hi[1]), (float)p.lo[1] - 1.f);
       // the row is walked in chunks of kRowChunk cells whose field values
       // and coordinates are loaded together first, so the loads overlap
       // instead of each cell waiting for its own
-      for (int kb = p.lo[1]; kb <= p.hi[1]; kb += kRowChunk) {
+      for (int kb = c_lo; kb <= c_hi; kb += kRowChunk) {
         float cv[kRowChunk], pv[kRowChunk], bv[GN ? kRowChunk : 1];
 #pragma unroll
         for (int i = 0; i < kRowChunk; ++i) {
-          const int k1 = min(kb + i, p.hi[1]);
+          const int k1 = min(kb + i, c_hi);
           cv[i] = __ldg(field + rbase + k1);
           pv[i] = __ldg(g.ax[1].coords + k1);
           if (GN) bv[i] = bfield ? __ldg(bfield + rbase + k1) : in.beta_const;
         }
 #pragma unroll
         for (int i = 0; i < kRowChunk; ++i) {
-          if (kb + i > p.hi[1]) break;
+          if (kb + i > c_hi) break;
           const float d1 = (pv[i] - p.qh[1]) - p.ql[1];
           const float m = fmaf(d1, fmaf(p.G[2], d1, u), t0);
           if (m <= 1.f) {
@@ -576,11 +599,16 @@ int set_tuning(int key, int value) {
     g_deriv_min_angles = value;
     return kOk;
   }
+  if (key == 2 && (value == 0 || (value >= 1 && value <= 32 && (value & (value - 1)) == 0))) {
+    g_deriv_atoms_per_warp = value;
+    return kOk;
+  }
   return kErrArg;
 }
 
 int get_tuning(int key) {
-  return key == 0 ? g_deriv_target_warps : key == 1 ? g_deriv_min_angles : -1;
+  return key == 0 ? g_deriv_target_warps : key == 1 ? g_deriv_min_angles
+         : key == 2 ? g_deriv_atoms_per_warp : -1;
 }
 
 size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order) {

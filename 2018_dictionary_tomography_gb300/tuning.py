@@ -2,7 +2,7 @@
 
 The derivative launch splits (atoms x angle chunks) into about
 ``GR_TUNE_DERIV_WARPS`` warps with at least ``GR_TUNE_DERIV_MIN_ANGLES`` angles
-per lane group; the best split depends on the atom count, angle count,
+per lane group and ``GR_TUNE_DERIV_ATOMS_PER_WARP`` atoms per warp; the best split depends on the atom count, angle count,
 support sizes and derivative order.  ``autotune_derivs`` times candidate
 splits on the actual problem with CUDA events and keeps the fastest; results
 are cached per shape class (detector dims, log2 atom count, log2 angle count,
@@ -15,20 +15,23 @@ import torch
 
 from . import _lib, engine
 
-WARPS = (1024, 2048, 4096, 8192, 16384, 32768)
+WARPS = (4096, 8192, 16384, 32768, 65536, 131072)
 MIN_ANGLES = (1, 2, 4, 8)
+ATOMS_PER_WARP = (1, 2, 4, 8)
 _cache = {}
 
 
-def set_split(target_warps, min_angles):
+def set_split(target_warps, min_angles, atoms_per_warp=None):
     lib = _lib.load()
     _lib.check(lib.gr_set_tuning(0, int(target_warps)), "gr_set_tuning")
     _lib.check(lib.gr_set_tuning(1, int(min_angles)), "gr_set_tuning")
+    if atoms_per_warp is not None:
+        _lib.check(lib.gr_set_tuning(2, int(atoms_per_warp)), "gr_set_tuning")
 
 
 def get_split():
     lib = _lib.load()
-    return int(lib.gr_get_tuning(0)), int(lib.gr_get_tuning(1))
+    return int(lib.gr_get_tuning(0)), int(lib.gr_get_tuning(1)), int(lib.gr_get_tuning(2))
 
 
 def shape_key(atoms, geom, order, psf=False):
@@ -39,13 +42,16 @@ def shape_key(atoms, geom, order, psf=False):
 def autotune_derivs(atoms, geom, field, beta_field=None, beta_const=1.0, order=1,
                     psf=False, reps=5, candidates=None):
     """Time every candidate split on this problem; apply and return the best
-    (target_warps, min_angles, ms)."""
+    (target_warps, min_angles, atoms_per_warp, ms)."""
     key = shape_key(atoms, geom, order, psf)
-    cands = candidates or [(w, m) for w in WARPS for m in MIN_ANGLES]
+    cands = candidates or [(w, m, g) for w in WARPS for m in MIN_ANGLES
+                           for g in ATOMS_PER_WARP]
     saved = get_split()
     best = None
-    for w, m in cands:
-        set_split(w, m)
+    for cand in cands:
+        w, m = cand[0], cand[1]
+        g = cand[2] if len(cand) > 2 else saved[2]
+        set_split(w, m, g)
         engine.atom_derivs(atoms, geom, "field", field, beta_field, beta_const, order, psf=psf)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
@@ -54,13 +60,13 @@ def autotune_derivs(atoms, geom, field, beta_field=None, beta_const=1.0, order=1
         b.record()
         torch.cuda.synchronize()
         ms = a.elapsed_time(b) / reps
-        if best is None or ms < best[2]:
-            best = (w, m, ms)
+        if best is None or ms < best[3]:
+            best = (w, m, g, ms)
     if best is None:
         set_split(*saved)
         return None
-    _cache[key] = best[:2]
-    set_split(best[0], best[1])
+    _cache[key] = best[:3]
+    set_split(*best[:3])
     return best
 
 

@@ -154,3 +154,24 @@ def test_atom_order_does_not_change_results(eng, cuda_ready, case, psf):
         assert entry_relerr(H1.cpu().numpy(), H0.cpu().numpy()) < 1e-6
         assert relerr(f1.cpu().numpy(), f0.cpu().numpy()) < 1e-6
 
+
+
+@pytest.mark.parametrize("case", ["2d", "3d"])
+def test_work_split_does_not_change_results(eng, cuda_ready, case):
+    """Every derivative work split (warps, angles per lane group, atoms per
+    warp) gives the same per-atom results up to rounding of the chunk sums."""
+    import importlib
+    tuning = importlib.import_module("2018_dictionary_tomography_gb300.tuning")
+    g, I, x, r = _setup(case, seed=23)
+    geom, atoms = engine_geometry(g), engine_atoms(I, x, r)
+    field = torch.from_numpy(go.radproj(I, x, r, g) * 0.9).float().cuda()
+    saved = tuning.get_split()
+    try:
+        f0, g0, H0 = eng.atom_derivs(atoms, geom, "inner", field, order=2)
+        for split in ((1024, 1, 1), (32768, 2, 2), (4096, 1, 8), (65536, 4, 0)):
+            tuning.set_split(*split)
+            f1, g1, H1 = eng.atom_derivs(atoms, geom, "inner", field, order=2)
+            assert entry_relerr(g1.cpu().numpy(), g0.cpu().numpy()) < 1e-6
+            assert entry_relerr(H1.cpu().numpy(), H0.cpu().numpy()) < 1e-6
+    finally:
+        tuning.set_split(*saved)
