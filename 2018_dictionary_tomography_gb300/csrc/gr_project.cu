@@ -8,15 +8,14 @@
 //      m <= 1 and set the atom's bit in the bitmap of every detector tile the
 //      box touches (integer atomicOr, so the bitmap does not depend on the
 //      order in which pairs run).
-//   2. gr_project_kernel: one warp per (angle, tile).  The warp reads its
-//      bitmap, so it meets its atoms in increasing index order, computes the
-//      pair data of up to 32 atoms at once (one per lane), then evaluates each
-//      atom densely over its support box clipped to the tile, lanes spread
-//      over the box cells, accumulating into shared-memory cell sums with a
-//      compensated (Kahan/Neumaier) add.  Each cell therefore sums its atoms in
-//      atom-index order, with no float atomics: results are bitwise
-//      reproducible.  The epilogue writes the sinogram and, fused, the
-//      residual or KL weight fields and per-tile loss partials.
+//   2. gr_project3d_kernel (3D / 2.5D detectors) and gr_project1d_kernel
+//      (2D sinograms): one warp per (angle, tile) item.  The warp meets the
+//      tile's atoms in increasing index order and sums every cell over its
+//      atoms in that order with a compensated add and no float atomics, so
+//      results are bitwise reproducible.  The epilogue writes the sinogram
+//      and, fused, the residual or KL weight fields and per-tile loss
+//      partials.  The 3D kernel is persistent: warps take items from a
+//      counter, so tiles of uneven weight do not leave warps idle.
 //   3. gr_loss_finalize_kernel: fixed-order FP64 sum of the loss partials.
 #include "gr_kernels.cuh"
 
@@ -51,31 +50,6 @@ __global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
   }
 }
 
-// Broadcast-ready pair data for the projection loop.
-struct PairLite {
-  float qh0, ql0, qh1, ql1, G0, G1, G2, l2amp, sgn;
-  int lo0, hi0, lo1, hi1;
-};
-
-__device__ __forceinline__ PairLite shfl_pair(const PairLite &v, int src) {
-  PairLite o;
-  const unsigned m = 0xffffffffu;
-  o.qh0 = __shfl_sync(m, v.qh0, src);
-  o.ql0 = __shfl_sync(m, v.ql0, src);
-  o.qh1 = __shfl_sync(m, v.qh1, src);
-  o.ql1 = __shfl_sync(m, v.ql1, src);
-  o.G0 = __shfl_sync(m, v.G0, src);
-  o.G1 = __shfl_sync(m, v.G1, src);
-  o.G2 = __shfl_sync(m, v.G2, src);
-  o.l2amp = __shfl_sync(m, v.l2amp, src);
-  o.sgn = __shfl_sync(m, v.sgn, src);
-  o.lo0 = __shfl_sync(m, v.lo0, src);
-  o.hi0 = __shfl_sync(m, v.hi0, src);
-  o.lo1 = __shfl_sync(m, v.lo1, src);
-  o.hi1 = __shfl_sync(m, v.hi1, src);
-  return o;
-}
-
 // Per-cell KL term f log(f/g) - f + g = g h(u), u = f/g, h(u) = u log u - u + 1,
 // evaluated without cancellation: a series in e = u - 1 near u = 1.
 __device__ __forceinline__ float kl_term(float f, float g) {
@@ -94,121 +68,149 @@ __device__ __forceinline__ float kl_term(float f, float g) {
   return g * h;
 }
 
-template <int K, bool KAHAN>
+// 3D detectors: a warp per (angle, tile) item.  Its atoms come from the
+// tile's bitmap in increasing index order; the pair data of each batch of 32
+// atoms is computed in parallel (one atom per lane) and staged in shared
+// memory (three float4 per atom, read as broadcasts, the tile-local clipped
+// box packed in one word); then each atom is evaluated densely over its box,
+// lanes spread over the box cells, into shared-memory cell sums with a
+// compensated (Kahan/Neumaier) add.  Each cell therefore sums its atoms in
+// atom-index order, with no float atomics: results are bitwise reproducible.
+// Sums and compensations use a padded row stride S so that the cells of one
+// box row-block fall in different banks.  Tiles are ROWS x 32 cells.
+template <int ROWS, int S>
+struct Proj3Smem {
+  static constexpr int kAcc = ROWS * S;
+  static constexpr int kRing = 128;     // ring list of atom indices
+  static constexpr int kFloats = 2 * kAcc + 32 * 12 + ROWS + 32 + kRing;
+};
+
+template <int ROWS, int S>
 __global__ void __launch_bounds__(kProjWarps * 32)
-    gr_project_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
-                      int W, ProjOut out) {
+    gr_project3d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap, int W,
+                        ProjOut out, int *next_item) {
+  using L = Proj3Smem<ROWS, S>;
+  constexpr int kRing = L::kRing;
+  static_assert((kRing & (kRing - 1)) == 0 && kRing >= 64, "ring");
   extern __shared__ float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int item = blockIdx.x * kProjWarps + warp;
   const int n_items = g.n_angles * tc.ntiles;
-  if (item >= n_items) return;  // whole warp leaves together
-  const int cells = tc.t0 * tc.t1;
-  float *acc = smem + (size_t)warp * kProjWarpFloats;
-  float *cmp = acc + kTileCells;
-  float *pc0 = cmp + kTileCells;              // coordinates of tile rows
-  float *pc1 = pc0 + 64;                      // coordinates of tile cols
-  int *list = reinterpret_cast<int *>(pc1 + kTileDim1);
+  float *acc = smem + (size_t)warp * L::kFloats;
+  float *cmp = acc + L::kAcc;
+  float4 *prm = reinterpret_cast<float4 *>(cmp + L::kAcc);  // 16-byte aligned
+  float *pc0 = reinterpret_cast<float *>(prm + 32 * 3);
+  float *pc1 = pc0 + ROWS;
+  int *list = reinterpret_cast<int *>(pc1 + 32);
 
+  // persistent warps: each takes the next (angle, tile) item from a counter,
+  // so heavy tiles do not hold a block's other warps idle; what an item
+  // computes does not depend on which warp takes it
+  for (;;) {
+  int item = 0;
+  if (lane == 0) item = atomicAdd(next_item, 1);
+  item = __shfl_sync(0xffffffffu, item, 0);
+  if (item >= n_items) break;  // whole warp leaves together
+  __syncwarp();  // the previous item's epilogue reads are done
   const int a = item / tc.ntiles, t = item - a * tc.ntiles;
   const int tr = t / tc.nt1, tcix = t - tr * tc.nt1;
-  const int r0 = tr * tc.t0, c0 = tcix * tc.t1;
-  const int D0 = g.ax[0].n, D1 = (K == 1) ? 1 : g.ax[1].n;
+  const int r0 = tr * ROWS, c0 = tcix * 32;
+  const int D0 = g.ax[0].n, D1 = g.ax[1].n;
 
-  for (int e = lane; e < cells; e += 32) {
+  for (int e = lane; e < L::kAcc; e += 32) {
     acc[e] = 0.f;
-    if (KAHAN) cmp[e] = 0.f;
+    cmp[e] = 0.f;
   }
-  for (int e = lane; e < tc.t0; e += 32)
+  for (int e = lane; e < ROWS; e += 32)
     pc0[e] = (r0 + e < D0) ? g.ax[0].coords[r0 + e] : 0.f;
-  if constexpr (K == 2)
-    for (int e = lane; e < tc.t1; e += 32)
-      pc1[e] = (c0 + e < D1) ? g.ax[1].coords[c0 + e] : 0.f;
-  Frame<K> f;
-  load_frame<K>(g.frames, a, f);
+  pc1[lane] = (c0 + lane < D1) ? g.ax[1].coords[c0 + lane] : 0.f;
+  Frame<2> f;
+  load_frame<2>(g.frames, a, f);
   __syncwarp();
 
+  // The tile's atoms, in index order, pass through a ring list: a refill
+  // reads 32 bitmap words (one per lane) and appends the atoms of as many
+  // whole words as fit, so every batch but the last holds 32 atoms however
+  // sparse the bitmap is.
   const uint32_t *words = bitmap + (size_t)item * W;
-  for (int wb = 0; wb < W; wb += kListWords) {
-    // compact the set bits of kListWords bitmap words into list[] in order
-    const int wi = wb + (lane < kListWords ? lane : 0);
-    uint32_t wd = (lane < kListWords && wi < W) ? words[wi] : 0u;
-    int cnt = __popc(wd), incl = cnt;
+  int head = 0, count = 0, wb = 0;
+  while (true) {
+    while (count < 32 && wb < W) {
+      const int wi = wb + lane;
+      uint32_t wd = wi < W ? words[wi] : 0u;
+      const int cnt = __popc(wd);
+      int incl = cnt;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    int pos = incl - cnt;
-    while (wd) {
-      const int b = __ffs(wd) - 1;
-      list[pos++] = (wi << 5) + b;
-      wd &= wd - 1;
-    }
-    __syncwarp();
-    for (int bs = 0; bs < total; bs += 32) {
-      const int idx = bs + lane;
-      PairLite mine;
-      mine.lo0 = 1;
-      mine.hi0 = 0;
-      mine.lo1 = 1;
-      mine.hi1 = 0;
-      if (idx < total) {
-        Pair<K> p;
-        pair_setup<K>(at, list[idx], f, g, p);
-        mine.qh0 = p.qh[0];
-        mine.ql0 = p.ql[0];
-        mine.G0 = p.G[0];
-        mine.G1 = p.G[1];
-        mine.G2 = p.G[2];
-        mine.l2amp = p.l2amp;
-        mine.sgn = p.sgn;
-        mine.lo0 = max(p.lo[0], r0);
-        mine.hi0 = min(p.hi[0], r0 + tc.t0 - 1);
-        if constexpr (K == 2) {
-          mine.qh1 = p.qh[1];
-          mine.ql1 = p.ql[1];
-          mine.lo1 = max(p.lo[1], c0);
-          mine.hi1 = min(p.hi[1], c0 + tc.t1 - 1);
-        } else {
-          mine.qh1 = 0.f;
-          mine.ql1 = 0.f;
-          mine.lo1 = 0;
-          mine.hi1 = 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      // incl never decreases along the lanes, so the lanes that fit are a
+      // prefix; at least one word fits (count < 32, a word adds <= 32)
+      const bool take = incl <= kRing - count;
+      const unsigned tmask = __ballot_sync(0xffffffffu, take);
+      const int ntake = __popc(tmask);
+      if (take) {
+        int pos = head + count + incl - cnt;
+        while (wd) {
+          const int b = __ffs(wd) - 1;
+          list[(pos++) & (kRing - 1)] = (wi << 5) + b;
+          wd &= wd - 1;
         }
       }
-      const int nb = min(32, total - bs);
-      for (int s = 0; s < nb; ++s) {
-        const PairLite q = shfl_pair(mine, s);
-        if (q.lo0 > q.hi0 || q.lo1 > q.hi1) continue;  // warp-uniform
-        const int bw = q.hi1 - q.lo1 + 1;
-        const int ncell = (q.hi0 - q.lo0 + 1) * bw;
-        const float inv_bw = 1.f / (float)bw;
+      count += __shfl_sync(0xffffffffu, incl, ntake - 1);
+      wb += ntake;
+      __syncwarp();
+    }
+    if (count == 0) break;
+    {
+      __syncwarp();  // every lane is done with the previous batch's data
+      const int nb = min(32, count);
+      float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A, C = A;
+      C.y = __int_as_float(0x000000ff);  // empty box: rows 255..0
+      if (lane < nb) {
+        Pair<2> p;
+        pair_setup<2>(at, list[(head + lane) & (kRing - 1)], f, g, p);
+        const int lr0 = max(p.lo[0], r0) - r0, lr1 = min(p.hi[0], r0 + ROWS - 1) - r0;
+        const int lc0 = max(p.lo[1], c0) - c0, lc1 = min(p.hi[1], c0 + 31) - c0;
+        const bool empty = lr0 > lr1 || lc0 > lc1;
+        A = make_float4(p.qh[0], p.ql[0], p.qh[1], p.ql[1]);
+        B = make_float4(p.G[0], 2.f * p.G[1], p.G[2], p.l2amp);
+        C.x = p.sgn;
+        C.y = __int_as_float(empty ? 0x000000ff
+                                   : (lr0 | (lr1 << 8) | (lc0 << 16) | (lc1 << 24)));
+      }
+      head += nb;
+      count -= nb;
+      prm[lane * 3 + 0] = A;
+      prm[lane * 3 + 1] = B;
+      prm[lane * 3 + 2] = C;
+      __syncwarp();
+      for (int sI = 0; sI < nb; ++sI) {
+        const float4 qC = prm[sI * 3 + 2];
+        const unsigned box = (unsigned)__float_as_int(qC.y);
+        const int lr0 = box & 0xff, lr1 = (box >> 8) & 0xff;
+        const int lc0 = (box >> 16) & 0xff, lc1 = box >> 24;
+        if (lr0 > lr1) continue;  // warp-uniform
+        const float4 qA = prm[sI * 3 + 0], qB = prm[sI * 3 + 1];
+        const int bw = lc1 - lc0 + 1;
+        const int ncell = (lr1 - lr0 + 1) * bw;
+        const float inv_bw = __frcp_rn((float)bw);
         for (int e = lane; e < ncell; e += 32) {
+          // (e + 1/2) / bw is at least 1/(2 bw) from an integer, far more
+          // than the rounding of the product: the row index is exact
           const int rr = (int)(((float)e + 0.5f) * inv_bw);
-          const int cc = e - rr * bw;
-          const int lr = q.lo0 - r0 + rr;        // tile-local row
-          const int lc = (K == 2) ? (q.lo1 - c0 + cc) : 0;
-          const float d0 = (pc0[lr] - q.qh0) - q.ql0;
-          float m;
-          if constexpr (K == 2) {
-            const float d1 = (pc1[lc] - q.qh1) - q.ql1;
-            m = fmaf(d0, fmaf(q.G0, d0, 2.f * q.G1 * d1), q.G2 * d1 * d1);
-          } else {
-            m = q.G0 * d0 * d0;
-          }
+          const int lr = lr0 + rr;
+          const int lc = lc0 + (e - rr * bw);
+          const float d0 = (pc0[lr] - qA.x) - qA.y;
+          const float d1 = (pc1[lc] - qA.z) - qA.w;
+          const float m = fmaf(d0, fmaf(qB.x, d0, qB.y * d1), qB.z * d1 * d1);
           if (m <= 1.f) {
-            const float v = q.sgn * ex2_approx(fmaf(m, kNegThirtyLog2e, q.l2amp));
-            const int ci = lr * tc.t1 + lc;
-            if (KAHAN) {
-              const float s0 = acc[ci];
-              const float tt = s0 + v;
-              cmp[ci] += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
-              acc[ci] = tt;
-            } else {
-              acc[ci] += v;
-            }
+            const float v = qC.x * ex2_approx(fmaf(m, kNegThirtyLog2e, qB.w));
+            const int ci = lr * S + lc;
+            const float s0 = acc[ci];
+            const float tt = s0 + v;
+            cmp[ci] += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
+            acc[ci] = tt;
           }
         }
         __syncwarp();
@@ -219,11 +221,12 @@ __global__ void __launch_bounds__(kProjWarps * 32)
 
   // epilogue: write the tile, fused fit fields and loss partial
   float lsum = 0.f, lcmp = 0.f;
-  for (int e = lane; e < cells; e += 32) {
-    const int lr = e / tc.t1, lc = e - lr * tc.t1;
-    const int row = r0 + lr, col = c0 + lc;
+  for (int e = lane; e < ROWS * 32; e += 32) {
+    const int lr = e >> 5;
+    const int row = r0 + lr, col = c0 + lane;
     if (row >= D0 || col >= D1) continue;
-    const float v = KAHAN ? (acc[e] + cmp[e]) : acc[e];
+    const int ci = lr * S + lane;
+    const float v = acc[ci] + cmp[ci];
     const size_t gi = ((size_t)a * D0 + row) * D1 + col;
     if (out.R) out.R[gi] = v;
     float l = 0.f;
@@ -246,6 +249,7 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   if (out.loss_part) {
     double d = warp_sum_d((double)lsum + (double)lcmp);
     if (lane == 0) out.loss_part[item] = d;
+  }
   }
 }
 
@@ -579,7 +583,40 @@ __global__ void gr_loss_finalize_kernel(const double *part, int n, double *out) 
   if (threadIdx.x == 0) out[0] = sh[0];
 }
 
-TileCfg make_tiles(int K, int D0, int D1) {
+// Form of the point-sampled 3D projection (gr_set_tuning key 3):
+// Tiling of the point-sampled 3D projection (gr_set_tuning key 3):
+// 1: 16-row tiles (more resident warps), 2: 32-row tiles (fewer atoms cut
+// by tile edges).
+int g_proj_form = 1;
+
+static int proj_rows(int form) { return form == 2 ? kTileDim0 : 16; }
+
+template <int ROWS, int S>
+static void launch_project3d(int blocks, const Atoms &at, const Geom &g, const TileCfg &tc,
+                             const uint32_t *bitmap, int W, const ProjOut &o, int *next_item,
+                             cudaStream_t stream) {
+  constexpr size_t smem = kProjWarps * Proj3Smem<ROWS, S>::kFloats * sizeof(float);
+  // below the 48 KB that needs no opt-in, so no function attribute is set
+  // (safe under stream capture)
+  static_assert(smem <= 48 * 1024, "smem");
+  // persistent grid: the resident blocks of every SM, at most one per 4 items
+  static int resident[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (resident[dev] == 0) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gr_project3d_kernel<ROWS, S>,
+                                                  kProjWarps * 32, smem);
+    resident[dev] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  }
+  const int grid = blocks < resident[dev] ? blocks : resident[dev];
+  gr_project3d_kernel<ROWS, S><<<grid, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o,
+                                                                        next_item);
+}
+
+TileCfg make_tiles(int K, int D0, int D1, int rows) {
   TileCfg tc;
   if (K == 1) {
     tc.t0 = kTile1D;
@@ -587,7 +624,7 @@ TileCfg make_tiles(int K, int D0, int D1) {
     tc.nt0 = (D0 + tc.t0 - 1) / tc.t0;
     tc.nt1 = 1;
   } else {
-    tc.t0 = kTileDim0;
+    tc.t0 = rows;
     tc.t1 = kTileDim1;
     tc.nt0 = (D0 + tc.t0 - 1) / tc.t0;
     tc.nt1 = (D1 + tc.t1 - 1) / tc.t1;
@@ -597,10 +634,13 @@ TileCfg make_tiles(int K, int D0, int D1) {
 }
 
 size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1) {
-  TileCfg tc = make_tiles(K, D0, D1);
+  // sized for the smaller of the point-sampled and pixel-integrated tilings
+  const int rows = proj_rows(g_proj_form) < kTileDim0 ? proj_rows(g_proj_form) : kTileDim0;
+  TileCfg tc = make_tiles(K, D0, D1, rows);
   const size_t W = (size_t)(n_atoms + 31) / 32;
   const size_t items = (size_t)n_angles * tc.ntiles;
-  size_t bytes = align_up(items * W * sizeof(uint32_t));
+  size_t bytes = align_up(sizeof(int));  // work counter of the persistent kernel
+  bytes += align_up(items * W * sizeof(uint32_t));
   bytes += align_up(items * sizeof(double));
   return bytes;
 }
@@ -610,22 +650,27 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
                    cudaStream_t stream) {
   const int K = g.K;
   const int D0 = g.ax[0].n, D1 = K == 1 ? 1 : g.ax[1].n;
-  TileCfg tc = make_tiles(K, D0, D1);
+  const int form = g_proj_form;
+  TileCfg tc = make_tiles(K, D0, D1, (K == 2 && !o_in.psf) ? proj_rows(form) : kTileDim0);
   const int W = (at.n + 31) / 32;
   const size_t items = (size_t)g.n_angles * tc.ntiles;
   const size_t need = project_workspace_bytes(K, at.n, g.n_angles, D0, D1);
   if (ws_bytes < need || (ws == nullptr && need > 0)) return kErrWorkspace;
   char *wp = static_cast<char *>(ws);
+  int *next_item = reinterpret_cast<int *>(wp);
+  wp += align_up(sizeof(int));
   uint32_t *bitmap = reinterpret_cast<uint32_t *>(wp);
   wp += align_up(items * W * sizeof(uint32_t));
   double *loss_part = reinterpret_cast<double *>(wp);
+  // one clear covers the work counter and the bitmap
+  if (cudaMemsetAsync(ws, 0, align_up(sizeof(int)) + items * W * sizeof(uint32_t), stream) !=
+      cudaSuccess)
+    return kErrLaunch;
   ProjOut o = o_in;
   o.loss_part = loss_out ? loss_part : nullptr;
   // half-width of the (square) cells of the pixel-integrated operator
   const float psf_s = 0.5f / g.ax[0].inv_step;
   if (W > 0) {
-    if (cudaMemsetAsync(bitmap, 0, items * W * sizeof(uint32_t), stream) != cudaSuccess)
-      return kErrLaunch;
     dim3 bgrid((at.n + 127) / 128, g.n_angles);
     if (o.psf) {
       if (K == 1) gr_psf_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, psf_s);
@@ -649,8 +694,10 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
       gr_psf_project_kernel<2><<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, psf_s, o);
   } else if (K == 1) {
     gr_project1d_kernel<true><<<blocks, kProjWarps * 32, 0, stream>>>(at, g, tc, bitmap, W, o);
+  } else if (form == 2) {
+    launch_project3d<32, 34>(blocks, at, g, tc, bitmap, W, o, next_item, stream);
   } else {
-    gr_project_kernel<2, true><<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o);
+    launch_project3d<16, 37>(blocks, at, g, tc, bitmap, W, o, next_item, stream);
   }
   note_launches(1);
   if (loss_out) {

@@ -29,6 +29,12 @@ def set_split(target_warps, min_angles, atoms_per_warp=None):
         _lib.check(lib.gr_set_tuning(2, int(atoms_per_warp)), "gr_set_tuning")
 
 
+def set_projection_tiling(form):
+    """1: 16 x 32-cell tiles (default), 2: 32 x 32 (3D point-sampled
+    projection)."""
+    _lib.check(_lib.load().gr_set_tuning(3, int(form)), "gr_set_tuning")
+
+
 def get_split():
     lib = _lib.load()
     return int(lib.gr_get_tuning(0)), int(lib.gr_get_tuning(1)), int(lib.gr_get_tuning(2))

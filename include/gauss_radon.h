@@ -245,20 +245,28 @@ int gr_probe_ex2(int blocks, int threads, int iters, float *sink, void *stream);
 unsigned long long gr_launch_count(void);
 
 /*
- * Work-split knobs of the derivative kernels, process-wide (no counterpart
+ * Work-split knobs of the kernels, process-wide (no counterpart
  * in the reference).  GR_TUNE_DERIV_WARPS: about this many warps per
  * derivative launch (atoms x angle chunks; default 131072);
  * GR_TUNE_DERIV_MIN_ANGLES: at least this many angles per lane group in a
  * chunk (default 1); GR_TUNE_DERIV_ATOMS_PER_WARP: atoms sharing a warp, a
  * power of two up to 32, the other lanes taking further angles of the same
  * atoms (default 0: automatic, one atom per warp for Hessians and for series
- * of 1024 or more angles, else four).  Set them before gr_workspace_bytes and keep them fixed
- * while launches that used the old values are in flight.  Results do not
- * depend on them beyond FP rounding of the chunk sums.  gr_set_tuning returns
+ * of 1024 or more angles, else four).  GR_TUNE_PROJ_TILING: tiles of the
+ * point-sampled 3D projection, 1 = 16 x 32 cells (default, more resident
+ * warps), 2 = 32 x 32 (fewer atoms cut by tile edges).  Set them before
+ * gr_workspace_bytes and keep them fixed while launches that used the old
+ * values are in flight.  Results do not depend on them beyond FP rounding of
+ * the derivative chunk sums (the tiling leaves projections bitwise equal).  gr_set_tuning returns
  * GR_ERR_ARG for an unknown key or out-of-range value; gr_get_tuning returns
  * the current value (-1 for an unknown key).
  */
-enum { GR_TUNE_DERIV_WARPS = 0, GR_TUNE_DERIV_MIN_ANGLES = 1, GR_TUNE_DERIV_ATOMS_PER_WARP = 2 };
+enum {
+  GR_TUNE_DERIV_WARPS = 0,
+  GR_TUNE_DERIV_MIN_ANGLES = 1,
+  GR_TUNE_DERIV_ATOMS_PER_WARP = 2,
+  GR_TUNE_PROJ_TILING = 3
+};
 int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);
 

@@ -175,3 +175,23 @@ def test_work_split_does_not_change_results(eng, cuda_ready, case):
             assert entry_relerr(H1.cpu().numpy(), H0.cpu().numpy()) < 1e-6
     finally:
         tuning.set_split(*saved)
+
+
+def test_projection_tiling_is_bitwise_neutral(eng, cuda_ready):
+    """Both 3D tilings sum every cell over its atoms in index order: the
+    sinogram and loss are bitwise equal."""
+    import importlib
+    tuning = importlib.import_module("2018_dictionary_tomography_gb300.tuning")
+    g, I, x, r = _setup("3d", seed=31)
+    geom, atoms = engine_geometry(g), engine_atoms(I, x, r)
+    data = torch.from_numpy(go.radproj(I, x, r, g) * 1.1).float().cuda()
+    outs = []
+    try:
+        for form in (1, 2):
+            tuning.set_projection_tiling(form)
+            fw = eng.fit_forward(atoms, geom, data, "l2", want_R=True)
+            outs.append((fw["R"].clone(), fw["loss"].clone()))
+    finally:
+        tuning.set_projection_tiling(1)
+    assert torch.equal(outs[0][0], outs[1][0])
+    assert relerr(outs[0][0].cpu().numpy(), go.radproj(I, x, r, g)) < TOL
