@@ -42,7 +42,7 @@ EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
            "gr_fit_forward", "gr_atom_derivs", "gr_count_support", "gr_probe_ex2",
            "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj", "gr_newton_accept",
            "gr_psf_radproj", "gr_psf_fit_forward", "gr_psf_atom_derivs", "gr_psf_volproj",
-           "gr_set_tuning", "gr_get_tuning")
+           "gr_set_tuning", "gr_get_tuning", "gr_kernel_timer", "gr_kernel_timer_read")
 
 _lock = threading.Lock()
 _lib = None
@@ -122,6 +122,11 @@ def load(build_if_missing=True):
         lib.gr_set_tuning.argtypes = [ctypes.c_int, ctypes.c_int]
         lib.gr_get_tuning.restype = ctypes.c_int
         lib.gr_get_tuning.argtypes = [ctypes.c_int]
+        lib.gr_kernel_timer.restype = ctypes.c_int
+        lib.gr_kernel_timer.argtypes = [ctypes.c_int, ctypes.c_int]
+        lib.gr_kernel_timer_read.restype = ctypes.c_int
+        lib.gr_kernel_timer_read.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                             ctypes.POINTER(ctypes.c_int)]
         lib.gr_launch_count.restype = ctypes.c_ulonglong
         lib.gr_launch_count.argtypes = []
         _lib = lib

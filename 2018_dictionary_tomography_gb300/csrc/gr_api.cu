@@ -276,6 +276,12 @@ int gr_probe_ex2(int blocks, int threads, int iters, float *sink, void *stream) 
 
 unsigned long long gr_launch_count(void) { return g_launches.load(); }
 
+int gr_kernel_timer(int which, int enable) { return gr::timer_enable(which, enable); }
+
+int gr_kernel_timer_read(int which, double *total_ms, int *launches) {
+  return gr::timer_read(which, total_ms, launches);
+}
+
 int gr_set_tuning(int key, int value) { return set_tuning(key, value); }
 
 int gr_get_tuning(int key) { return get_tuning(key); }

@@ -474,43 +474,35 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// Sum chunk partials (FP64) in a fixed order: a block covers 32 atoms x 8
-// chunk slices; thread (atom, slice) sums chunks slice, slice + 8, ... (reads
-// of consecutive atoms are coalesced), then slice 0 adds the 8 slice sums in
-// slice order.
+// Sum chunk partials (FP64) in chunk order, expand the packed Hessian and
+// apply the isotropic chain rule r_aniso = (s, .., s, 0, ..).  A block covers
+// 32 atoms; its 8 warps share out the partial values (reads of consecutive
+// atoms are coalesced), then warp 0 finishes the atoms.
 constexpr int kRedSlices = 8;
-__global__ void __launch_bounds__(32 * kRedSlices)
-    gr_deriv_reduce_kernel(const float *part, DerivCfg cfg, int n, double *sums) {
-  __shared__ double sh[kRedSlices][32];
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int j = blockIdx.x * 32 + tx;
-  const int q = blockIdx.y;
-  double s = 0.0;
-  if (j < n)
-    for (int c = ty; c < cfg.nchunks; c += kRedSlices)
-      s += (double)part[((size_t)c * cfg.qn + q) * n + j];
-  sh[ty][tx] = s;
-  __syncthreads();
-  if (ty == 0 && j < n) {
-    double t = 0.0;
-#pragma unroll
-    for (int k = 0; k < kRedSlices; ++k) t += sh[k][tx];
-    sums[(size_t)q * n + j] = t;
-  }
-}
-
-// Expand the packed Hessian and apply the isotropic chain rule
-// r_aniso = (s, .., s, 0, ..).
 template <int K>
-__global__ void gr_deriv_finalize_kernel(const double *sums, DerivCfg cfg, int n,
-                                         int deriv_order, int r_iso, DerivOut out,
-                                         const double *f_extra, const int *order) {
+__global__ void __launch_bounds__(32 * kRedSlices)
+    gr_deriv_finalize_kernel(const float *part, DerivCfg cfg, int n, int deriv_order,
+                             int r_iso, DerivOut out, const double *f_extra,
+                             const int *order) {
   constexpr int D = K + 1;
   constexpr int P = n_par<K>();
-  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-  if (slot >= n) return;
-  double v[1 + P + P * (P + 1) / 2];
-  for (int q = 0; q < cfg.qn; ++q) v[q] = sums[(size_t)q * n + slot];
+  constexpr int QN = 1 + P + P * (P + 1) / 2;
+  // chunk sums in FP64 in chunk order: thread (atom, ty) sums values
+  // q = ty, ty + kRedSlices, ... of its atom, all loads independent
+  __shared__ double vs[QN][32];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int slot = blockIdx.x * 32 + tx;
+  if (slot < n)
+    for (int q = ty; q < cfg.qn; q += kRedSlices) {
+      double t = 0.0;
+#pragma unroll 4
+      for (int c = 0; c < cfg.nchunks; ++c) t += (double)part[((size_t)c * cfg.qn + q) * n + slot];
+      vs[q][tx] = t;
+    }
+  __syncthreads();
+  if (ty != 0 || slot >= n) return;
+  double v[QN];
+  for (int q = 0; q < cfg.qn; ++q) v[q] = vs[q][tx];
   const int j = order ? order[slot] : slot;  // atom of the slot
   double f = v[0] + (f_extra ? f_extra[0] : 0.0);
   double H[P][P];
@@ -618,7 +610,6 @@ int get_tuning(int key) {
 size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order) {
   DerivCfg c = deriv_cfg(K, n_atoms, n_angles, order);
   size_t b = align_up((size_t)c.nchunks * c.qn * (size_t)n_atoms * sizeof(float));
-  b += align_up((size_t)c.qn * n_atoms * sizeof(double));
   b += align_up(kSumSqBlocks * sizeof(double)) + align_up(sizeof(double));
   return b;
 }
@@ -635,8 +626,6 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
   char *wp = static_cast<char *>(ws);
   float *part = reinterpret_cast<float *>(wp);
   wp += align_up((size_t)c.nchunks * c.qn * (size_t)at.n * sizeof(float));
-  double *sums = reinterpret_cast<double *>(wp);
-  wp += align_up((size_t)c.qn * at.n * sizeof(double));
   double *sumsq_part = reinterpret_cast<double *>(wp);
   wp += align_up(kSumSqBlocks * sizeof(double));
   double *f_extra = reinterpret_cast<double *>(wp);
@@ -650,8 +639,8 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
   }
   const int warps = ((at.n + c.ag - 1) / c.ag) * c.nchunks;
   const int blocks = (warps + 3) / 4;
-  const dim3 rgrid((at.n + 31) / 32, c.qn);
   const float s = 0.5f / g.ax[0].inv_step;  // cell half-width (pixel-integrated operator)
+  timer_mark(2, 0, stream);
   if (in.psf) {
     if (K == 1) {
       if (in.order == 1) gr_psf_deriv_kernel<1, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part, s);
@@ -660,25 +649,22 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
       if (in.order == 1) gr_psf_deriv_kernel<2, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part, s);
       else gr_psf_deriv_kernel<2, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part, s);
     }
-    gr_deriv_reduce_kernel<<<rgrid, 32 * kRedSlices, 0, stream>>>(part, c, at.n, sums);
-    if (K == 1)
-      gr_deriv_finalize_kernel<1><<<(at.n + 127) / 128, 128, 0, stream>>>(sums, c, at.n, in.order, at.r_iso, out, fe, at.order);
-    else
-      gr_deriv_finalize_kernel<2><<<(at.n + 127) / 128, 128, 0, stream>>>(sums, c, at.n, in.order, at.r_iso, out, fe, at.order);
   } else if (K == 1) {
     if (in.order == 1) gr_deriv_kernel<1, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
     else gr_deriv_kernel<1, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
-    gr_deriv_reduce_kernel<<<rgrid, 32 * kRedSlices, 0, stream>>>(part, c, at.n, sums);
-    gr_deriv_finalize_kernel<1><<<(at.n + 127) / 128, 128, 0, stream>>>(
-        sums, c, at.n, in.order, at.r_iso, out, fe, at.order);
   } else {
     if (in.order == 1) gr_deriv_kernel<2, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
     else gr_deriv_kernel<2, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
-    gr_deriv_reduce_kernel<<<rgrid, 32 * kRedSlices, 0, stream>>>(part, c, at.n, sums);
-    gr_deriv_finalize_kernel<2><<<(at.n + 127) / 128, 128, 0, stream>>>(
-        sums, c, at.n, in.order, at.r_iso, out, fe, at.order);
   }
-  note_launches(3);
+  timer_mark(2, 1, stream);
+  const int fblocks = (at.n + 31) / 32;
+  if (K == 1)
+    gr_deriv_finalize_kernel<1><<<fblocks, 32 * kRedSlices, 0, stream>>>(
+        part, c, at.n, in.order, at.r_iso, out, fe, at.order);
+  else
+    gr_deriv_finalize_kernel<2><<<fblocks, 32 * kRedSlices, 0, stream>>>(
+        part, c, at.n, in.order, at.r_iso, out, fe, at.order);
+  note_launches(2);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 

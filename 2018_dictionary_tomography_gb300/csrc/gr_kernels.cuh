@@ -107,6 +107,10 @@ int get_tuning(int key);
 
 // host-side count of kernels launched by this library
 void note_launches(int n);
+// kernel timers (which: 1 projection kernel, 2 derivative kernel)
+void timer_mark(int which, int end, cudaStream_t stream);
+int timer_enable(int which, int enable);
+int timer_read(int which, double *total_ms, int *launches);
 extern std::atomic<unsigned long long> g_launches;
 
 }  // namespace gr

@@ -5,7 +5,10 @@
 //   * gr_ex2_probe_kernel: MUFU ex2 throughput of this GPU (independent
 //     ex2.approx chains), the denominator of the SFU roofline.
 //   * a host-side counter of kernel launches made by this library.
+//   * kernel timers: CUDA events recorded on the launching stream around
+//     each launch of the projection or derivative kernel, summed on read.
 #include <atomic>
+#include <mutex>
 
 #include "gr_kernels.cuh"
 
@@ -14,6 +17,53 @@ namespace gr {
 std::atomic<unsigned long long> g_launches{0};
 
 void note_launches(int n) { g_launches.fetch_add((unsigned long long)n); }
+
+namespace {
+constexpr int kTimerSlots = 1024;
+struct KernelTimer {
+  bool on = false;
+  int n = 0;
+  cudaEvent_t ev[2 * kTimerSlots] = {};
+};
+KernelTimer g_timers[3];
+std::mutex g_timer_mu;
+}  // namespace
+
+void timer_mark(int which, int end, cudaStream_t stream) {
+  if (which < 1 || which > 2) return;
+  KernelTimer &t = g_timers[which];
+  if (!t.on || t.n >= kTimerSlots) return;
+  cudaEventRecord(t.ev[2 * t.n + end], stream);
+  if (end) ++t.n;
+}
+
+int timer_enable(int which, int enable) {
+  if (which < 1 || which > 2) return kErrArg;
+  std::lock_guard<std::mutex> lk(g_timer_mu);
+  KernelTimer &t = g_timers[which];
+  if (enable && t.ev[0] == nullptr)
+    for (int i = 0; i < 2 * kTimerSlots; ++i)
+      if (cudaEventCreate(&t.ev[i]) != cudaSuccess) return kErrLaunch;
+  t.on = enable != 0;
+  t.n = 0;
+  return kOk;
+}
+
+int timer_read(int which, double *total_ms, int *launches) {
+  if (which < 1 || which > 2 || !total_ms || !launches) return kErrArg;
+  KernelTimer &t = g_timers[which];
+  double sum = 0.0;
+  for (int i = 0; i < t.n; ++i) {
+    if (cudaEventSynchronize(t.ev[2 * i + 1]) != cudaSuccess) return kErrLaunch;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, t.ev[2 * i], t.ev[2 * i + 1]) != cudaSuccess)
+      return kErrLaunch;
+    sum += ms;
+  }
+  *total_ms = sum;
+  *launches = t.n;
+  return kOk;
+}
 
 template <int K>
 __global__ void __launch_bounds__(128) gr_count_kernel(Atoms at, Geom g,

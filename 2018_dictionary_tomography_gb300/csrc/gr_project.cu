@@ -253,21 +253,24 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   }
 }
 
-// 2D sinograms: atom footprints are a few cells wide, so a warp owns a tile
-// of 32 consecutive cells of one angle, one cell per lane, with the cell sum
-// in registers.  Pair data of up to 32 listed atoms is computed in parallel
-// (one atom per lane) and staged in shared memory; every lane then walks the
-// batch in atom order and adds the atoms whose support box holds its cell.
+// 2D sinograms: atom footprints are a few cells wide, so a block owns a tile
+// of 32 consecutive cells of one angle, one cell per lane.  The tile's
+// bitmap words are split into kProjWarps consecutive ranges, one per warp, so
+// a tile's atoms are walked by four warps at once; each warp keeps its
+// partial cell sums in registers.  Pair data of up to 32 listed atoms is
+// computed in parallel (one atom per lane) and staged in shared memory; every
+// lane then walks the batch in atom order and adds the atoms whose support
+// box holds its cell.  The warps' partial sums are combined in warp order
+// with a compensated sum: results are bitwise reproducible.
 template <bool KAHAN>
 __global__ void __launch_bounds__(kProjWarps * 32)
     gr_project1d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
-                        int W, ProjOut out) {
+                        int W, ProjOut out, double *loss_out, int *done) {
   __shared__ float4 prm[kProjWarps][32][2];
   __shared__ int lists[kProjWarps][kListWords * 32];
+  __shared__ float parts[kProjWarps][2][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int item = blockIdx.x * kProjWarps + warp;
-  const int n_items = g.n_angles * tc.ntiles;
-  if (item >= n_items) return;  // whole warp leaves together
+  const int item = blockIdx.x;
   int *list = lists[warp];
   const int a = item / tc.ntiles, t = item - a * tc.ntiles;
   const int D0 = g.ax[0].n;
@@ -278,9 +281,11 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   float acc = 0.f, cmp = 0.f;
 
   const uint32_t *words = bitmap + (size_t)item * W;
-  for (int wb = 0; wb < W; wb += kListWords) {
+  const int wq = (W + kProjWarps - 1) / kProjWarps;
+  const int w_lo = warp * wq, w_hi = min(W, w_lo + wq);
+  for (int wb = w_lo; wb < w_hi; wb += kListWords) {
     const int wi = wb + (lane < kListWords ? lane : 0);
-    uint32_t wd = (lane < kListWords && wi < W) ? words[wi] : 0u;
+    uint32_t wd = (lane < kListWords && wi < w_hi) ? words[wi] : 0u;
     int cnt = __popc(wd), incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -332,10 +337,26 @@ __global__ void __launch_bounds__(kProjWarps * 32)
       __syncwarp();
     }
   }
+  parts[warp][0][lane] = acc;
+  parts[warp][1][lane] = cmp;
+  __syncthreads();
+  if (warp != 0) return;
+  // combine the warps' partial sums in warp order (compensated)
+  float s0 = 0.f, c0 = 0.f;
+#pragma unroll
+  for (int w = 0; w < kProjWarps; ++w) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const float v = parts[w][h][lane];
+      const float tt = s0 + v;
+      c0 += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
+      s0 = tt;
+    }
+  }
 
   float l = 0.f;
   if (cell < D0) {
-    const float v = KAHAN ? acc + cmp : acc;
+    const float v = s0 + c0;
     const size_t gi = (size_t)a * D0 + cell;
     if (out.R) out.R[gi] = v;
     if (out.epilogue == kEpiL2) {
@@ -354,6 +375,22 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   if (out.loss_part) {
     const double d = warp_sum_d((double)l);
     if (lane == 0) out.loss_part[item] = d;
+    if (loss_out) {
+      // the last block to finish sums the per-tile partials in tile order
+      int last = 0;
+      if (lane == 0) {
+        __threadfence();
+        last = atomicAdd(done, 1) == (int)gridDim.x - 1;
+      }
+      if (__shfl_sync(0xffffffffu, last, 0)) {
+        __threadfence();
+        const volatile double *lp = out.loss_part;
+        double t = 0.0;
+        for (int i = lane; i < (int)gridDim.x; i += 32) t += lp[i];
+        t = warp_sum_d(t);
+        if (lane == 0) loss_out[0] = t;
+      }
+    }
   }
 }
 
@@ -583,13 +620,14 @@ __global__ void gr_loss_finalize_kernel(const double *part, int n, double *out) 
   if (threadIdx.x == 0) out[0] = sh[0];
 }
 
-// Form of the point-sampled 3D projection (gr_set_tuning key 3):
 // Tiling of the point-sampled 3D projection (gr_set_tuning key 3):
 // 1: 16-row tiles (more resident warps), 2: 32-row tiles (fewer atoms cut
 // by tile edges).
 int g_proj_form = 1;
 
 static int proj_rows(int form) { return form == 2 ? kTileDim0 : 16; }
+
+constexpr size_t kFusedLossItems = 65536;
 
 template <int ROWS, int S>
 static void launch_project3d(int blocks, const Atoms &at, const Geom &g, const TileCfg &tc,
@@ -639,7 +677,9 @@ size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1)
   TileCfg tc = make_tiles(K, D0, D1, rows);
   const size_t W = (size_t)(n_atoms + 31) / 32;
   const size_t items = (size_t)n_angles * tc.ntiles;
-  size_t bytes = align_up(sizeof(int));  // work counter of the persistent kernel
+  // item counter of the persistent 3D kernel, finished-block counter of the
+  // 2D kernel
+  size_t bytes = align_up(2 * sizeof(int));
   bytes += align_up(items * W * sizeof(uint32_t));
   bytes += align_up(items * sizeof(double));
   return bytes;
@@ -658,12 +698,12 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   if (ws_bytes < need || (ws == nullptr && need > 0)) return kErrWorkspace;
   char *wp = static_cast<char *>(ws);
   int *next_item = reinterpret_cast<int *>(wp);
-  wp += align_up(sizeof(int));
+  wp += align_up(2 * sizeof(int));
   uint32_t *bitmap = reinterpret_cast<uint32_t *>(wp);
   wp += align_up(items * W * sizeof(uint32_t));
   double *loss_part = reinterpret_cast<double *>(wp);
-  // one clear covers the work counter and the bitmap
-  if (cudaMemsetAsync(ws, 0, align_up(sizeof(int)) + items * W * sizeof(uint32_t), stream) !=
+  // one clear covers the counters and the bitmap
+  if (cudaMemsetAsync(ws, 0, align_up(2 * sizeof(int)) + items * W * sizeof(uint32_t), stream) !=
       cudaSuccess)
     return kErrLaunch;
   ProjOut o = o_in;
@@ -687,20 +727,27 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   // smem (kProjWarps * kProjWarpFloats floats) stays below the 48 KB that
   // needs no opt-in, so no function attribute is set (safe under capture)
   static_assert(kProjWarps * kProjWarpFloats * sizeof(float) <= 48 * 1024, "smem");
+  bool fused_loss = false;
+  timer_mark(1, 0, stream);
   if (o.psf) {
     if (K == 1)
       gr_psf_project_kernel<1><<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, psf_s, o);
     else
       gr_psf_project_kernel<2><<<blocks, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, psf_s, o);
   } else if (K == 1) {
-    gr_project1d_kernel<true><<<blocks, kProjWarps * 32, 0, stream>>>(at, g, tc, bitmap, W, o);
+    // one block per (angle, tile) item; for up to kFusedLossItems tiles the
+    // last block also sums the loss partials (no separate finalize launch)
+    fused_loss = loss_out != nullptr && items <= kFusedLossItems;
+    gr_project1d_kernel<true><<<(unsigned)items, kProjWarps * 32, 0, stream>>>(
+        at, g, tc, bitmap, W, o, fused_loss ? loss_out : nullptr, next_item + 1);
   } else if (form == 2) {
     launch_project3d<32, 34>(blocks, at, g, tc, bitmap, W, o, next_item, stream);
   } else {
     launch_project3d<16, 37>(blocks, at, g, tc, bitmap, W, o, next_item, stream);
   }
+  timer_mark(1, 1, stream);
   note_launches(1);
-  if (loss_out) {
+  if (loss_out && !fused_loss) {
     gr_loss_finalize_kernel<<<1, 256, 0, stream>>>(loss_part, (int)items, loss_out);
     note_launches(1);
   }

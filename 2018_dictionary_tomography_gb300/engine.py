@@ -247,6 +247,23 @@ def probe_ex2(blocks, threads, iters, device=None):
     _lib.check(st, "gr_probe_ex2")
 
 
+TIMER_PROJECT, TIMER_DERIVS = 1, 2
+
+
+def kernel_timer(which, enable=True):
+    """Start (clearing) or stop the CUDA-event timer around the projection
+    (TIMER_PROJECT) or derivative (TIMER_DERIVS) kernel launches."""
+    _lib.check(_lib.load().gr_kernel_timer(int(which), 1 if enable else 0), "gr_kernel_timer")
+
+
+def kernel_timer_read(which):
+    """(summed ms, launches) of the timed kernel launches (waits for them)."""
+    ms, n = ctypes.c_double(), ctypes.c_int()
+    _lib.check(_lib.load().gr_kernel_timer_read(int(which), ctypes.byref(ms), ctypes.byref(n)),
+               "gr_kernel_timer_read")
+    return ms.value, n.value
+
+
 def launch_count():
     """Kernels launched by the engine library so far in this process."""
     return int(_lib.load().gr_launch_count())

@@ -178,6 +178,8 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     l0 = engine.launch_count()
+    engine.kernel_timer(engine.TIMER_PROJECT, True)
+    engine.kernel_timer(engine.TIMER_DERIVS, True)
     sampler.start()
     for i in range(args.steps):
         flush.zero_()                                   # evict L2 between steps
@@ -191,6 +193,10 @@ def run_ours(args):
     torch.cuda.synchronize()
     clocks = sampler.stop()
     launches = engine.launch_count() - l0
+    kt_fwd, n_kf = engine.kernel_timer_read(engine.TIMER_PROJECT)
+    kt_der, n_kd = engine.kernel_timer_read(engine.TIMER_DERIVS)
+    engine.kernel_timer(engine.TIMER_PROJECT, False)
+    engine.kernel_timer(engine.TIMER_DERIVS, False)
     t_fwd = [a.elapsed_time(b) for a, b, _ in ev]
     t_der = [b.elapsed_time(c) for _, b, c in ev]
     total_ms = sum(t_fwd) + sum(t_der)
@@ -245,34 +251,44 @@ def run_ours(args):
     ex2_rate = probe_ex2_rate(engine, dev)
     fwd_ms = statistics.mean(t_fwd)
     der_ms = statistics.mean(t_der)
-    dom = "derivatives" if der_ms >= fwd_ms else "forward"
-    dom_ms = max(fwd_ms, der_ms)
+    # the kernels' own launch durations (CUDA events on their stream)
+    k_fwd = kt_fwd / max(1, n_kf)
+    k_der = kt_der / max(1, n_kd)
+    dom = "derivatives" if k_der >= k_fwd else "forward"
+    dom_ms = max(k_fwd, k_der)
+    fwd_kernel = "gr_project3d_kernel" if geom.dim == 3 else "gr_project1d_kernel"
+    dom_kernel = "gr_deriv_kernel" if dom == "derivatives" else fwd_kernel
     cells = int(np.prod(geom.shape))
-    # algorithmic bytes per launch of each call
+    # algorithmic bytes per launch: data and fields once, atoms, outputs
     atom_bytes = N * (1 + atoms.dim + (1 if atoms.iso else atoms.r.shape[1])) * 4
     fields = 2 if fit == "kl" else 1
     fwd_bytes = cells * 4 * (1 + fields) + atom_bytes
     der_bytes = cells * 4 * fields + atom_bytes + N * (P + (P * P if order == 2 else 0)) * 8
     dom_bytes = der_bytes if dom == "derivatives" else fwd_bytes
+    traffic = profiled_traffic(W.name, dom_kernel)
     roofline = {
         "bound": "sfu",
-        "kernel": "gr_deriv_kernel" if dom == "derivatives" else "gr_project_kernel",
+        "kernel": dom_kernel,
         "achieved": S / (dom_ms * 1e-3) / 1e9,
         "peak": ex2_rate / 1e9,
         "unit": "Gex2/s",
         "frac": (S / (dom_ms * 1e-3)) / ex2_rate,
         "peak_source": "measured ex2.approx probe on this GPU (gr_probe_ex2)",
-        "traffic": None,
+        "traffic": traffic,
         "ms_per_launch": dom_ms,
+        "units_per_launch": S,
+        "unit_note": "one ex2 per in-support (atom, angle, cell) evaluation",
     }
     roofline_hbm = {
         "bound": "hbm",
+        "kernel": dom_kernel,
         "achieved": dom_bytes / (dom_ms * 1e-3) / 1e9,
         "peak": peaks["hbm_gbs"],
         "unit": "GB/s",
         "frac": dom_bytes / (dom_ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
         "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src,
         "algorithmic_bytes": dom_bytes,
+        "traffic": traffic,
     }
 
     out = {
@@ -286,6 +302,7 @@ def run_ours(args):
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "dense_equiv_evals_per_s": dense * args.steps * ws / (total_ms * 1e-3),
         "ms_forward": fwd_ms, "ms_derivatives": der_ms,
+        "ms_kernel": {fwd_kernel: k_fwd, "gr_deriv_kernel": k_der},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / n_e2e},
         "gpu_launches": launches, "gpu_launches_per_step": launches / args.steps,
@@ -299,6 +316,18 @@ def run_ours(args):
     if ws > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
+
+
+def profiled_traffic(workload, kernel):
+    """DRAM bytes (read + write) per launch of the kernel from the committed
+    ncu summary (profiles/traffic.json), or None when not profiled."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        tab = json.load(f)
+    v = tab.get(workload.split(":")[0], {}).get(kernel)
+    return None if v is None else float(v)
 
 
 def probe_ex2_rate(engine, dev):

@@ -271,6 +271,21 @@ int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);
 
 /*
+ * Kernel timers (no counterpart in the reference; measurement only).  While
+ * enabled, CUDA events are recorded on the launching stream around each
+ * launch of GR_TIMER_PROJECT (the projection kernel of gr_radproj /
+ * gr_fit_forward and their pixel-integrated forms) or GR_TIMER_DERIVS (the
+ * per-atom derivative kernel of gr_atom_derivs), up to 1024 launches.
+ * gr_kernel_timer(which, 1) clears and starts, (which, 0) stops;
+ * gr_kernel_timer_read waits for the recorded launches and returns their
+ * summed duration in ms and their number.  Not for use while a stream is
+ * being captured into a graph; not thread-safe against concurrent launches.
+ */
+enum { GR_TIMER_PROJECT = 1, GR_TIMER_DERIVS = 2 };
+int gr_kernel_timer(int which, int enable);
+int gr_kernel_timer_read(int which, double *total_ms, int *launches);
+
+/*
  * gr_radproj without a caller-supplied workspace.  No counterpart in the
  * reference (its kernels are Numba launches that allocate as they please).
  *
