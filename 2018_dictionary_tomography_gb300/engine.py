@@ -357,3 +357,101 @@ def newton_accept_into(dim, iso, loss_cur, loss_trial, theta, theta_trial, lam, 
         trial_atoms.r.data_ptr(), hist.data_ptr(), hist_acc.data_ptr(), counter.data_ptr(),
         int(hist.numel()), _stream_handle(device))
     _lib.check(st, "gr_newton_accept")
+
+
+class FitStep:
+    """One fit evaluation from host inputs to host results, as a CUDA graph.
+
+    Loss, per-atom gradient and (order 2) Hessian of the L2 or KL fit of
+    ``n_atoms`` atoms to a sinogram on ``geom``.  The graph holds the
+    host->device copies of the atoms and data from this object's pinned host
+    buffers, the fused projection + fit (``gr_fit_forward``), the per-atom
+    derivatives (``gr_atom_derivs`` in field mode) and the device->host copies
+    of loss, gradient and Hessian into pinned host buffers, so one evaluation
+    is one graph launch.  ``run`` copies new inputs into the pinned buffers
+    (when given), replays and waits; its results are views of the pinned
+    output buffers, overwritten by the next run.
+    """
+
+    def __init__(self, geom, n_atoms, iso=False, fit="l2", background=0.0, order=2,
+                 psf=False):
+        dev = geom.device
+        _require_cuda(dev)
+        if fit not in ("l2", "kl"):
+            raise ValueError("fit must be 'l2' or 'kl'")
+        self.geom, self.fit, self.order, self.psf = geom, fit, int(order), bool(psf)
+        self.background = float(background)
+        n, d = int(n_atoms), geom.dim
+        pr = 1 if iso else (3 if d == 2 else 6)
+        pin = dict(dtype=torch.float32, pin_memory=True)
+        self.I_h = torch.zeros(n, **pin)
+        self.x_h = torch.zeros(n, d, **pin)
+        self.r_h = torch.ones(n, pr, **pin)
+        self.data_h = torch.zeros(geom.shape, **pin)
+        self.I_d = torch.zeros(n, device=dev)
+        self.x_d = torch.zeros(n, d, device=dev)
+        self.r_d = torch.ones(n, pr, device=dev)
+        self.data_d = torch.zeros(geom.shape, device=dev)
+        self.atoms = DeviceAtoms(self.I_d, self.x_d, self.r_d, dev)
+        P = self.atoms.n_params()
+        f32 = dict(dtype=torch.float32, device=dev)
+        self.alpha = torch.empty(geom.shape, **f32)
+        self.beta = torch.empty(geom.shape, **f32) if fit == "kl" else None
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.loss = torch.zeros((), **f64)
+        self.f = torch.zeros(n, **f64)
+        self.g = torch.zeros(n, P, **f64)
+        self.H = torch.zeros(n, P, P, **f64) if self.order > 1 else None
+        self.loss_h = torch.zeros((), dtype=torch.float64, pin_memory=True)
+        self.g_h = torch.zeros(n, P, dtype=torch.float64, pin_memory=True)
+        self.H_h = (torch.zeros(n, P, P, dtype=torch.float64, pin_memory=True)
+                    if self.order > 1 else None)
+        nb = max(workspace_bytes(_lib.GR_OP_PROJECT, self.atoms, geom),
+                 workspace_bytes(_lib.GR_OP_DERIVS_2 if self.order > 1 else _lib.GR_OP_DERIVS_1,
+                                 self.atoms, geom))
+        self.ws = torch.empty(max(nb, 256), dtype=torch.uint8, device=dev)
+        self.h2d_bytes = sum(t.numel() * t.element_size()
+                             for t in (self.I_h, self.x_h, self.r_h, self.data_h))
+        self.d2h_bytes = sum(t.numel() * t.element_size()
+                             for t in (self.loss_h, self.g_h, self.H_h) if t is not None)
+        stream = torch.cuda.Stream(dev)
+        stream.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(stream):
+            self._body()                     # warm-up outside the capture
+        stream.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, stream=stream):
+            self._body()
+        torch.cuda.synchronize(dev)
+
+    def _body(self):
+        self.I_d.copy_(self.I_h, non_blocking=True)
+        self.x_d.copy_(self.x_h, non_blocking=True)
+        self.r_d.copy_(self.r_h, non_blocking=True)
+        self.data_d.copy_(self.data_h, non_blocking=True)
+        fit_forward_into(self.atoms, self.geom, self.data_d, self.fit, self.background, None,
+                         self.alpha, self.beta, self.loss, self.ws, psf=self.psf)
+        bc = 1.0 if self.fit == "l2" else 0.0
+        atom_derivs_into(self.atoms, self.geom, "field", self.alpha, self.beta, bc, self.order,
+                         self.f, self.g, self.H, self.ws, psf=self.psf)
+        self.loss_h.copy_(self.loss, non_blocking=True)
+        self.g_h.copy_(self.g, non_blocking=True)
+        if self.H_h is not None:
+            self.H_h.copy_(self.H, non_blocking=True)
+
+    def set_inputs(self, I=None, x=None, r=None, data=None):
+        """Copy new atoms and/or data into the pinned input buffers."""
+        for src, dst in ((I, self.I_h), (x, self.x_h), (r, self.r_h), (data, self.data_h)):
+            if src is not None:
+                dst.copy_(torch.as_tensor(src, dtype=torch.float32).reshape(dst.shape))
+
+    def launch(self):
+        """Replay the graph on the current stream (no wait)."""
+        self.graph.replay()
+
+    def run(self, I=None, x=None, r=None, data=None):
+        """(loss, gradient (N, P), Hessian (N, P, P) or None) as host tensors."""
+        self.set_inputs(I, x, r, data)
+        self.graph.replay()
+        torch.cuda.current_stream(self.geom.device).synchronize()
+        return float(self.loss_h), self.g_h, self.H_h

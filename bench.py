@@ -208,19 +208,12 @@ def run_ours(args):
     value = S * args.steps * ws / (total_ms * 1e-3)
 
     # ---- end-to-end through the API with host buffers ----------------------
-    Ih = torch.as_tensor(I0, dtype=torch.float32).pin_memory()
-    xh = torch.as_tensor(x0, dtype=torch.float32).pin_memory()
-    rh = torch.as_tensor(r0, dtype=torch.float32).reshape(N, -1).pin_memory()
-    dh = torch.as_tensor(W.data, dtype=torch.float32).pin_memory()
-    Id = torch.empty_like(Ih, device=dev)
-    xd = torch.empty_like(xh, device=dev)
-    rd = torch.empty_like(rh, device=dev)
-    dd = torch.empty_like(dh, device=dev)
-    loss_h = torch.empty((), dtype=torch.float64).pin_memory()
-    g_h = torch.empty((N, P), dtype=torch.float64).pin_memory()
-    H_h = torch.empty((N, P, P), dtype=torch.float64).pin_memory() if order == 2 else None
-    h2d = sum(t.numel() * t.element_size() for t in (Ih, xh, rh, dh))
-    d2h = 8 + g_h.numel() * 8 + (H_h.numel() * 8 if H_h is not None else 0)
+    # engine.FitStep: every step copies the atoms and data from pinned host
+    # memory, runs the fused projection + fit and the per-atom derivatives,
+    # and copies loss, gradient and Hessian back to pinned host memory
+    fs = engine.FitStep(geom, N, iso=atoms.iso, fit=fit, background=bg, order=order)
+    fs.set_inputs(I0, x0, r0, W.data)
+    h2d, d2h = fs.h2d_bytes, fs.d2h_bytes
     n_e2e = max(10, args.steps // 4)
     e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2e_ms = 0.0
@@ -228,23 +221,14 @@ def run_ours(args):
         flush.zero_()
         if i >= 3:
             e_start.record(stream)
-        Id.copy_(Ih, non_blocking=True)
-        xd.copy_(xh, non_blocking=True)
-        rd.copy_(rh, non_blocking=True)
-        dd.copy_(dh, non_blocking=True)
-        at = engine.DeviceAtoms(Id, xd, rd, dev)
-        fw = engine.fit_forward(at, geom, dd, fit, bg)
-        f, g, H = engine.atom_derivs(at, geom, "field", fw["alpha"], fw["beta"],
-                                     1.0 if fit == "l2" else 0.0, order)
-        loss_h.copy_(fw["loss"], non_blocking=True)
-        g_h.copy_(g, non_blocking=True)
-        if H_h is not None:
-            H_h.copy_(H, non_blocking=True)
+        fs.launch()
         if i >= 3:
             e_end.record(stream)
-            torch.cuda.synchronize()
+        torch.cuda.synchronize()
+        if i >= 3:
             e2e_ms += e_start.elapsed_time(e_end)
     e2e_value = S * n_e2e * ws / (e2e_ms * 1e-3)
+    e2e_loss = float(fs.loss_h)
 
     # ---- roofline ----------------------------------------------------------
     peaks, src = measured_peaks()
@@ -304,7 +288,9 @@ def run_ours(args):
         "ms_forward": fwd_ms, "ms_derivatives": der_ms,
         "ms_kernel": {fwd_kernel: k_fwd, "gr_deriv_kernel": k_der},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / n_e2e},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / n_e2e,
+                "api": "engine.FitStep (one CUDA graph: H2D, fit, derivatives, D2H)",
+                "loss": e2e_loss},
         "gpu_launches": launches, "gpu_launches_per_step": launches / args.steps,
         "roofline": roofline, "roofline_hbm": roofline_hbm,
         "clocks": clocks,

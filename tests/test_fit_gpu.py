@@ -196,3 +196,33 @@ def test_batched_newton_matches_oracle(eng, cuda_ready, kind):
     _, lo = fit_oracle.newton_batched(I0, x0, r0, g, data, iters, kind, bg)
     assert abs(losses[-1] - lo[-1]) <= 1e-4 * abs(lo[-1])
     assert lo[-1] < lo[0]
+
+
+@pytest.mark.parametrize("case", ["2d_kl", "3d_l2"])
+def test_fit_step_graph_matches_direct_calls(eng, cuda_ready, case):
+    """engine.FitStep (one graph: H2D, fit, derivatives, D2H) gives exactly
+    the results of the direct calls on the same inputs."""
+    if case == "2d_kl":
+        g = make_geometry("2d", 24, 80)
+        I, x, r = make_atoms(2, 12, 41)
+        fit, bg, order = "kl", 0.05, 2
+    else:
+        g = make_geometry("3d", 9, 40, 44)
+        I, x, r = make_atoms(3, 10, 42)
+        fit, bg, order = "l2", 0.0, 2
+    data = go.radproj(I * 1.1, x, r, g) + 0.01
+    geom = engine_geometry(g)
+    fs = eng.FitStep(geom, len(I), fit=fit, background=bg, order=order)
+    loss, gh, Hh = fs.run(I, x, r, data)
+    atoms = engine_atoms(I, x, r)
+    d = torch.from_numpy(data).float().cuda()
+    fw = eng.fit_forward(atoms, geom, d, fit, bg)
+    f, gd, Hd = eng.atom_derivs(atoms, geom, "field", fw["alpha"], fw["beta"],
+                                1.0 if fit == "l2" else 0.0, order)
+    assert loss == fw["loss"].item()
+    assert torch.equal(gh, gd.cpu()) and torch.equal(Hh, Hd.cpu())
+    # a second run with other atoms reuses the graph
+    loss2, gh2, _ = fs.run(I * 0.9, x, r, data)
+    atoms2 = engine_atoms(I * 0.9, x, r)
+    fw2 = eng.fit_forward(atoms2, geom, d, fit, bg)
+    assert loss2 == fw2["loss"].item()
