@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-orient", type=int, default=None,
+                    help="config4: fewer orientations (a reduced case for profiling)")
     return ap.parse_args()
 
 
@@ -128,8 +130,10 @@ def measured_peaks():
 # --------------------------------------------------------------------------
 # our arm
 # --------------------------------------------------------------------------
-def build_workload(name):
+def build_workload(name, n_orient=None):
     wl = importlib.import_module(PKG + ".workloads")
+    if name == "config4" and n_orient:
+        return wl.config4(n_orient=n_orient)
     return {"config1": wl.config1, "config2": wl.config2, "config4": wl.config4}[name]()
 
 
@@ -145,7 +149,7 @@ def run_ours(args):
     engine = importlib.import_module(PKG + ".engine")
     geometry = importlib.import_module(PKG + ".geometry")
 
-    W = build_workload(args.workload)
+    W = build_workload(args.workload, args.n_orient)
     I0, x0, r0 = W.init
     geom = geometry.DeviceGeometry(W.orientations, W.ortho, W.detector, dev)
     atoms = engine.DeviceAtoms(I0, x0, r0, dev)
