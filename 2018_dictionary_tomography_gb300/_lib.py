@@ -42,7 +42,9 @@ EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
            "gr_fit_forward", "gr_atom_derivs", "gr_count_support", "gr_probe_ex2",
            "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj", "gr_newton_accept",
            "gr_psf_radproj", "gr_psf_fit_forward", "gr_psf_atom_derivs", "gr_psf_volproj",
-           "gr_set_tuning", "gr_get_tuning", "gr_kernel_timer", "gr_kernel_timer_read")
+           "gr_set_tuning", "gr_get_tuning", "gr_kernel_timer", "gr_kernel_timer_read",
+           "gr_fit_loop_begin", "gr_fit_loop_end", "gr_fit_loop_instantiate",
+           "gr_fit_loop_launch", "gr_fit_loop_destroy")
 
 _lock = threading.Lock()
 _lib = None
@@ -124,6 +126,18 @@ def load(build_if_missing=True):
         lib.gr_get_tuning.argtypes = [ctypes.c_int]
         lib.gr_kernel_timer.restype = ctypes.c_int
         lib.gr_kernel_timer.argtypes = [ctypes.c_int, ctypes.c_int]
+        vp = ctypes.c_void_p
+        lib.gr_fit_loop_begin.restype = ctypes.c_int
+        lib.gr_fit_loop_begin.argtypes = [vp, vp, ctypes.POINTER(vp)]
+        lib.gr_fit_loop_end.restype = ctypes.c_int
+        lib.gr_fit_loop_end.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_double, ctypes.c_int, vp]
+        lib.gr_fit_loop_instantiate.restype = ctypes.c_int
+        lib.gr_fit_loop_instantiate.argtypes = [vp]
+        lib.gr_fit_loop_launch.restype = ctypes.c_int
+        lib.gr_fit_loop_launch.argtypes = [vp, vp]
+        lib.gr_fit_loop_destroy.restype = ctypes.c_int
+        lib.gr_fit_loop_destroy.argtypes = [vp]
         lib.gr_kernel_timer_read.restype = ctypes.c_int
         lib.gr_kernel_timer_read.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                              ctypes.POINTER(ctypes.c_int)]

@@ -455,3 +455,64 @@ class FitStep:
         self.graph.replay()
         torch.cuda.current_stream(self.geom.device).synchronize()
         return float(self.loss_h), self.g_h, self.H_h
+
+
+class FitLoop:
+    """A whole damped-Newton fit as one CUDA graph (``gr_fit_loop_*``).
+
+    ``capture_iteration()`` must issue one iteration on the current stream
+    (projection + fit, derivatives, ``newton_solve_into``, trial projection,
+    ``newton_accept_into``) with preallocated buffers only; it is captured
+    into the body of a WHILE node.  After each iteration a device-side stop
+    test reads ``hist``, ``hist_acc`` and ``counter`` (written by the accept
+    kernel): it stops after ``max_iter`` iterations, after ``max_reject``
+    rejected trials in a row, or when the last accepted iteration changed the
+    loss by at most ``tol`` relative.  ``launch()`` runs the whole fit on
+    ``stream`` with no host round trip.  ``close()`` waits for the device to
+    idle (a property of destroying an executable graph): close finished loops
+    when nothing runs.
+    """
+
+    def __init__(self, stream, capture_iteration, hist, hist_acc, counter, max_iter,
+                 max_reject, tol, device):
+        lib = _lib.load()
+        self._lib = lib
+        self.stream = stream
+        self.handle = None
+        self.guard = torch.zeros(1, dtype=torch.int32, device=device)
+        self.stop_reason = torch.zeros(1, dtype=torch.int32, device=device)
+        self._keep = (hist, hist_acc, counter)
+        h = ctypes.c_void_p()
+        sh = ctypes.c_void_p(stream.cuda_stream)
+        with torch.cuda.stream(stream):
+            _lib.check(lib.gr_fit_loop_begin(sh, self.guard.data_ptr(), ctypes.byref(h)),
+                       "gr_fit_loop_begin")
+            self.handle = h
+            try:
+                capture_iteration()
+            finally:
+                rc = lib.gr_fit_loop_end(
+                    h, sh, hist.data_ptr(), hist_acc.data_ptr(), counter.data_ptr(),
+                    int(hist.numel()), int(max_iter), int(max_reject), float(tol),
+                    int(max_iter) + int(max_reject) + 2, self.stop_reason.data_ptr())
+        if rc == 0:
+            rc = lib.gr_fit_loop_instantiate(h)
+        if rc != 0:
+            self.close()
+            _lib.check(rc, "gr_fit_loop_end")
+
+    def launch(self):
+        _lib.check(self._lib.gr_fit_loop_launch(self.handle,
+                                                ctypes.c_void_p(self.stream.cuda_stream)),
+                   "gr_fit_loop_launch")
+
+    def close(self):
+        if self.handle is not None and self.handle.value:
+            self._lib.gr_fit_loop_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

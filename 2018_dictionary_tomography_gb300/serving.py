@@ -3,8 +3,8 @@
 Fitting requests of uneven size (2D or 3D, any atom count, angle count and
 detector size) arrive over time.  The server admits a request as soon as a
 slot and enough free HBM are available, also while other requests are being
-fitted; every admitted request owns its device buffers, a CUDA stream and a
-CUDA graph of one damped-Newton iteration:
+fitted; every admitted request owns its device buffers and a CUDA stream, and
+one damped-Newton iteration
 
   gr_fit_forward(current atoms)  -> fit fields, loss
   gr_atom_derivs(all atoms)      -> gradient and Hessian blocks
@@ -13,17 +13,27 @@ CUDA graph of one damped-Newton iteration:
   gr_newton_accept               -> device-side accept/reject, damping update,
                                     loss history
 
-so an iteration needs no host round trip.  The host loop replays each
-request's graph a few iterations at a time on its stream, polls completion
-events, reads the loss history (copied asynchronously to pinned memory) and
-retires a request when its relative loss change drops below ``tol`` (or after
-``max_iter`` iterations, or after 8 rejected trials in a row).  Requests on
-different streams overlap on the device.  A request's result does not depend
-on what else is running: its kernels are deterministic and its state private
-(tests/test_serving_gpu.py checks that results alone and in the mix agree).
+is captured once into the body of a device-resident loop (engine.FitLoop: a
+CUDA graph whose WHILE node repeats the iteration until a device-side stop
+test ends it: relative loss change below ``tol`` after an accepted step,
+``max_iter`` iterations, or 8 rejected trials in a row).  A whole fit is one
+graph launch; the host only polls a completion event and reads the result.
+Requests on different streams overlap on the device.  Where the device loop
+cannot be built, the request falls back to a graph of one iteration replayed
+a few iterations at a time, with the same stop test on the host copy of the
+loss history.  A request's result does not depend on what else is running:
+its kernels are deterministic and its state private (tests/test_serving_gpu.py
+checks that results alone and in the mix agree).
+
+Host-side care that keeps the loop from stalling behind fits in flight:
+buffers of a new request are built on a separate setup stream; finished
+loop graphs are destroyed only when no fit runs (destroying an executable
+graph waits for the device to idle); pinned host buffers are pooled.  Among
+requests that have arrived, the largest are admitted first, so the longest
+fits start early.
 
 ``serve_plain`` is the baseline: the same fits one after another with the
-eager host-driven loop (solvers.newton_batched), one host sync per iteration.
+eager host-driven loop, one host sync per iteration.
 """
 import collections
 import time
@@ -39,7 +49,19 @@ MAX_BACKTRACK = 8
 
 class FitRequest:
     """One fitting problem.  ``make_data(geom, device, stream)`` returns the
-    data sinogram as a float32 device tensor (called at admission)."""
+    data sinogram as a float32 device tensor (called at admission) unless the
+    request carries it as ``data_host`` (pinned host memory), which admission
+    copies in."""
+
+    def device_data(self, geom, device, stream):
+        """The data sinogram on the device: the carried payload copied in
+        (asynchronously on ``stream``), else ``make_data``."""
+        if self.data_host is not None:
+            d = torch.empty(geom.shape, dtype=torch.float32, device=device)
+            with torch.cuda.stream(stream):
+                d.copy_(self.data_host.reshape(geom.shape), non_blocking=True)
+            return d
+        return self.make_data(geom, device, stream)
 
     def __init__(self, rid, orientations, ortho, detector, init, make_data, fit="l2",
                  background=0.0, max_iter=100, tol=1e-6, arrival=0.0, lam0=1.0):
@@ -55,6 +77,7 @@ class FitRequest:
         self.tol = tol
         self.arrival = arrival
         self.lam0 = lam0
+        self.data_host = None       # optional payload (pinned host tensor)
         n = len(init[0])
         cells = len(orientations) * int(np.prod([len(d) for d in detector]))
         self.size_hint = (n, cells)
@@ -63,12 +86,17 @@ class FitRequest:
 class _Slot:
     """Device state of one admitted request."""
 
-    def __init__(self, req, stream, device, use_graph=True, iters_per_launch=4):
+    def __init__(self, req, stream, device, use_graph=True, iters_per_launch=4,
+                 device_loop=True, setup_stream=None, pinned=None):
         self.req = req
         self.stream = stream
         self.dev = device
         self.k = iters_per_launch
-        with torch.cuda.stream(stream):
+        # Buffers are built and filled on a setup stream: the compute stream
+        # may still hold queued fits of earlier requests.
+        setup = setup_stream if setup_stream is not None else stream
+        t_start = time.perf_counter()
+        with torch.cuda.stream(setup):
             self.geom = DeviceGeometry(req.orientations, req.ortho, req.detector, device)
             I0, x0, r0 = req.init
             n = len(I0)
@@ -81,7 +109,7 @@ class _Slot:
             self.theta_trial = self.theta.clone()
             self.lam = torch.full((n,), float(req.lam0), dtype=torch.float64, device=device)
             shape = self.geom.shape
-            self.data = req.make_data(self.geom, device, stream)
+            self.data = req.device_data(self.geom, device, setup)
             self.alpha = torch.empty(shape, dtype=torch.float32, device=device)
             self.beta = (torch.empty(shape, dtype=torch.float32, device=device)
                          if req.fit == "kl" else None)
@@ -99,17 +127,59 @@ class _Slot:
             self.hist = torch.zeros(L, dtype=torch.float64, device=device)
             self.hist_acc = torch.zeros(L, dtype=torch.int32, device=device)
             self.counter = torch.zeros(1, dtype=torch.int32, device=device)
-            self.h_hist = torch.zeros(L, dtype=torch.float64).pin_memory()
-            self.h_acc = torch.zeros(L, dtype=torch.int32).pin_memory()
-            self.h_counter = torch.zeros(1, dtype=torch.int32).pin_memory()
+            if pinned is None:
+                pinned = (torch.zeros(L, dtype=torch.float64).pin_memory(),
+                          torch.zeros(L, dtype=torch.int32).pin_memory(),
+                          torch.zeros(1, dtype=torch.int32).pin_memory())
+            self.pinned = pinned
+            self.h_hist, self.h_acc, self.h_counter = pinned
+        t_bufs = time.perf_counter()
+        if setup is not stream:
+            ready = torch.cuda.Event()
+            ready.record(setup)
+            stream.wait_event(ready)
+            for t in (self.geom.frames, self.geom.det, self.cur.I, self.cur.x,
+                      self.cur.r, self.trial.I, self.trial.x, self.trial.r, self.theta,
+                      self.theta_trial, self.lam, self.data, self.alpha, self.beta,
+                      self.loss_cur, self.loss_trial, self.f, self.g, self.H, self.step,
+                      self.ws_p, self.ws_d, self.hist, self.hist_acc, self.counter):
+                for u in (t if isinstance(t, (list, tuple)) else (t,)):
+                    if u is not None:
+                        u.record_stream(stream)
+        t_cap = time.perf_counter()
+        with torch.cuda.stream(stream):
             self.event = torch.cuda.Event()
             self.graph = None
+            self.loop = None
             self.loss0 = None
+            if use_graph and device_loop:
+                # the whole fit as one graph: the iteration repeats on the
+                # device until the device-side stop test ends it
+                try:
+                    self.loop = engine.FitLoop(stream, self.iterate, self.hist, self.hist_acc,
+                                               self.counter, req.max_iter, MAX_BACKTRACK,
+                                               req.tol, device)
+                except _lib.EngineError:
+                    self.loop = None
+            t_loop = time.perf_counter()
+            self.phase_seconds = {"buffers": t_bufs - t_start, "streams": t_cap - t_bufs,
+                                  "capture": t_loop - t_cap}
+            if self.loop is not None:
+                self.iterations_launched = 0
+                return
             self.iterate()                       # eager first iteration (also warms up)
             if use_graph:
+                # captured directly on this request's stream: the
+                # torch.cuda.graph context would synchronise the whole device
+                # and run the garbage collector at every admission, stalling
+                # the requests already in flight (no allocation happens
+                # inside the capture: every buffer exists already)
                 self.graph = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(self.graph, stream=stream):
+                self.graph.capture_begin(capture_error_mode="thread_local")
+                try:
                     self.iterate()
+                finally:
+                    self.graph.capture_end()
             self._copy_back()
         self.iterations_launched = 1
 
@@ -141,6 +211,12 @@ class _Slot:
         self.event.record(self.stream)
 
     def launch(self):
+        if self.loop is not None:
+            with torch.cuda.stream(self.stream):
+                self.loop.launch()
+                self._copy_back()
+            self.iterations_launched = self.req.max_iter
+            return
         with torch.cuda.stream(self.stream):
             for _ in range(self.k):
                 if self.graph is not None:
@@ -152,7 +228,9 @@ class _Slot:
 
     def done(self):
         """Convergence test on the host copy of the history (call after the
-        event completed)."""
+        event completed).  A device loop has stopped by itself."""
+        if self.loop is not None:
+            return True
         c = int(self.h_counter[0])
         if c >= self.req.max_iter:
             return True
@@ -175,29 +253,74 @@ class _Slot:
     def result(self):
         self.stream.synchronize()
         c = int(self.h_counter[0])
-        return {"theta": self.theta.cpu().numpy(), "loss": float(self.loss_cur.item()),
-                "iterations": min(c, self.req.max_iter)}
+        with torch.cuda.stream(self.stream):
+            theta = self.theta.cpu().numpy()
+            loss = float(self.loss_cur.item())
+        return {"theta": theta, "loss": loss, "iterations": min(c, self.req.max_iter)}
+
+
+_warmed = set()
+
+
+def _warm_engine(device):
+    """Run every kernel family once eagerly on tiny 2D and 3D problems, so
+    that the library's one-time per-device set-up happens outside any stream
+    capture."""
+    if device in _warmed:
+        return
+    for dim in (2, 3):
+        th = np.linspace(0, 3, 3)
+        T = np.stack([np.cos(th), np.sin(th)], 1)
+        w = (np.stack([-T[:, 1], T[:, 0]], 1),)
+        c = np.linspace(-1, 1, 16)
+        if dim == 2:
+            geom = DeviceGeometry(T, w, [c], device)
+            r = np.array([[5.0, 5.0, 0.0]])
+        else:
+            geom = DeviceGeometry(T, w, [c, c.copy()], device)
+            r = np.array([[5.0, 5.0, 5.0, 0.0, 0.0, 0.0]])
+        atoms = engine.DeviceAtoms(np.ones(1), np.zeros((1, dim)), r, device)
+        data = torch.zeros(geom.shape, dtype=torch.float32, device=device)
+        for fit in ("l2", "kl"):
+            fw = engine.fit_forward(atoms, geom, data, fit, 1.0)
+            engine.atom_derivs(atoms, geom, "field", fw["alpha"], fw["beta"],
+                               1.0 if fit == "l2" else 0.0, 2)
+    torch.cuda.synchronize(device)
+    _warmed.add(device)
 
 
 class GaussFitServer:
     """Continuous-batching fitting server (see the module docstring)."""
 
     def __init__(self, device=None, max_slots=32, n_streams=16, hbm_budget=None,
-                 hbm_reserve=4 << 30, use_graphs=True, iters_per_launch=4):
+                 hbm_reserve=4 << 30, use_graphs=True, iters_per_launch=4, device_loop=True,
+                 largest_first=True):
         self.dev = torch.device(device or "cuda")
         engine._require_cuda(self.dev)
         self.max_slots = max_slots
         self.streams = [torch.cuda.Stream(self.dev) for _ in range(n_streams)]
+        self.setup_stream = torch.cuda.Stream(self.dev)
         free, _total = torch.cuda.mem_get_info(self.dev)
         self.budget = hbm_budget if hbm_budget is not None else max(0, free - hbm_reserve)
         self.use_graphs = use_graphs
         self.k = iters_per_launch
+        self.device_loop = device_loop
+        self.largest_first = largest_first
         self.pending = collections.deque()
         self.active = []
         self.results = {}
         self.in_use = 0
         self.stream_busy = [0] * n_streams
         self.admitted_while_busy = 0
+        self.admit_seconds = 0.0     # host time spent setting up admitted requests
+        self.admit_phases = {}       # the same by phase (buffers, streams, capture)
+        self.device_loops = 0        # requests run as one device-resident loop graph
+        # Finished requests' loop graphs are destroyed only when no fit runs:
+        # destroying an executable graph waits for the whole device to idle,
+        # which would stall the host loop behind every fit in flight.
+        self._retired_loops = []
+        self._pinned = {}            # history length -> free pinned host buffers
+        _warm_engine(self.dev)
 
     @staticmethod
     def estimate_bytes(req):
@@ -217,6 +340,14 @@ class GaussFitServer:
         self.pending.append(req)
 
     def _admit(self, now):
+        if self.largest_first and len(self.pending) > 1:
+            # among the requests that have arrived, the largest go first, so
+            # the longest fits start early (arrival order otherwise kept)
+            arrived = [r for r in self.pending if r.arrival <= now]
+            if len(arrived) > 1:
+                later = [r for r in self.pending if r.arrival > now]
+                arrived.sort(key=lambda r: -(r.size_hint[0] * r.size_hint[1]))
+                self.pending = collections.deque(arrived + later)
         while self.pending and len(self.active) < self.max_slots:
             req = self.pending[0]
             if req.arrival > now:
@@ -232,8 +363,17 @@ class GaussFitServer:
             self.stream_busy[si] += 1
             if self.active:
                 self.admitted_while_busy += 1
-            slot = _Slot(req, self.streams[si], self.dev, self.use_graphs, self.k)
+            ta = time.perf_counter()
+            L = req.max_iter + MAX_BACKTRACK + 8
+            free = self._pinned.get(L)
+            slot = _Slot(req, self.streams[si], self.dev, self.use_graphs, self.k,
+                         self.device_loop, self.setup_stream, free.pop() if free else None)
+            self.admit_seconds += time.perf_counter() - ta
+            for k, v in slot.phase_seconds.items():
+                self.admit_phases[k] = self.admit_phases.get(k, 0.0) + v
             slot.stream_index = si
+            if slot.loop is not None:
+                self.device_loops += 1
             slot.need = need
             slot.t_admit = time.perf_counter()
             self.in_use += need
@@ -261,9 +401,15 @@ class GaussFitServer:
                     self.active.remove(slot)
                     self.in_use -= slot.need
                     self.stream_busy[slot.stream_index] -= 1
+                    if slot.loop is not None:
+                        self._retired_loops.append(slot.loop)
+                        slot.loop = None
+                    self._pinned.setdefault(len(slot.h_hist), []).append(slot.pinned)
                     if on_done:
                         on_done(slot.req, res)
                     del slot
+                    if not self.active:
+                        self._release_loops()
                 else:
                     slot.launch()
             if not progressed:
@@ -273,7 +419,16 @@ class GaussFitServer:
                         time.sleep(min(wait, 0.01))
                 else:
                     time.sleep(20e-6)
+        self._release_loops()
         return self.results
+
+    def _release_loops(self):
+        """Destroy the retired loop graphs (nothing of this server runs)."""
+        if self._retired_loops:
+            torch.cuda.synchronize(self.dev)
+            for lp in self._retired_loops:
+                lp.close()
+            self._retired_loops = []
 
 
 def serve_plain(requests, device=None, t0=None):
@@ -289,7 +444,7 @@ def serve_plain(requests, device=None, t0=None):
         if req.arrival > now:
             time.sleep(req.arrival - now)
         geom = DeviceGeometry(req.orientations, req.ortho, req.detector, dev)
-        data = req.make_data(geom, dev, stream)
+        data = req.device_data(geom, dev, stream)
         atoms = engine.DeviceAtoms(*req.init, dev)
         losses = []
         cur, losses = _plain_fit(atoms, geom, data, req)

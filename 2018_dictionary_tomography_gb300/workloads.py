@@ -220,6 +220,21 @@ def config3_requests(n=512, rate=200.0, seed=3, p2d=0.6, atoms=(16, 4096),
     return reqs
 
 
+def materialize_data(requests, device):
+    """Generate every request's data sinogram once (on the device, as
+    ``make_data`` does) and keep it in pinned host memory as
+    ``req.data_host``: the request then carries its payload, and admission
+    only copies it to the device."""
+    import torch
+    from .geometry import DeviceGeometry
+    for req in requests:
+        geom = DeviceGeometry(req.orientations, req.ortho, req.detector, device)
+        d = req.make_data(geom, device, torch.cuda.current_stream(device))
+        req.data_host = d.cpu().pin_memory()
+    torch.cuda.synchronize(device)
+    return requests
+
+
 def _data_maker(truth, seed):
     def make(geom, device, stream):
         import torch

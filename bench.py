@@ -469,7 +469,9 @@ def run_serving(args):
     serving.serve_plain(wl.config3_requests(n=2, rate=1e9, seed=98, atoms=(16, 64), det=(64, 96)), dev)
 
     # (1) saturation comparison on the same requests: served vs plain
-    cmp_reqs = wl.config3_requests(n=args.compare, seed=3)
+    # requests carry their data (generated once, kept in pinned host memory);
+    # admission copies it in, for the served and the plain runs alike
+    cmp_reqs = wl.materialize_data(wl.config3_requests(n=args.compare, seed=3), dev)
     for r in cmp_reqs:
         r.arrival = 0.0
     t0 = time.perf_counter()
@@ -478,15 +480,19 @@ def run_serving(args):
         srv.submit(r)
     served_cmp = srv.run(t0=t0)
     t_served = time.perf_counter() - t0
+    admit_cmp = srv.admit_seconds
+    phases_cmp = dict(srv.admit_phases)
+    loops_cmp = srv.device_loops
     plain_reqs = wl.config3_requests(n=args.compare, seed=3)
-    for r in plain_reqs:
+    for r, c in zip(plain_reqs, cmp_reqs):
         r.arrival = 0.0
+        r.data_host = c.data_host
     t0 = time.perf_counter()
     plain = serving.serve_plain(plain_reqs, dev, t0=t0)
     t_plain = time.perf_counter() - t0
 
     # (2) the Poisson stream (200 requests/s)
-    stream_reqs = wl.config3_requests(n=args.requests, seed=3)
+    stream_reqs = wl.materialize_data(wl.config3_requests(n=args.requests, seed=3), dev)
     sampler = ClockSampler(local)
     sampler.start()
     t0 = time.perf_counter()
@@ -515,6 +521,9 @@ def run_serving(args):
             "served_fits_s": args.compare / t_served,
             "plain_fits_s": args.compare / t_plain,
             "speedup": t_plain / t_served,
+            "served_admission_host_s": admit_cmp,
+            "served_admission_phases_s": phases_cmp,
+            "served_device_loops": loops_cmp,
             "served_latency_p99_s": pct([v["latency"] for v in served_cmp.values()], 99),
             "plain_latency_p99_s": pct([v["latency"] for v in plain.values()], 99),
         },

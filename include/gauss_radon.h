@@ -271,6 +271,47 @@ int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);
 
 /*
+ * Device-resident fitting loop.  Replaces the host-driven iteration of the
+ * reference's Newton loop (GaussDictCode/NewtonGaussian.py:18-109: a Python
+ * loop over sweeps with a host decision per step) by one CUDA graph per
+ * fitting problem whose WHILE conditional node repeats a captured iteration.
+ *
+ *   gr_fit_loop_begin(stream, guard, &loop)  creates the graph (a memset of
+ *       the caller's device int *guard, then the WHILE node) and starts
+ *       capturing `stream` into the loop body (thread-local capture mode);
+ *   the caller then issues ONE iteration on `stream` (gr_fit_forward,
+ *       gr_atom_derivs, gr_newton_solve, gr_fit_forward of the trial atoms,
+ *       gr_newton_accept; no other stream, no host synchronisation, no
+ *       allocation);
+ *   gr_fit_loop_end(loop, stream, hist, hist_acc, counter, hist_len,
+ *       max_iter, max_reject, tol, guard_max, stop_flag) appends the stop
+ *       test and ends the capture;
+ *   gr_fit_loop_instantiate(loop) instantiates the graph (touches no
+ *       stream).  The body runs again unless: counter >= max_iter; the last
+ *       max_reject entries of hist_acc are 0; the last accepted iteration
+ *       i >= 1 changed the loss by at most tol * |hist[i - 1]|; or the body
+ *       ran guard_max times (a bound that holds whatever the buffers
+ *       contain).  The reason is written to *stop_flag (device int,
+ *       nullable): 1 iterations or guard, 2 rejects, 3 converged;
+ *   gr_fit_loop_launch(loop, stream)  runs the whole fit (one graph launch);
+ *   gr_fit_loop_destroy(loop)  (waits until the device is idle: destroy
+ *       finished loops when no fit is running).
+ *
+ * The buffers captured in the body are used by every launch; the caller
+ * keeps them alive until gr_fit_loop_destroy.  On a capture or instantiation
+ * failure gr_fit_loop_end / gr_fit_loop_instantiate return GR_ERR_LAUNCH (the
+ * loop can only be destroyed); gr_fit_loop_launch before a successful
+ * instantiation returns GR_ERR_ARG.
+ */
+int gr_fit_loop_begin(void *stream, int *guard, void **loop);
+int gr_fit_loop_end(void *loop, void *stream, const double *hist, const int *hist_acc,
+                    const int *counter, int hist_len, int max_iter, int max_reject,
+                    double tol, int guard_max, int *stop_flag);
+int gr_fit_loop_instantiate(void *loop);
+int gr_fit_loop_launch(void *loop, void *stream);
+int gr_fit_loop_destroy(void *loop);
+
+/*
  * Kernel timers (no counterpart in the reference; measurement only).  While
  * enabled, CUDA events are recorded on the launching stream around each
  * launch of GR_TIMER_PROJECT (the projection kernel of gr_radproj /

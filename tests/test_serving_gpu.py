@@ -78,3 +78,29 @@ def test_served_fit_matches_plain_fit(cuda_ready):
         # same update rule; the served loop checks convergence after each
         # iteration here, so both stop at the same iteration
         assert abs(served[k]["loss"] - plain[k]["loss"]) <= 1e-5 * abs(plain[k]["loss"])
+
+
+def test_device_loop_matches_host_stepped_graphs(cuda_ready):
+    """The device-resident loop (one graph launch per fit, stop test on the
+    device) and the host-stepped one-iteration graphs (stop test on the host
+    after every iteration) apply the same rule: same iterations, bitwise
+    the same parameters."""
+    reqs = _requests(n=4)
+    for r in reqs:
+        r.arrival = 0.0
+    dev_srv = serving.GaussFitServer(max_slots=4, n_streams=2)
+    for r in reqs:
+        dev_srv.submit(r)
+    dev = dev_srv.run()
+    assert dev_srv.device_loops == len(reqs)
+    host_srv = serving.GaussFitServer(max_slots=4, n_streams=2, device_loop=False,
+                                      iters_per_launch=1)
+    reqs2 = _requests(n=4)
+    for r in reqs2:
+        r.arrival = 0.0
+        host_srv.submit(r)
+    host = host_srv.run()
+    assert host_srv.device_loops == 0
+    for k in dev:
+        assert dev[k]["iterations"] == host[k]["iterations"]
+        assert np.array_equal(dev[k]["theta"], host[k]["theta"])
