@@ -32,6 +32,11 @@ graph waits for the device to idle); pinned host buffers are pooled.  Among
 requests that have arrived, the largest are admitted first, so the longest
 fits start early.
 
+The process should give every stream its own hardware work queue
+(environment ``CUDA_DEVICE_MAX_CONNECTIONS`` >= n_streams + 1, set before CUDA
+starts): with fewer, streams share queues and a request's set-up can wait
+behind another request's whole fit.
+
 ``serve_plain`` is the baseline: the same fits one after another with the
 eager host-driven loop, one host sync per iteration.
 """

@@ -449,6 +449,10 @@ def run_reference(args):
 # config 3: served stream
 # --------------------------------------------------------------------------
 def run_serving(args):
+    # one hardware work queue per stream (16 fit streams + the setup stream):
+    # with the default 8, streams share queues and a short copy can wait
+    # behind another request's whole fit; must be set before CUDA starts
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     import torch
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
