@@ -484,19 +484,27 @@ class FitLoop:
         self._keep = (hist, hist_acc, counter)
         h = ctypes.c_void_p()
         sh = ctypes.c_void_p(stream.cuda_stream)
+        import time
+        t0 = time.perf_counter()
         with torch.cuda.stream(stream):
             _lib.check(lib.gr_fit_loop_begin(sh, self.guard.data_ptr(), ctypes.byref(h)),
                        "gr_fit_loop_begin")
             self.handle = h
+            t1 = time.perf_counter()
             try:
                 capture_iteration()
             finally:
+                t2 = time.perf_counter()
                 rc = lib.gr_fit_loop_end(
                     h, sh, hist.data_ptr(), hist_acc.data_ptr(), counter.data_ptr(),
                     int(hist.numel()), int(max_iter), int(max_reject), float(tol),
                     int(max_iter) + int(max_reject) + 2, self.stop_reason.data_ptr())
+        t3 = time.perf_counter()
         if rc == 0:
             rc = lib.gr_fit_loop_instantiate(h)
+        # host seconds of each step of building the loop
+        self.seconds = {"loop_begin": t1 - t0, "loop_iteration": t2 - t1,
+                        "loop_end": t3 - t2, "loop_instantiate": time.perf_counter() - t3}
         if rc != 0:
             self.close()
             _lib.check(rc, "gr_fit_loop_end")

@@ -374,7 +374,10 @@ class GaussFitServer:
             slot = _Slot(req, self.streams[si], self.dev, self.use_graphs, self.k,
                          self.device_loop, self.setup_stream, free.pop() if free else None)
             self.admit_seconds += time.perf_counter() - ta
-            for k, v in slot.phase_seconds.items():
+            phases = dict(slot.phase_seconds)
+            if slot.loop is not None:
+                phases.update(slot.loop.seconds)
+            for k, v in phases.items():
                 self.admit_phases[k] = self.admit_phases.get(k, 0.0) + v
             slot.stream_index = si
             if slot.loop is not None:
