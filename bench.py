@@ -465,8 +465,11 @@ def run_serving(args):
         return float(np.percentile(np.asarray(v), q)) if len(v) else None
 
     # warm-up (compilation of lazy modules, allocator)
-    warm = wl.config3_requests(n=4, rate=1e9, seed=99, atoms=(16, 64), det=(64, 96))
-    srv = serving.GaussFitServer(dev, max_slots=4, n_streams=4)
+    # (64 tiny fits at once: the driver's one-time cost of the first wave of
+    # graph instantiations in a process is paid here, as by a running server)
+    warm = wl.config3_requests(n=64, rate=1e9, seed=99, atoms=(16, 64), angles=(10, 20),
+                               det=(32, 48), max_iter=4)
+    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=16)
     for r in warm:
         srv.submit(r)
     srv.run()
