@@ -16,6 +16,11 @@ constexpr int kListWords = 16;       // bitmap words compacted per pass
 constexpr int kProjWarpFloats =
     2 * kTileCells + 64 + kTileDim1 + kListWords * 32;
 
+// Parameters of a per-atom regulariser (gr_reg.cu).
+struct RegParams {
+  double p[8];
+};
+
 struct TileCfg {
   int t0, t1;     // tile extent along detector axes 0 and 1
   int nt0, nt1;   // tiles along each axis

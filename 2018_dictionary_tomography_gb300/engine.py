@@ -524,3 +524,30 @@ class FitLoop:
             self.close()
         except Exception:
             pass
+
+
+REG_KINDS = {"null": 0, "joubert": 1, "mass": 2, "volume": 3, "radius": 4, "iso": 5}
+
+
+def regulariser(kind, params, atoms, f=None, g=None, H=None, accumulate=False, order=2):
+    """Per-atom regulariser value (N,), gradient (N, P) and Hessian (N, P, P)
+    (order 2) in FP64 on the device (``gr_regulariser``); with
+    ``accumulate=True`` the terms are added to the given f, g, H (e.g. the
+    outputs of ``atom_derivs``).  ``kind`` is a name of ``REG_KINDS``."""
+    import numpy as np
+    dev = atoms.I.device
+    n, P = atoms.n, atoms.n_params()
+    f64 = dict(dtype=torch.float64, device=dev)
+    if f is None:
+        f = torch.zeros(n, **f64)
+    if g is None:
+        g = torch.zeros(n, P, **f64)
+    if H is None and order > 1:
+        H = torch.zeros(n, P, P, **f64)
+    p = np.ascontiguousarray(np.asarray(params, dtype=np.float64).reshape(-1))
+    lib = _lib.load()
+    st = lib.gr_regulariser(REG_KINDS[kind], p.ctypes.data if p.size else None, int(p.size),
+                            ctypes.byref(atoms.struct), int(atoms.dim), _ptr(f), _ptr(g),
+                            _ptr(H), 1 if accumulate else 0, _stream_handle(dev))
+    _lib.check(st, "gr_regulariser")
+    return f, g, H

@@ -271,6 +271,37 @@ int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);
 
 /*
+ * Per-atom regularisers of the fitting loops.  Replaces the regulariser
+ * classes of GaussDictCode/regularisation.py (Joubert :41-107, Mass :110-208,
+ * Volume :211-297, Radius :300-366, Iso :369-442), whose value, gradient and
+ * Hessian the Newton loop adds to each atom's block (NewtonGaussian.py:59-66).
+ * For every atom: value f[j], gradient g[j, P] and Hessian H[j, P, P] in the
+ * parameter order [I, x, r] (P = 1 + dim + 3|6, or 2 + dim for isotropic
+ * atoms), in FP64; written, or added to the arrays when accumulate != 0 (so
+ * the call can follow gr_atom_derivs on the same outputs).  f and H may be
+ * NULL.  kind and params (n_params <= 8):
+ *   GR_REG_JOUBERT  (a, b, c, d, e): -a log I + b/2|x|^2 + c R - d log R - e,
+ *                   R = prod(diag r) or s^dim; the reference's
+ *                   Joubert(dim, intensity, location, radius) has a =
+ *                   intensity, b = location, c = radius[1], d = radius[1]
+ *                   radius[0], e = radius[0] radius[1] (1 - log radius[0]);
+ *   GR_REG_MASS     (m, k, w): w (I V - m)^k, V = 1/prod(diag r) or s^dim;
+ *   GR_REG_VOLUME   (v0, k, w): w |R - v0|^k, R = prod(diag r) or s^-dim
+ *                   (the reference's r0 gives v0 = |r0|^dim);
+ *   GR_REG_RADIUS   (r0, w, k): w sum (r_ii - r0)^-k (isotropic: dim (s - r0)^-k);
+ *   GR_REG_ISO      (w): w/2 |off-diagonal r|^2.
+ * Values outside the domain (log or power of a non-positive number) are
+ * +inf, as in the reference.  Hessians are exact (the reference's Joubert has
+ * none, its Volume Hessian cannot run, its Mass Hessian misses mixed r-r
+ * terms).  GR_ERR_ARG for an unknown kind, dim not 2 or 3, or missing
+ * pointers.
+ */
+enum { GR_REG_NULL = 0, GR_REG_JOUBERT = 1, GR_REG_MASS = 2, GR_REG_VOLUME = 3,
+       GR_REG_RADIUS = 4, GR_REG_ISO = 5 };
+int gr_regulariser(int kind, const double *params, int n_params, const gr_atoms *atoms, int dim,
+                   double *f, double *g, double *H, int accumulate, void *stream);
+
+/*
  * Device-resident fitting loop.  Replaces the host-driven iteration of the
  * reference's Newton loop (GaussDictCode/NewtonGaussian.py:18-109: a Python
  * loop over sweeps with a host decision per step) by one CUDA graph per
