@@ -264,23 +264,35 @@ def atoms_of(theta, dim, dev):
 
 
 def newton_batched(atoms, geom, data, iters, fit="l2", background=0.0, lam0=1.0,
-                   lam_min=1e-4, lam_max=1e4, max_backtrack=8, tol=0.0, history=None):
+                   lam_min=1e-4, lam_max=1e4, max_backtrack=8, tol=0.0, history=None,
+                   reg=None):
     """Damped Newton on every atom at once, FP64 Hessian solves on the device.
 
     Each iteration: one fused forward (fit fields + loss), one derivative call
     (gradient and Hessian of every atom), then backtracking: solve
     (H_j + lam 1) d_j = -g_j for all atoms, re-evaluate the loss, accept when
     it does not increase (lam /= 2), else lam *= 10 and retry.
-    Stops after ``iters`` iterations or when the relative loss change falls
-    below ``tol``.  Returns (DeviceAtoms, losses list).
+    With a regulariser (``regularisation.Joubert`` etc.) its per-atom
+    gradient and Hessian are added on the device to every block and the
+    energy loss + reg(atoms) is what must not increase, as in the
+    reference's loop (NewtonGaussian.py:59-66).
+    Stops after ``iters`` iterations or when the relative change falls
+    below ``tol``.  Returns (DeviceAtoms, energies list).
     """
+    use_reg = reg is not None and hasattr(reg, "terms")
+
+    def energy(a, fit_loss):
+        if not use_reg:
+            return fit_loss
+        return fit_loss + float(reg.terms(a, order=1)[0].sum().item())
+
     dev = geom.device
     dim = atoms.dim
     iso = atoms.iso
     theta = theta_of(atoms.I, atoms.x, atoms.r)
     beta_c = 1.0 if fit == "l2" else 0.0
     fw = engine.fit_forward(atoms, geom, data, fit, background)
-    loss = float(fw["loss"].item())
+    loss = energy(atoms, float(fw["loss"].item()))
     losses = [loss] if history is None else history
     if history is not None:
         history.append(loss)
@@ -289,12 +301,14 @@ def newton_batched(atoms, geom, data, iters, fit="l2", background=0.0, lam0=1.0,
     rel = float("inf")
     for _ in range(iters):
         _f, g, H = engine.atom_derivs(cur, geom, "field", fw["alpha"], fw["beta"], beta_c, 2)
+        if use_reg:
+            reg.device_terms(cur, _f, g, H)
         accepted = False
         for _b in range(max_backtrack):
             th_new, _step, _fail = newton_solve_t(dim, iso, g, H, lam, theta)
             trial = atoms_of(th_new, dim, dev)
             fw_new = engine.fit_forward(trial, geom, data, fit, background)
-            new_loss = float(fw_new["loss"].item())
+            new_loss = energy(trial, float(fw_new["loss"].item()))
             if new_loss <= loss:
                 accepted = True
                 rel = (loss - new_loss) / max(abs(loss), 1e-300)
