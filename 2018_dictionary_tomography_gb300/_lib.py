@@ -44,7 +44,8 @@ EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
            "gr_psf_radproj", "gr_psf_fit_forward", "gr_psf_atom_derivs", "gr_psf_volproj",
            "gr_set_tuning", "gr_get_tuning", "gr_kernel_timer", "gr_kernel_timer_read",
            "gr_fit_loop_begin", "gr_fit_loop_end", "gr_fit_loop_instantiate",
-           "gr_fit_loop_launch", "gr_fit_loop_destroy", "gr_regulariser")
+           "gr_fit_loop_launch", "gr_fit_loop_destroy", "gr_regulariser",
+           "gr_sino_moments")
 
 _lock = threading.Lock()
 _lib = None
@@ -127,6 +128,9 @@ def load(build_if_missing=True):
         lib.gr_kernel_timer.restype = ctypes.c_int
         lib.gr_kernel_timer.argtypes = [ctypes.c_int, ctypes.c_int]
         vp = ctypes.c_void_p
+        lib.gr_sino_moments.restype = ctypes.c_int
+        lib.gr_sino_moments.argtypes = [ctypes.POINTER(GrGeometry), vp, vp, ctypes.c_float,
+                                        ctypes.c_float, vp, vp, vp, vp]
         lib.gr_regulariser.restype = ctypes.c_int
         lib.gr_regulariser.argtypes = [ctypes.c_int, vp, ctypes.c_int, ctypes.POINTER(GrAtoms),
                                        ctypes.c_int, vp, vp, vp, ctypes.c_int, vp]

@@ -17,7 +17,8 @@ INC = os.path.join(ROOT, "include")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libgauss_radon.so")
 SOURCES = ["gr_api.cu", "gr_project.cu", "gr_derivs.cu", "gr_probe.cu", "gr_noalloc.cu",
-           "gr_update.cu", "gr_volume.cu", "gr_loop.cu", "gr_reg.cu"]
+           "gr_update.cu", "gr_volume.cu", "gr_loop.cu", "gr_reg.cu",
+           "gr_moments.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -276,6 +276,16 @@ int gr_probe_ex2(int blocks, int threads, int iters, float *sink, void *stream) 
 
 unsigned long long gr_launch_count(void) { return g_launches.load(); }
 
+int gr_sino_moments(const gr_geometry *geom, const float *res, const float *rr, float t,
+                    float scale, double *S0, double *S1, double *S2, void *stream) {
+  gr_atoms none = {};
+  Atoms at;
+  Geom g;
+  int st;
+  if (!to_internal(&none, geom, at, g, &st)) return st;
+  return launch_moments(g, res, rr, t, scale, S0, S1, S2, static_cast<cudaStream_t>(stream));
+}
+
 int gr_kernel_timer(int which, int enable) { return gr::timer_enable(which, enable); }
 
 int gr_kernel_timer_read(int which, double *total_ms, int *launches) {

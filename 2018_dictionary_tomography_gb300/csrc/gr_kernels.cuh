@@ -112,6 +112,8 @@ int get_tuning(int key);
 
 // host-side count of kernels launched by this library
 void note_launches(int n);
+int launch_moments(const Geom &g, const float *res, const float *rr, float t, float scale,
+                   double *S0, double *S1, double *S2, cudaStream_t stream);
 // kernel timers (which: 1 projection kernel, 2 derivative kernel)
 void timer_mark(int which, int end, cudaStream_t stream);
 int timer_enable(int which, int enable);

@@ -271,6 +271,22 @@ int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);
 
 /*
+ * Per-angle detector moments of a sinogram, for the moment-matching initial
+ * guess of a new atom.  Replaces the reference's MOM0 / MOM1 / MOM2
+ * (KL_GaussRadon.py:227-253, :347-368), CPU loops inside its guess
+ * doKL_ProjGDStep_iso (:57-121).  Over the target
+ *     f = max(0, res)                          (rr == NULL)
+ *     f = max(0, t res + (1 - t) scale rr)     (otherwise; the blend of the
+ *                                                reference's iteration)
+ * (res, rr: sinograms of geom's shape) it writes, in FP64 and a fixed order,
+ *     S0[a] = sum f,  S1[a][i] = sum f p_i,  S2[a][i] = sum f p_i^2
+ * for every angle a and detector axis i < kdet (p_i the cell coordinate).
+ * GR_ERR_ARG for missing pointers or an invalid geometry.
+ */
+int gr_sino_moments(const gr_geometry *geom, const float *res, const float *rr, float t,
+                    float scale, double *S0, double *S1, double *S2, void *stream);
+
+/*
  * Per-atom regularisers of the fitting loops.  Replaces the regulariser
  * classes of GaussDictCode/regularisation.py (Joubert :41-107, Mass :110-208,
  * Volume :211-297, Radius :300-366, Iso :369-442), whose value, gradient and
