@@ -121,22 +121,60 @@ def step_params(I, x, r, d, dim, iso):
 
 def Newton_linesearch(recon, data, max_iter, fidelity, reg, Radon, view=None,
                       guess=None, tol=1e-4, min_iter=1, resync=True, **kwargs):
-    """Damped per-atom Newton sweeps (NewtonGaussian.linesearch)."""
-    if guess is not None:
-        raise NotImplementedError("moment-matching initial guesses are not provided")
+    """Damped per-atom Newton sweeps (NewtonGaussian.linesearch).
+
+    With ``guess`` (e.g. ``lambda res, atom: KL_GaussRadon.doKL_ProjGDStep_iso(
+    res, atom, 1.0, Radon)``) atoms are inserted one at a time as in the
+    reference (NewtonGaussian.py:27-106): atom n is guessed from the residual
+    data - R(atoms[:n]) and the first n atoms are swept; with a third entry in
+    ``max_iter`` a final round of max_iter[2] sweeps covers all atoms.
+    """
     max_iter = _max_iter(max_iter)
     nAtoms = len(recon)
-    E = np.zeros(int(np.prod(max_iter[:2])) * nAtoms + 1)
+    per = int(np.prod(max_iter[:2]))
+    size = per * nAtoms * (nAtoms + 1) // 2 + nAtoms + 2
+    if len(max_iter) > 2:
+        size += int(max_iter[2]) * int(max_iter[1]) * nAtoms
+    E = np.zeros(size if guess is not None else per * nAtoms + 1)
     F = np.zeros_like(E)
-    eps = 1e-4
     h = [1.0] * nAtoms
-    st = _DeviceFit(recon, data, fidelity, Radon)
-    F[0] = st.loss
-    E[0] = F[0] + reg(recon)
     dim, iso = recon.space.dim, recon.space.isotropic
-    n = nAtoms
     np.random.seed(1)
+    if guess is None:
+        st = _DeviceFit(recon, data, fidelity, Radon)
+        F[0] = st.loss
+        E[0] = F[0] + reg(recon)
+        jj = _newton_sweeps(recon, nAtoms, st, h, E, F, 1, max_iter, reg, tol, min_iter,
+                            resync, dim, iso)
+        return recon, E[:jj], F[:jj]
+    d = data.asarray() if hasattr(data, "asarray") else data
+    d = np.asarray(d.detach().cpu() if hasattr(d, "detach") else d, dtype=np.float64)
+    n = 1
     jj = 1
+    while n <= nAtoms + 1:
+        if n == nAtoms + 1:
+            if len(max_iter) == 2:
+                break
+            n = nAtoms
+            max_iter = [max_iter[2], max_iter[1]]
+        else:
+            sub = recon[:n].copy()
+            res = d - np.asarray(Radon(sub).asarray(), dtype=np.float64)
+            recon[n - 1] = guess(res, recon[n - 1].copy())
+        sub = recon[:n].copy()
+        st = _DeviceFit(sub, data, fidelity, Radon)
+        F[jj - 1] = st.loss
+        E[jj - 1] = F[jj - 1] + reg(sub)
+        jj = _newton_sweeps(sub, n, st, h, E, F, jj, max_iter, reg, tol, min_iter, resync,
+                            dim, iso)
+        recon[:n] = sub
+        n += 1
+    return recon, E[:jj], F[:jj]
+
+
+def _newton_sweeps(recon, n, st, h, E, F, jj, max_iter, reg, tol, min_iter, resync, dim, iso):
+    """Sweeps of per-atom damped Newton steps over recon[:n]; returns jj."""
+    eps = 1e-4
     for it in range(max_iter[0]):
         BREAK = [True, True]
         for j in np.random.permutation(np.arange(n)):
@@ -179,7 +217,7 @@ def Newton_linesearch(recon, data, max_iter, fidelity, reg, Radon, view=None,
             st.resync(recon)
         if BREAK[0] and it > min_iter:
             break
-    return recon, E[:jj], F[:jj]
+    return jj
 
 
 def GD_linesearch_block(recon, data, max_iter, fidelity, reg, Radon, view=None,
