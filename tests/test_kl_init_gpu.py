@@ -26,13 +26,14 @@ def test_moment_kernel_matches_numpy(cuda_ready, kind):
     for rrt, t, s in ((None, 1.0, 1.0), (rr, 0.3, 1.7)):
         dev_rr = None if rrt is None else torch.from_numpy(rrt).cuda()
         S0, S1, S2 = kl.sino_moments(geom, torch.from_numpy(res).cuda(), dev_rr, t, s)
-        f = np.maximum(0.0, res if rrt is None else t * res.astype(np.float64)
-                       + (1 - t) * s * rrt.astype(np.float64))
         f = np.maximum(0.0, (res if rrt is None else (np.float32(t) * res
                         + np.float32(1 - t) * np.float32(s) * rrt)).astype(np.float64))
         o0, o1, o2 = ko.moments(f, g)
+        # FP64 sums of the same FP32 cells; the blend is formed in FP32 on
+        # the device (possibly fused), so it may differ in the last bit
+        tol = 1e-10 if rrt is None else 1e-6
         for a, b in ((S0, o0), (S1, o1), (S2, o2)):
-            assert np.abs(a.cpu().numpy() - b).max() <= 1e-10 * max(1.0, np.abs(b).max())
+            assert np.abs(a.cpu().numpy() - b).max() <= tol * max(1.0, np.abs(b).max())
 
 
 @pytest.mark.parametrize("kind", ["2d", "2p5d", "3d"])
