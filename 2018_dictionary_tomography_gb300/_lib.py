@@ -45,7 +45,7 @@ EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
            "gr_set_tuning", "gr_get_tuning", "gr_kernel_timer", "gr_kernel_timer_read",
            "gr_fit_loop_begin", "gr_fit_loop_end", "gr_fit_loop_instantiate",
            "gr_fit_loop_launch", "gr_fit_loop_destroy", "gr_regulariser",
-           "gr_sino_moments")
+           "gr_sino_moments", "gr_accept_fields")
 
 _lock = threading.Lock()
 _lib = None
@@ -128,6 +128,8 @@ def load(build_if_missing=True):
         lib.gr_kernel_timer.restype = ctypes.c_int
         lib.gr_kernel_timer.argtypes = [ctypes.c_int, ctypes.c_int]
         vp = ctypes.c_void_p
+        lib.gr_accept_fields.restype = ctypes.c_int
+        lib.gr_accept_fields.argtypes = [vp, vp, vp, vp, vp, vp, ctypes.c_size_t, vp]
         lib.gr_sino_moments.restype = ctypes.c_int
         lib.gr_sino_moments.argtypes = [ctypes.POINTER(GrGeometry), vp, vp, ctypes.c_float,
                                         ctypes.c_float, vp, vp, vp, vp]

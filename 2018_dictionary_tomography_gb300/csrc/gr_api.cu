@@ -286,6 +286,13 @@ int gr_sino_moments(const gr_geometry *geom, const float *res, const float *rr, 
   return launch_moments(g, res, rr, t, scale, S0, S1, S2, static_cast<cudaStream_t>(stream));
 }
 
+int gr_accept_fields(const double *loss_cur, const double *loss_trial, const float *alpha_trial,
+                     float *alpha, const float *beta_trial, float *beta, size_t n_cells,
+                     void *stream) {
+  return launch_accept_fields(loss_cur, loss_trial, alpha_trial, alpha, beta_trial, beta, n_cells,
+                              static_cast<cudaStream_t>(stream));
+}
+
 int gr_kernel_timer(int which, int enable) { return gr::timer_enable(which, enable); }
 
 int gr_kernel_timer_read(int which, double *total_ms, int *launches) {

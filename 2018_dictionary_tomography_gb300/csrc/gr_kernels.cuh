@@ -112,6 +112,9 @@ int get_tuning(int key);
 
 // host-side count of kernels launched by this library
 void note_launches(int n);
+int launch_accept_fields(const double *loss_cur, const double *loss_trial, const float *alpha_t,
+                         float *alpha, const float *beta_t, float *beta, size_t n,
+                         cudaStream_t stream);
 int launch_moments(const Geom &g, const float *res, const float *rr, float t, float scale,
                    double *S0, double *S1, double *S2, cudaStream_t stream);
 // kernel timers (which: 1 projection kernel, 2 derivative kernel)

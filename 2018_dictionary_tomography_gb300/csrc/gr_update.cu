@@ -313,6 +313,35 @@ __global__ void gr_newton_accept_kernel(int n, int P, int pr, int dim,
   }
 }
 
+// After gr_newton_accept: when the trial was accepted (the accept kernel
+// then set loss_cur to exactly loss_trial; a rejected trial has a larger
+// loss), the trial's fit fields become the current ones, so the next
+// iteration needs no projection of the current atoms.
+__global__ void __launch_bounds__(256)
+    gr_accept_fields_kernel(const double *loss_cur, const double *loss_trial,
+                            const float *alpha_t, float *alpha, const float *beta_t,
+                            float *beta, size_t n) {
+  if (!(*loss_cur == *loss_trial)) return;  // rejected: keep the current fields
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    alpha[e] = alpha_t[e];
+    if (beta) beta[e] = beta_t[e];
+  }
+}
+
+int launch_accept_fields(const double *loss_cur, const double *loss_trial, const float *alpha_t,
+                         float *alpha, const float *beta_t, float *beta, size_t n,
+                         cudaStream_t stream) {
+  if (!loss_cur || !loss_trial || !alpha_t || !alpha || (beta && !beta_t)) return kErrArg;
+  if (n == 0) return kOk;
+  size_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  gr_accept_fields_kernel<<<(unsigned)blocks, 256, 0, stream>>>(loss_cur, loss_trial, alpha_t,
+                                                                alpha, beta_t, beta, n);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
 int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
                          const double *loss_trial, double *theta,
                          const double *theta_trial, double *lam, double lam_min,

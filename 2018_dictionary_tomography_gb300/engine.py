@@ -347,6 +347,14 @@ def newton_solve_into(dim, iso, g, H, lam, theta, theta_new, step, trial_atoms, 
     _lib.check(st, "gr_newton_solve")
 
 
+def accept_fields_into(loss_cur, loss_trial, alpha_t, alpha, beta_t, beta, device):
+    """Trial fields become the current ones if the trial was accepted."""
+    st = _lib.load().gr_accept_fields(
+        loss_cur.data_ptr(), loss_trial.data_ptr(), alpha_t.data_ptr(), alpha.data_ptr(),
+        _ptr(beta_t), _ptr(beta), int(alpha.numel()), _stream_handle(device))
+    _lib.check(st, "gr_accept_fields")
+
+
 def newton_accept_into(dim, iso, loss_cur, loss_trial, theta, theta_trial, lam, lam_min,
                        lam_max, cur_atoms, trial_atoms, hist, hist_acc, counter, device):
     st = _lib.load().gr_newton_accept(

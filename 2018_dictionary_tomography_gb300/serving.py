@@ -6,12 +6,15 @@ slot and enough free HBM are available, also while other requests are being
 fitted; every admitted request owns its device buffers and a CUDA stream, and
 one damped-Newton iteration
 
-  gr_fit_forward(current atoms)  -> fit fields, loss
   gr_atom_derivs(all atoms)      -> gradient and Hessian blocks
   gr_newton_solve                -> trial parameters (FP64 solves on the device)
-  gr_fit_forward(trial atoms)    -> trial loss
+  gr_fit_forward(trial atoms)    -> trial fit fields, trial loss
   gr_newton_accept               -> device-side accept/reject, damping update,
                                     loss history
+  gr_accept_fields               -> an accepted trial's fields become current
+
+(one projection per iteration: the current atoms' fields come from the
+prologue's gr_fit_forward, an accepted trial, or stay after a rejection)
 
 is captured once into the body of a device-resident loop (engine.FitLoop: a
 CUDA graph whose WHILE node repeats the iteration until a device-side stop
@@ -118,6 +121,10 @@ class _Slot:
             self.alpha = torch.empty(shape, dtype=torch.float32, device=device)
             self.beta = (torch.empty(shape, dtype=torch.float32, device=device)
                          if req.fit == "kl" else None)
+            # the trial's fit fields (adopted when the trial is accepted)
+            self.alpha_t = torch.empty(shape, dtype=torch.float32, device=device)
+            self.beta_t = (torch.empty(shape, dtype=torch.float32, device=device)
+                           if req.fit == "kl" else None)
             self.loss_cur = torch.zeros((), dtype=torch.float64, device=device)
             self.loss_trial = torch.zeros((), dtype=torch.float64, device=device)
             self.f = torch.empty(n, dtype=torch.float64, device=device)
@@ -146,6 +153,7 @@ class _Slot:
             for t in (self.geom.frames, self.geom.det, self.cur.I, self.cur.x,
                       self.cur.r, self.trial.I, self.trial.x, self.trial.r, self.theta,
                       self.theta_trial, self.lam, self.data, self.alpha, self.beta,
+                      self.alpha_t, self.beta_t,
                       self.loss_cur, self.loss_trial, self.f, self.g, self.H, self.step,
                       self.ws_p, self.ws_d, self.hist, self.hist_acc, self.counter):
                 for u in (t if isinstance(t, (list, tuple)) else (t,)):
@@ -172,6 +180,7 @@ class _Slot:
             if self.loop is not None:
                 self.iterations_launched = 0
                 return
+            self.prologue()
             self.iterate()                       # eager first iteration (also warms up)
             if use_graph:
                 # captured directly on this request's stream: the
@@ -189,25 +198,35 @@ class _Slot:
         self.iterations_launched = 1
 
     def bytes(self):
-        tensors = [self.data, self.alpha, self.beta, self.g, self.H, self.ws_p, self.ws_d,
+        tensors = [self.data, self.alpha, self.beta, self.alpha_t, self.beta_t, self.g,
+                   self.H, self.ws_p, self.ws_d,
                    self.theta, self.theta_trial]
         return sum(t.numel() * t.element_size() for t in tensors if t is not None)
 
-    def iterate(self):
+    def prologue(self):
+        """Fit fields and loss of the starting atoms (once per fit)."""
         r = self.req
-        beta_c = 1.0 if r.fit == "l2" else 0.0
         engine.fit_forward_into(self.cur, self.geom, self.data, r.fit, r.background, None,
                                 self.alpha, self.beta, self.loss_cur, self.ws_p)
+
+    def iterate(self):
+        """One damped-Newton iteration.  The current atoms' fields are always
+        valid here (from the prologue, an accepted trial, or unchanged after
+        a rejected one), so only the trial is projected."""
+        r = self.req
+        beta_c = 1.0 if r.fit == "l2" else 0.0
         engine.atom_derivs_into(self.cur, self.geom, "field", self.alpha, self.beta, beta_c, 2,
                                 self.f, self.g, self.H, self.ws_d)
         engine.newton_solve_into(self.dim, self.iso, self.g, self.H, self.lam, self.theta,
                                  self.theta_trial, self.step, self.trial, self.dev)
         engine.fit_forward_into(self.trial, self.geom, self.data, r.fit, r.background, None,
-                                None, None, self.loss_trial, self.ws_p)
+                                self.alpha_t, self.beta_t, self.loss_trial, self.ws_p)
         engine.newton_accept_into(self.dim, self.iso, self.loss_cur, self.loss_trial,
                                   self.theta, self.theta_trial, self.lam, 1e-4, 1e4,
                                   self.cur, self.trial, self.hist, self.hist_acc,
                                   self.counter, self.dev)
+        engine.accept_fields_into(self.loss_cur, self.loss_trial, self.alpha_t, self.alpha,
+                                  self.beta_t, self.beta, self.dev)
 
     def _copy_back(self):
         self.h_counter.copy_(self.counter, non_blocking=True)
@@ -218,6 +237,7 @@ class _Slot:
     def launch(self):
         if self.loop is not None:
             with torch.cuda.stream(self.stream):
+                self.prologue()
                 self.loop.launch()
                 self._copy_back()
             self.iterations_launched = self.req.max_iter
@@ -333,7 +353,7 @@ class GaussFitServer:
         n, cells = req.size_hint
         dim = len(req.init[1][0]) if n else 2
         P = 1 + dim + (1 if np.asarray(req.init[2]).reshape(n, -1).shape[1] == 1 else (3 if dim == 2 else 6))
-        sino = cells * 4 * (2 + (1 if req.fit == "kl" else 0))
+        sino = cells * 4 * (3 + (2 if req.fit == "kl" else 0))
         tiles = max(1, cells // (32 if dim == 2 else 1024)) + len(req.orientations)
         bitmap = tiles * ((n + 31) // 32) * 4 + tiles * 8
         qn = 1 + P + P * (P + 1) // 2

@@ -318,6 +318,19 @@ int gr_regulariser(int kind, const double *params, int n_params, const gr_atoms 
                    double *f, double *g, double *H, int accumulate, void *stream);
 
 /*
+ * After gr_newton_accept: if the trial was accepted (loss_cur == loss_trial),
+ * copy the trial's fit fields (from gr_fit_forward of the trial atoms) over
+ * the current ones; otherwise do nothing.  With it a Newton iteration needs
+ * one projection (of the trial) instead of two: the current atoms' fields
+ * are either the accepted trial's or unchanged.  No counterpart in the
+ * reference, whose host loop re-projects (NewtonGaussian.py:59-75).
+ * beta / beta_trial may be NULL (L2 fits).
+ */
+int gr_accept_fields(const double *loss_cur, const double *loss_trial, const float *alpha_trial,
+                     float *alpha, const float *beta_trial, float *beta, size_t n_cells,
+                     void *stream);
+
+/*
  * Device-resident fitting loop.  Replaces the host-driven iteration of the
  * reference's Newton loop (GaussDictCode/NewtonGaussian.py:18-109: a Python
  * loop over sweeps with a host decision per step) by one CUDA graph per
