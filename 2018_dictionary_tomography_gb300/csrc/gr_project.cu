@@ -255,20 +255,20 @@ __global__ void __launch_bounds__(kProjWarps * 32)
 
 // 2D sinograms: atom footprints are a few cells wide, so a block owns a tile
 // of 32 consecutive cells of one angle, one cell per lane.  The tile's
-// bitmap words are split into kProjWarps consecutive ranges, one per warp, so
-// a tile's atoms are walked by four warps at once; each warp keeps its
+// bitmap words are split into NW consecutive ranges, one per warp (4 warps,
+// 8 for long atom lists), so a tile's atoms are walked by NW warps at once; each warp keeps its
 // partial cell sums in registers.  Pair data of up to 32 listed atoms is
 // computed in parallel (one atom per lane) and staged in shared memory; every
 // lane then walks the batch in atom order and adds the atoms whose support
 // box holds its cell.  The warps' partial sums are combined in warp order
 // with a compensated sum: results are bitwise reproducible.
-template <bool KAHAN>
-__global__ void __launch_bounds__(kProjWarps * 32)
+template <bool KAHAN, int NW>
+__global__ void __launch_bounds__(NW * 32)
     gr_project1d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
                         int W, ProjOut out, double *loss_out, int *done) {
-  __shared__ float4 prm[kProjWarps][32][2];
-  __shared__ int lists[kProjWarps][kListWords * 32];
-  __shared__ float parts[kProjWarps][2][32];
+  __shared__ float4 prm[NW][32][2];
+  __shared__ int lists[NW][kListWords * 32];
+  __shared__ float parts[NW][2][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int item = blockIdx.x;
   int *list = lists[warp];
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   float acc = 0.f, cmp = 0.f;
 
   const uint32_t *words = bitmap + (size_t)item * W;
-  const int wq = (W + kProjWarps - 1) / kProjWarps;
+  const int wq = (W + NW - 1) / NW;
   const int w_lo = warp * wq, w_hi = min(W, w_lo + wq);
   for (int wb = w_lo; wb < w_hi; wb += kListWords) {
     const int wi = wb + (lane < kListWords ? lane : 0);
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   // combine the warps' partial sums in warp order (compensated)
   float s0 = 0.f, c0 = 0.f;
 #pragma unroll
-  for (int w = 0; w < kProjWarps; ++w) {
+  for (int w = 0; w < NW; ++w) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const float v = parts[w][h][lane];
@@ -607,8 +607,10 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   }
 }
 
-__global__ void gr_loss_finalize_kernel(const double *part, int n, double *out) {
-  __shared__ double sh[256];
+constexpr int kLossThreads = 1024;
+__global__ void __launch_bounds__(kLossThreads)
+    gr_loss_finalize_kernel(const double *part, int n, double *out) {
+  __shared__ double sh[kLossThreads];
   double s = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
   sh[threadIdx.x] = s;
@@ -738,8 +740,13 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
     // one block per (angle, tile) item; for up to kFusedLossItems tiles the
     // last block also sums the loss partials (no separate finalize launch)
     fused_loss = loss_out != nullptr && items <= kFusedLossItems;
-    gr_project1d_kernel<true><<<(unsigned)items, kProjWarps * 32, 0, stream>>>(
-        at, g, tc, bitmap, W, o, fused_loss ? loss_out : nullptr, next_item + 1);
+    double *lo = fused_loss ? loss_out : nullptr;
+    if (W >= 32)  // long atom lists: 8 warps share a tile's bitmap words
+      gr_project1d_kernel<true, 8><<<(unsigned)items, 8 * 32, 0, stream>>>(
+          at, g, tc, bitmap, W, o, lo, next_item + 1);
+    else
+      gr_project1d_kernel<true, kProjWarps><<<(unsigned)items, kProjWarps * 32, 0, stream>>>(
+          at, g, tc, bitmap, W, o, lo, next_item + 1);
   } else if (form == 2) {
     launch_project3d<32, 34>(blocks, at, g, tc, bitmap, W, o, next_item, stream);
   } else {
@@ -748,7 +755,7 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   timer_mark(1, 1, stream);
   note_launches(1);
   if (loss_out && !fused_loss) {
-    gr_loss_finalize_kernel<<<1, 256, 0, stream>>>(loss_part, (int)items, loss_out);
+    gr_loss_finalize_kernel<<<1, kLossThreads, 0, stream>>>(loss_part, (int)items, loss_out);
     note_launches(1);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;

@@ -153,41 +153,50 @@ int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int 
 // ---------------------------------------------------------------------------
 // batched damped Newton step
 // ---------------------------------------------------------------------------
+// Cholesky solve on the packed lower triangle L (row i holds entries
+// i(i+1)/2 .. i(i+1)/2 + i), in place; every loop has a fixed trip count, so
+// L and b stay in registers.  Returns false when the block is not positive
+// definite (b is then unusable).
 template <int P>
-__device__ bool solve_spd_or_lu(double (&A)[P][P], double (&b)[P]) {
-  // Cholesky A = L L^T in place (lower triangle)
-  double L[P][P];
+__device__ __forceinline__ bool cholesky_solve_packed(double (&L)[P * (P + 1) / 2],
+                                                      double (&b)[P]) {
   bool spd = true;
-  for (int i = 0; i < P && spd; ++i) {
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+#pragma unroll
     for (int j = 0; j <= i; ++j) {
-      double s = A[i][j];
-      for (int k = 0; k < j; ++k) s -= L[i][k] * L[j][k];
+      double s = L[i * (i + 1) / 2 + j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) s -= L[i * (i + 1) / 2 + k] * L[j * (j + 1) / 2 + k];
       if (i == j) {
-        if (!(s > 0.0)) {
-          spd = false;
-          break;
-        }
-        L[i][i] = sqrt(s);
+        spd = spd && (s > 0.0);
+        L[i * (i + 1) / 2 + i] = sqrt(s > 0.0 ? s : 1.0);
       } else {
-        L[i][j] = s / L[j][j];
+        L[i * (i + 1) / 2 + j] = s / L[j * (j + 1) / 2 + j];
       }
     }
   }
-  if (spd) {
-    double y[P];
-    for (int i = 0; i < P; ++i) {
-      double s = b[i];
-      for (int k = 0; k < i; ++k) s -= L[i][k] * y[k];
-      y[i] = s / L[i][i];
-    }
-    for (int i = P - 1; i >= 0; --i) {
-      double s = y[i];
-      for (int k = i + 1; k < P; ++k) s -= L[k][i] * b[k];
-      b[i] = s / L[i][i];
-    }
-    return true;
+  double y[P];
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    double s = b[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) s -= L[i * (i + 1) / 2 + k] * y[k];
+    y[i] = s / L[i * (i + 1) / 2 + i];
   }
-  // partial-pivoting LU (Gaussian elimination)
+#pragma unroll
+  for (int i = P - 1; i >= 0; --i) {
+    double s = y[i];
+#pragma unroll
+    for (int k = i + 1; k < P; ++k) s -= L[k * (k + 1) / 2 + i] * b[k];
+    b[i] = s / L[i * (i + 1) / 2 + i];
+  }
+  return spd;
+}
+
+// partial-pivoting LU (Gaussian elimination) of a full block, in place
+template <int P>
+__device__ bool solve_lu(double (&A)[P][P], double (&b)[P]) {
   for (int c = 0; c < P; ++c) {
     int piv = c;
     double best = fabs(A[c][c]);
@@ -231,14 +240,31 @@ __global__ void gr_newton_solve_kernel(int n, int iso, const double *g, const do
                                        double *step_norm, int *fail, AtomOut ao) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  double A[P][P], b[P];
+  // Cholesky of the damped block (the common case) in registers; the full
+  // block is re-read for the LU fallback only when it is not positive definite
+  double L[P * (P + 1) / 2], b[P];
+  const double lj = lam[j];
+#pragma unroll
   for (int a = 0; a < P; ++a) {
     b[a] = -g[(size_t)j * P + a];
-    for (int c = 0; c < P; ++c) A[a][c] = H[((size_t)j * P + a) * P + c];
-    A[a][a] += lam[j];
+#pragma unroll
+    for (int c = 0; c <= a; ++c)
+      L[a * (a + 1) / 2 + c] = H[((size_t)j * P + a) * P + c] + (a == c ? lj : 0.0);
   }
   const bool active = mask == nullptr || mask[j] != 0;
-  bool ok = active && solve_spd_or_lu<P>(A, b);
+  bool ok = false;
+  if (active) {
+    ok = cholesky_solve_packed<P>(L, b);
+    if (!ok) {
+      double A[P][P];
+      for (int a = 0; a < P; ++a) {
+        b[a] = -g[(size_t)j * P + a];
+        for (int c = 0; c < P; ++c) A[a][c] = H[((size_t)j * P + a) * P + c];
+        A[a][a] += lj;
+      }
+      ok = solve_lu<P>(A, b);
+    }
+  }
   for (int a = 0; a < P; ++a)
     if (!(b[a] == b[a]) || fabs(b[a]) > 1e30) ok = false;
   double nrm = 0.0;
