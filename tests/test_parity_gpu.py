@@ -46,6 +46,21 @@ def test_forward_large_2d_matches_oracle(eng, cuda_ready):
     assert relerr(R, go.radproj(I, x, r, g)) < TOL
 
 
+def test_forward_and_kl_fit_many_2d_atoms(eng, cuda_ready):
+    """1100 atoms: tiles' atom lists span >= 32 bitmap words, so eight warps
+    share each 2D tile (the long-list form of the 2D projection)."""
+    g = make_geometry("2d", 24, 160)
+    I, x, r = make_atoms(2, 1100, 13, box=0.6)
+    geom, atoms = engine_geometry(g), engine_atoms(I, x, r)
+    Ro = go.radproj(I, x, r, g)
+    R = eng.radproj(atoms, geom).cpu().numpy()
+    assert relerr(R, Ro) < TOL
+    counts = np.random.default_rng(4).poisson(Ro + 1.0).astype(np.float64)
+    fw = eng.fit_forward(atoms, geom, torch.from_numpy(counts).float().cuda(), "kl", 1.0)
+    lo = go.kl_value(counts, Ro, 1.0)
+    assert abs(fw["loss"].item() - lo) <= TOL * abs(lo)
+
+
 @pytest.mark.parametrize("case", list(CASES))
 @pytest.mark.parametrize("order", [1, 2])
 def test_inner_derivs_match_oracle(eng, cuda_ready, case, order):
