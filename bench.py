@@ -177,14 +177,12 @@ def run_ours(args):
     # ---- device-resident timing (value) ------------------------------------
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    sampler = ClockSampler(local)
-    if ws > 1:
-        torch.distributed.barrier()
+    # (a) eager calls, with the library's kernel timers: per-call and
+    #     per-kernel times for the roofline
     torch.cuda.synchronize()
     l0 = engine.launch_count()
     engine.kernel_timer(engine.TIMER_PROJECT, True)
     engine.kernel_timer(engine.TIMER_DERIVS, True)
-    sampler.start()
     for i in range(args.steps):
         flush.zero_()                                   # evict L2 between steps
         e0, e1, e2 = ev[i]
@@ -195,15 +193,63 @@ def run_ours(args):
                            1.0 if fit == "l2" else 0.0, order)
         e2.record(stream)
     torch.cuda.synchronize()
-    clocks = sampler.stop()
-    launches = engine.launch_count() - l0
+    launches_per_step = (engine.launch_count() - l0) / args.steps
     kt_fwd, n_kf = engine.kernel_timer_read(engine.TIMER_PROJECT)
     kt_der, n_kd = engine.kernel_timer_read(engine.TIMER_DERIVS)
     engine.kernel_timer(engine.TIMER_PROJECT, False)
     engine.kernel_timer(engine.TIMER_DERIVS, False)
+    eager_ms = (sum(a.elapsed_time(b) for a, b, _ in ev)
+                + sum(b.elapsed_time(c) for _, b, c in ev)) / args.steps
+
+    # (b) the timed steps (value): the same step captured once as a CUDA
+    #     graph on preallocated buffers and replayed, L2 flushed between steps
+    f64 = dict(dtype=torch.float64, device=dev)
+    g_alpha = torch.empty(geom.shape, dtype=torch.float32, device=dev)
+    g_beta = torch.empty(geom.shape, dtype=torch.float32, device=dev) if fit == "kl" else None
+    g_loss = torch.zeros((), **f64)
+    g_f, g_g = torch.zeros(N, **f64), torch.zeros(N, P, **f64)
+    g_H = torch.zeros(N, P, P, **f64) if order == 2 else None
+    ws_p = torch.empty(max(256, engine.workspace_bytes(0, atoms, geom)), dtype=torch.uint8, device=dev)
+    ws_d = torch.empty(max(256, engine.workspace_bytes(order, atoms, geom)), dtype=torch.uint8,
+                       device=dev)
+    bc = 1.0 if fit == "l2" else 0.0
+
+    def graph_step():
+        engine.fit_forward_into(atoms, geom, data_d, fit, bg, None, g_alpha, g_beta, g_loss, ws_p)
+        engine.atom_derivs_into(atoms, geom, "field", g_alpha, g_beta, bc, order, g_f, g_g, g_H,
+                                ws_d)
+
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        graph_step()
+    torch.cuda.synchronize()
+    step_graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(step_graph, stream=side):
+        graph_step()
+    for _ in range(3):
+        step_graph.replay()
+    torch.cuda.synchronize()
+    gev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    for i in range(args.steps):
+        flush.zero_()                                   # evict L2 between steps
+        gev[i][0].record(stream)
+        step_graph.replay()
+        gev[i][1].record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    graph_ms = sum(a.elapsed_time(b) for a, b in gev)
+    assert float(g_loss) == float(fw["loss"]), "graph step differs from the eager step"
+    launches = int(round(launches_per_step * args.steps))
     t_fwd = [a.elapsed_time(b) for a, b, _ in ev]
     t_der = [b.elapsed_time(c) for _, b, c in ev]
-    total_ms = sum(t_fwd) + sum(t_der)
+    total_ms = graph_ms
     if ws > 1:
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -289,6 +335,9 @@ def run_ours(args):
                    "dense_pairs_per_pass": dense, "l2": "flushed between steps (256 MB write)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "dense_equiv_evals_per_s": dense * args.steps * ws / (total_ms * 1e-3),
+        "ms_per_step_eager": eager_ms,
+        "timing": "CUDA events around graph replays of the step (eager per-call and per-kernel "
+                  "times also given); L2 flushed between steps",
         "ms_forward": fwd_ms, "ms_derivatives": der_ms,
         "ms_kernel": {fwd_kernel: k_fwd, "gr_deriv_kernel": k_der},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
