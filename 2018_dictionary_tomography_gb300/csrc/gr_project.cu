@@ -78,10 +78,6 @@ __device__ __forceinline__ float kl_term(float f, float g) {
 // atom-index order, with no float atomics: results are bitwise reproducible.
 // Sums and compensations use a padded row stride S so that the cells of one
 // box row-block fall in different banks.  Tiles are ROWS x 32 cells.
-// Boxes up to this many columns are walked row by row (a lane keeps one
-// column); wider boxes are walked in flattened order.
-constexpr int kRowWalkMaxWidth = 10;
-
 template <int ROWS, int S>
 struct Proj3Smem {
   static constexpr int kAcc = ROWS * S;
@@ -197,33 +193,8 @@ __global__ void __launch_bounds__(kProjWarps * 32)
         if (lr0 > lr1) continue;  // warp-uniform
         const float4 qA = prm[sI * 3 + 0], qB = prm[sI * 3 + 1];
         const int bw = lc1 - lc0 + 1;
-        const float inv_bw = __frcp_rn((float)bw);
-        if (bw <= kRowWalkMaxWidth) {
-          // narrow box: lane -> (row offset r, column c) once per atom; the
-          // lane keeps its column's offset and steps down every rpi-th row
-          const int rpi = (int)((32.f + 0.5f) * inv_bw);   // rows per pass, exact
-          const int r = (int)(((float)lane + 0.5f) * inv_bw);
-          if (r < rpi) {
-            const int lc = lc0 + (lane - r * bw);
-            const float d1 = (pc1[lc] - qA.z) - qA.w;
-            const float gd1 = qB.y * d1, g2d1 = qB.z * d1 * d1;
-            for (int lr = lr0 + r; lr <= lr1; lr += rpi) {
-              const float d0 = (pc0[lr] - qA.x) - qA.y;
-              const float m = fmaf(d0, fmaf(qB.x, d0, gd1), g2d1);
-              if (m <= 1.f) {
-                const float v = qC.x * ex2_approx(fmaf(m, kNegThirtyLog2e, qB.w));
-                const int ci = lr * S + lc;
-                const float s0 = acc[ci];
-                const float tt = s0 + v;
-                cmp[ci] += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
-                acc[ci] = tt;
-              }
-            }
-          }
-          __syncwarp();
-          continue;
-        }
         const int ncell = (lr1 - lr0 + 1) * bw;
+        const float inv_bw = __frcp_rn((float)bw);
         for (int e = lane; e < ncell; e += 32) {
           // (e + 1/2) / bw is at least 1/(2 bw) from an integer, far more
           // than the rounding of the product: the row index is exact
