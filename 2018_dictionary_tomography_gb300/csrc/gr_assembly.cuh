@@ -170,63 +170,108 @@ __device__ __forceinline__ void psi_r_derivs(
   constexpr int D = K + 1;
   constexpr int PR = n_rparam<K>();
   constexpr int NG = K * (K + 1) / 2;
+  constexpr int NE = NG + K + 1;  // distinct Q entries: G entries, (m, T), (T, T)
   const float w = p.Q[K][K], iq = 1.f / w;
-  // dQ_cd / dr_p for the entries used: (i,j) detector pairs, (i,T), (T,T)
-  auto dQ = [&](int c, int d, int q) -> float {
-    const int a = rrow<K>(q), b = rcol<K>(q);
-    return basis<K>(f, c, b) * p.Kc[d][a] + basis<K>(f, d, b) * p.Kc[c][a];
-  };
-  auto ddQ = [&](int c, int d, int q, int s) -> float {
-    if (rrow<K>(q) != rrow<K>(s)) return 0.f;
-    const int b = rcol<K>(q), b2 = rcol<K>(s);
-    return basis<K>(f, c, b) * basis<K>(f, d, b2) + basis<K>(f, d, b) * basis<K>(f, c, b2);
-  };
-  float wp[PR];
-#pragma unroll
-  for (int q = 0; q < PR; ++q) {
-    wp[q] = dQ(K, K, q);
-    Jr[0][q] = -0.5f * wp[q] * iq;
-  }
-  // G params in order (0,0), (0,1), (1,1) for K = 2
-  int gi[NG], gj[NG];
+  // entry e = (ec, ed): the NG detector pairs in G order, then (m, T), (T, T)
+  int ec[NE], ed[NE];
   if constexpr (K == 1) {
-    gi[0] = 0; gj[0] = 0;
+    ec[0] = 0; ed[0] = 0;
+    ec[1] = 0; ed[1] = 1;
+    ec[2] = 1; ed[2] = 1;
   } else {
-    gi[0] = 0; gj[0] = 0;
-    gi[1] = 0; gj[1] = 1;
-    gi[2] = 1; gj[2] = 1;
+    ec[0] = 0; ed[0] = 0;
+    ec[1] = 0; ed[1] = 1;
+    ec[2] = 1; ed[2] = 1;
+    ec[3] = 0; ed[3] = 2;
+    ec[4] = 1; ed[4] = 2;
+    ec[5] = 2; ed[5] = 2;
   }
+  // DQ[e][q] = dQ_e / dr_q = B_c[b] K_d[a] + B_d[b] K_c[a], r_q = r_ab
+  float DQ[NE][PR];
 #pragma unroll
-  for (int k = 0; k < NG; ++k) {
-    const int i = gi[k], j = gj[k];
-    const float u = p.Q[i][K], v = p.Q[j][K];
+  for (int e = 0; e < NE; ++e)
 #pragma unroll
     for (int q = 0; q < PR; ++q) {
-      const float up = dQ(i, K, q), vp = dQ(j, K, q);
-      Jr[1 + k][q] = dQ(i, j, q) - (up * v + u * vp) * iq + u * v * wp[q] * iq * iq;
+      const int a = rrow<K>(q), b = rcol<K>(q);
+      DQ[e][q] = basis<K>(f, ec[e], b) * p.Kc[ed[e]][a] + basis<K>(f, ed[e], b) * p.Kc[ec[e]][a];
+    }
+  float uT[K];
+#pragma unroll
+  for (int m = 0; m < K; ++m) uT[m] = p.Q[m][K];
+  // first derivatives: psi_0 = ln n = -ln(Q_TT)/2, G_ij = Q_ij - Q_iT Q_jT / Q_TT
+#pragma unroll
+  for (int q = 0; q < PR; ++q) Jr[0][q] = -0.5f * DQ[NE - 1][q] * iq;
+#pragma unroll
+  for (int k = 0; k < NG; ++k) {
+    const int i = ec[k], j = ed[k];
+#pragma unroll
+    for (int q = 0; q < PR; ++q)
+      Jr[1 + k][q] = DQ[k][q] - (DQ[NG + i][q] * uT[j] + uT[i] * DQ[NG + j][q]) * iq +
+                     uT[i] * uT[j] * DQ[NE - 1][q] * iq * iq;
+  }
+  // Second derivatives of Psi = sum_k A_k psi_k through the entries of Q:
+  //   d2Psi/dr dr = DQ^T (d2Psi/dQ dQ) DQ + [same row of r] (B^T Abar B)
+  // with Abar = dPsi/dQ; d2Psi/dQ dQ is non-zero only among the (m, T) and
+  // (T, T) entries.
+  float Abar[NE], A2[K + 1][K + 1];
+  float sg = 0.f;  // sum_k A_k Q_iT Q_jT
+#pragma unroll
+  for (int k = 0; k < NG; ++k) {
+    Abar[k] = A[1 + k];
+    sg = fmaf(A[1 + k], uT[ec[k]] * uT[ed[k]], sg);
+  }
+#pragma unroll
+  for (int m = 0; m < K; ++m) {
+    float t = 0.f;  // sum_k A_k dG_k/dQ_mT * (-Q_TT)
+#pragma unroll
+    for (int k = 0; k < NG; ++k)
+      t += A[1 + k] * ((ec[k] == m ? uT[ed[k]] : 0.f) + (ed[k] == m ? uT[ec[k]] : 0.f));
+    Abar[NG + m] = -t * iq;
+    A2[m][K] = A2[K][m] = t * iq * iq;
+#pragma unroll
+    for (int n = 0; n < K; ++n) {
+      float t2 = 0.f;
+#pragma unroll
+      for (int k = 0; k < NG; ++k)
+        t2 += A[1 + k] * (((ec[k] == m && ed[k] == n) ? 1.f : 0.f) +
+                          ((ed[k] == m && ec[k] == n) ? 1.f : 0.f));
+      A2[m][n] = -t2 * iq;
     }
   }
+  Abar[NE - 1] = sg * iq * iq - 0.5f * A[0] * iq;
+  A2[K][K] = -2.f * sg * iq * iq * iq + 0.5f * A[0] * iq * iq;
+  // M = sum_e Abar_e (B_c B_d^T + B_d B_c^T)
+  float M[D][D];
+#pragma unroll
+  for (int b = 0; b < D; ++b)
+#pragma unroll
+    for (int b2 = 0; b2 < D; ++b2) {
+      float t = 0.f;
+#pragma unroll
+      for (int e = 0; e < NE; ++e)
+        t = fmaf(Abar[e], basis<K>(f, ec[e], b) * basis<K>(f, ed[e], b2) +
+                              basis<K>(f, ed[e], b) * basis<K>(f, ec[e], b2), t);
+      M[b][b2] = t;
+    }
+  // Y = (d2Psi/dQ_T dQ_T) DQ_T
+  float Y[K + 1][PR];
+#pragma unroll
+  for (int e = 0; e <= K; ++e)
+#pragma unroll
+    for (int s2 = 0; s2 < PR; ++s2) {
+      float t = 0.f;
+#pragma unroll
+      for (int e2 = 0; e2 <= K; ++e2) t = fmaf(A2[e][e2], DQ[NG + e2][s2], t);
+      Y[e][s2] = t;
+    }
   int o = 0;
 #pragma unroll
   for (int q = 0; q < PR; ++q)
 #pragma unroll
-    for (int s = q; s < PR; ++s, ++o) {
-      const float wpq = ddQ(K, K, q, s);
-      float h = A[0] * (-0.5f) * (wpq * iq - wp[q] * wp[s] * iq * iq);
+    for (int s2 = q; s2 < PR; ++s2, ++o) {
+      float h = (rrow<K>(q) == rrow<K>(s2)) ? M[rcol<K>(q)][rcol<K>(s2)] : 0.f;
 #pragma unroll
-      for (int k = 0; k < NG; ++k) {
-        const int i = gi[k], j = gj[k];
-        const float u = p.Q[i][K], v = p.Q[j][K];
-        const float up = dQ(i, K, q), us = dQ(i, K, s);
-        const float vp = dQ(j, K, q), vs = dQ(j, K, s);
-        const float ups = ddQ(i, K, q, s), vps = ddQ(j, K, q, s);
-        const float fqs = (ups * v + up * vs + us * vp + u * vps) * iq -
-                          (up * v + u * vp) * wp[s] * iq * iq -
-                          (us * v + u * vs) * wp[q] * iq * iq -
-                          u * v * wpq * iq * iq +
-                          2.f * u * v * wp[q] * wp[s] * iq * iq * iq;
-        h += A[1 + k] * (ddQ(i, j, q, s) - fqs);
-      }
+      for (int e = 0; e <= K; ++e) h = fmaf(DQ[NG + e][q], Y[e][s2], h);
       Hr[o] = h;
     }
 }
