@@ -115,101 +115,121 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
     det = p.G[0] * p.G[2] - p.G[1] * p.G[1];
     iG2 = 1.f / p.G[2];
   }
-  for (int k0 = p.lo[0]; k0 <= p.hi[0]; ++k0) {
-    const float d0 = (__ldg(g.ax[0].coords + k0) - p.qh[0]) - p.ql[0];
-    if constexpr (K == 1) {
-      const float m = p.G[0] * d0 * d0;
-      if (m <= 1.f) {
-        const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
-        const float c = __ldg(field + abase + k0);
-        const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
-        float w = al * E;
+  if constexpr (K == 1) {
+    // the detector row is walked in chunks of kRowChunk cells whose field
+    // values and coordinates are loaded together first (one cell per load
+    // round trip would leave the lane waiting on every cell)
+    const int c_hi = p.hi[0];
+    for (int kb = p.lo[0]; kb <= c_hi; kb += kRowChunk) {
+      float cv[kRowChunk], pv[kRowChunk], bv[GN ? kRowChunk : 1];
 #pragma unroll
-        for (int q = 0; q < NM; ++q) {
-          mo.Ma[q] += w;
-          w *= d0;
-        }
-        if (GN) {
-          const float be = bfield ? __ldg(bfield + abase + k0) : in.beta_const;
-          float wb = be * E * E;
+      for (int i = 0; i < kRowChunk; ++i) {
+        const int k0 = min(kb + i, c_hi);
+        cv[i] = __ldg(field + abase + k0);
+        pv[i] = __ldg(g.ax[0].coords + k0);
+        if (GN) bv[i] = bfield ? __ldg(bfield + abase + k0) : in.beta_const;
+      }
+#pragma unroll
+      for (int i = 0; i < kRowChunk; ++i) {
+        if (kb + i > c_hi) break;
+        const float d0 = (pv[i] - p.qh[0]) - p.ql[0];
+        const float m = p.G[0] * d0 * d0;
+        if (m <= 1.f) {
+          const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
+          const float c = cv[i];
+          const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
+          float w = al * E;
 #pragma unroll
           for (int q = 0; q < NM; ++q) {
-            mo.Mb[q] += wb;
-            wb *= d0;
+            mo.Ma[q] += w;
+            w *= d0;
+          }
+          if (GN) {
+            float wb = bv[i] * E * E;
+#pragma unroll
+            for (int q = 0; q < NM; ++q) {
+              mo.Mb[q] += wb;
+              wb *= d0;
+            }
+          }
+          if (in.mode == kModeL2Atom) {
+            mo.X0 = fmaf(E, c, mo.X0);
+            mo.Y0 = fmaf(E, E, mo.Y0);
           }
         }
-        if (in.mode == kModeL2Atom) {
-          mo.X0 = fmaf(E, c, mo.X0);
-          mo.Y0 = fmaf(E, E, mo.Y0);
-        }
       }
-    } else {
-      const float t0 = p.G[0] * d0 * d0;
-      const float u = 2.f * p.G[1] * d0;
-      float Sa[DEG + 1], Sb[GN ? DEG + 1 : 1];
+    }
+  } else {
+    for (int k0 = p.lo[0]; k0 <= p.hi[0]; ++k0) {
+      const float d0 = (__ldg(g.ax[0].coords + k0) - p.qh[0]) - p.ql[0];
+      {
+        const float t0 = p.G[0] * d0 * d0;
+        const float u = 2.f * p.G[1] * d0;
+        float Sa[DEG + 1], Sb[GN ? DEG + 1 : 1];
 #pragma unroll
-      for (int q = 0; q <= DEG; ++q) {
-        Sa[q] = 0.f;
-        if (GN) Sb[q] = 0.f;
-      }
-      const size_t rbase = abase + (size_t)k0 * D1;
-      const float rem = fmaf(-d0 * d0, det, p.G[2]);
-      const float rc = (p.qh[1] - p.G[1] * d0 * iG2 - g.ax[1].first) * g.ax[1].inv_step;
-      const float rh = sqrtf(fmaxf(rem, 0.f)) * iG2 * g.ax[1].inv_step * 1.0001f + 1e-3f;
-      const float rlo = ceilf(rc - rh), rhi = floorf(rc + rh);
-      const int c_lo = (int)fminf(fmaxf(rlo, (float)p.lo[1]), (float)p.hi[1] + 1.f);
-      const int c_hi = (int)fmaxf(fminf(rhi, (float)p.hi[1]), (float)p.lo[1] - 1.f);
-      // the row is walked in chunks of kRowChunk cells whose field values
-      // and coordinates are loaded together first, so the loads overlap
-      // instead of each cell waiting for its own
-      for (int kb = c_lo; kb <= c_hi; kb += kRowChunk) {
-        float cv[kRowChunk], pv[kRowChunk], bv[GN ? kRowChunk : 1];
-#pragma unroll
-        for (int i = 0; i < kRowChunk; ++i) {
-          const int k1 = min(kb + i, c_hi);
-          cv[i] = __ldg(field + rbase + k1);
-          pv[i] = __ldg(g.ax[1].coords + k1);
-          if (GN) bv[i] = bfield ? __ldg(bfield + rbase + k1) : in.beta_const;
+        for (int q = 0; q <= DEG; ++q) {
+          Sa[q] = 0.f;
+          if (GN) Sb[q] = 0.f;
         }
+        const size_t rbase = abase + (size_t)k0 * D1;
+        const float rem = fmaf(-d0 * d0, det, p.G[2]);
+        const float rc = (p.qh[1] - p.G[1] * d0 * iG2 - g.ax[1].first) * g.ax[1].inv_step;
+        const float rh = sqrtf(fmaxf(rem, 0.f)) * iG2 * g.ax[1].inv_step * 1.0001f + 1e-3f;
+        const float rlo = ceilf(rc - rh), rhi = floorf(rc + rh);
+        const int c_lo = (int)fminf(fmaxf(rlo, (float)p.lo[1]), (float)p.hi[1] + 1.f);
+        const int c_hi = (int)fmaxf(fminf(rhi, (float)p.hi[1]), (float)p.lo[1] - 1.f);
+        // the row is walked in chunks of kRowChunk cells whose field values
+        // and coordinates are loaded together first, so the loads overlap
+        // instead of each cell waiting for its own
+        for (int kb = c_lo; kb <= c_hi; kb += kRowChunk) {
+          float cv[kRowChunk], pv[kRowChunk], bv[GN ? kRowChunk : 1];
 #pragma unroll
-        for (int i = 0; i < kRowChunk; ++i) {
-          if (kb + i > c_hi) break;
-          const float d1 = (pv[i] - p.qh[1]) - p.ql[1];
-          const float m = fmaf(d1, fmaf(p.G[2], d1, u), t0);
-          if (m <= 1.f) {
-            const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
-            const float c = cv[i];
-            const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
-            float w = al * E;
+          for (int i = 0; i < kRowChunk; ++i) {
+            const int k1 = min(kb + i, c_hi);
+            cv[i] = __ldg(field + rbase + k1);
+            pv[i] = __ldg(g.ax[1].coords + k1);
+            if (GN) bv[i] = bfield ? __ldg(bfield + rbase + k1) : in.beta_const;
+          }
 #pragma unroll
-            for (int q = 0; q <= DEG; ++q) {
-              Sa[q] += w;
-              w *= d1;
-            }
-            if (GN) {
-              float wb = bv[i] * E * E;
+          for (int i = 0; i < kRowChunk; ++i) {
+            if (kb + i > c_hi) break;
+            const float d1 = (pv[i] - p.qh[1]) - p.ql[1];
+            const float m = fmaf(d1, fmaf(p.G[2], d1, u), t0);
+            if (m <= 1.f) {
+              const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
+              const float c = cv[i];
+              const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
+              float w = al * E;
 #pragma unroll
               for (int q = 0; q <= DEG; ++q) {
-                Sb[q] += wb;
-                wb *= d1;
+                Sa[q] += w;
+                w *= d1;
               }
-            }
-            if (in.mode == kModeL2Atom) {
-              mo.X0 = fmaf(E, c, mo.X0);
-              mo.Y0 = fmaf(E, E, mo.Y0);
+              if (GN) {
+                float wb = bv[i] * E * E;
+#pragma unroll
+                for (int q = 0; q <= DEG; ++q) {
+                  Sb[q] += wb;
+                  wb *= d1;
+                }
+              }
+              if (in.mode == kModeL2Atom) {
+                mo.X0 = fmaf(E, c, mo.X0);
+                mo.Y0 = fmaf(E, E, mo.Y0);
+              }
             }
           }
         }
-      }
-      float pw = 1.f;
+        float pw = 1.f;
 #pragma unroll
-      for (int i = 0; i <= DEG; ++i) {
+        for (int i = 0; i <= DEG; ++i) {
 #pragma unroll
-        for (int j = 0; j <= DEG - i; ++j) {
-          mo.Ma[mi(i, j)] = fmaf(pw, Sa[j], mo.Ma[mi(i, j)]);
-          if (GN) mo.Mb[mi(i, j)] = fmaf(pw, Sb[j], mo.Mb[mi(i, j)]);
+          for (int j = 0; j <= DEG - i; ++j) {
+            mo.Ma[mi(i, j)] = fmaf(pw, Sa[j], mo.Ma[mi(i, j)]);
+            if (GN) mo.Mb[mi(i, j)] = fmaf(pw, Sb[j], mo.Mb[mi(i, j)]);
+          }
+          pw *= d0;
         }
-        pw *= d0;
       }
     }
   }

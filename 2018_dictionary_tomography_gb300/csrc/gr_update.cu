@@ -14,7 +14,7 @@
 // 2. gr_newton_solve_kernel -- batched damped Newton step for every atom:
 //    (H_j + lambda_j 1) dtheta = -g_j in FP64 (Cholesky; partial-pivoting LU
 //    when the damped block is not positive definite, like numpy.linalg.solve
-//    in NewtonGaussian.py:74), then the reference's parameter update with its
+//    in NewtonGaussian.py:74), one group of lanes per atom, then the reference's parameter update with its
 //    clamps: I >= 0, and sign flips keeping diag(r) >= 0 (GD_lib.py:504-522).
 #include "gr_kernels.cuh"
 
@@ -153,172 +153,223 @@ int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int 
 // ---------------------------------------------------------------------------
 // batched damped Newton step
 // ---------------------------------------------------------------------------
-// Cholesky solve on the packed lower triangle L (row i holds entries
-// i(i+1)/2 .. i(i+1)/2 + i), in place; every loop has a fixed trip count, so
-// L and b stay in registers.  Returns false when the block is not positive
-// definite (b is then unusable).
-template <int P>
-__device__ __forceinline__ bool cholesky_solve_packed(double (&L)[P * (P + 1) / 2],
-                                                      double (&b)[P]) {
+// FP64 arithmetic is a narrow pipe on this GPU, so a P x P factorisation run
+// by one thread is one long chain of dependent FP64 operations (about a
+// thousand for P = 10, divisions and square roots included) and its latency,
+// not its work, sets the kernel time.  Here a group of G lanes (G a power of
+// two >= P) shares one atom: lane l holds row l of the damped block in
+// registers, columns are broadcast with shuffles, and each column costs one
+// reciprocal square root (Cholesky) or one reciprocal (LU), after which the
+// lanes update their rows independently.  The dependent chain per column is
+// a broadcast, the reciprocal and two multiply-adds.
+//
+// Every lane of a warp executes every shuffle (no lane leaves early), so a
+// group whose atom is out of range or masked runs on an identity block and
+// stores nothing.
+
+// Right-looking Cholesky H = L L^T on the group, then L y = b, L^T x = y.
+// Lane l: a[] row l of the block (overwritten by row l of L), b = rhs[l].
+// Returns (identically on all lanes of the group) whether every pivot was
+// positive; x[] receives the solution on every lane.
+template <int P, int G>
+__device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l,
+                                               double (&x)[P]) {
+  constexpr unsigned kAll = 0xffffffffu;
+  double inv[P], col[P];
   bool spd = true;
 #pragma unroll
-  for (int i = 0; i < P; ++i) {
+  for (int k = 0; k < P; ++k) col[k] = 0.0;
 #pragma unroll
-    for (int j = 0; j <= i; ++j) {
-      double s = L[i * (i + 1) / 2 + j];
+  for (int j = 0; j < P; ++j) {
+    const double piv = __shfl_sync(kAll, a[j], j, G);
+    spd = spd && (piv > 0.0);
+    const double ij = rsqrt(piv > 0.0 ? piv : 1.0);
+    inv[j] = ij;
+    const double lij = (l == j) ? piv * ij : a[j] * ij;   // L[l][j] for l >= j
+    a[j] = lij;
 #pragma unroll
-      for (int k = 0; k < j; ++k) s -= L[i * (i + 1) / 2 + k] * L[j * (j + 1) / 2 + k];
-      if (i == j) {
-        spd = spd && (s > 0.0);
-        L[i * (i + 1) / 2 + i] = sqrt(s > 0.0 ? s : 1.0);
-      } else {
-        L[i * (i + 1) / 2 + j] = s / L[j * (j + 1) / 2 + j];
-      }
+    for (int k = j + 1; k < P; ++k) {
+      const double lkj = __shfl_sync(kAll, lij, k, G);
+      if (l == j) col[k] = lkj;         // lane j keeps column j of L
+      a[k] = fma(-lij, lkj, a[k]);      // trailing rows (only k <= l is used)
     }
   }
+  // forward: y_j = (b_j - sum_{k<j} L[j][k] y_k) / L[j][j]; lane l folds
+  // each y_j into its own b as soon as it is known
   double y[P];
 #pragma unroll
-  for (int i = 0; i < P; ++i) {
-    double s = b[i];
-#pragma unroll
-    for (int k = 0; k < i; ++k) s -= L[i * (i + 1) / 2 + k] * y[k];
-    y[i] = s / L[i * (i + 1) / 2 + i];
+  for (int j = 0; j < P; ++j) {
+    y[j] = __shfl_sync(kAll, b, j, G) * inv[j];
+    b = fma(-a[j], y[j], b);
   }
+  // backward: x_i = (y_i - sum_{k>i} L[k][i] x_k) / L[i][i]; lane i holds
+  // column i of L below the diagonal in col[]
+  double acc = 0.0;
 #pragma unroll
-  for (int i = P - 1; i >= 0; --i) {
-    double s = y[i];
-#pragma unroll
-    for (int k = i + 1; k < P; ++k) s -= L[k * (k + 1) / 2 + i] * b[k];
-    b[i] = s / L[i * (i + 1) / 2 + i];
+  for (int k = P - 1; k >= 0; --k) {
+    const double v = (y[k] - acc) * inv[k];
+    x[k] = __shfl_sync(kAll, v, k, G);
+    acc = fma(col[k], x[k], acc);
   }
   return spd;
 }
 
-// partial-pivoting LU (Gaussian elimination) of a full block, in place
-template <int P>
-__device__ bool solve_lu(double (&A)[P][P], double (&b)[P]) {
+// Partial-pivoting LU (Gaussian elimination, as numpy.linalg.solve's LAPACK
+// getrf/getrs) on the group, without moving rows: the pivot of column c is
+// the largest |a[c]| among the rows not yet used as pivots (ties to the
+// lower row), its row is broadcast and every other unused row eliminates
+// column c with the multiplier a[c] * (1 / pivot).  Returns false for a
+// zero pivot column.
+template <int P, int G>
+__device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, double (&x)[P]) {
+  constexpr unsigned kAll = 0xffffffffu;
+  bool used = l >= P;                   // padding lanes never pivot
+  bool ok = true;
+  int prow[P];
+  double pinv[P];
+#pragma unroll
   for (int c = 0; c < P; ++c) {
-    int piv = c;
-    double best = fabs(A[c][c]);
-    for (int i = c + 1; i < P; ++i)
-      if (fabs(A[i][c]) > best) {
-        best = fabs(A[i][c]);
-        piv = i;
+    double v = used ? -1.0 : fabs(a[c]);
+    int idx = l;
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+      const double ov = __shfl_xor_sync(kAll, v, off, G);
+      const int oi = __shfl_xor_sync(kAll, idx, off, G);
+      if (ov > v || (ov == v && oi < idx)) {
+        v = ov;
+        idx = oi;
       }
-    if (best == 0.0) return false;
-    if (piv != c) {
-      for (int k = 0; k < P; ++k) {
-        double t = A[c][k];
-        A[c][k] = A[piv][k];
-        A[piv][k] = t;
-      }
-      double t = b[c];
-      b[c] = b[piv];
-      b[piv] = t;
     }
-    for (int i = c + 1; i < P; ++i) {
-      const double m = A[i][c] / A[c][c];
-      for (int k = c; k < P; ++k) A[i][k] -= m * A[c][k];
-      b[i] -= m * b[c];
+    ok = ok && (v > 0.0);
+    const double piv = __shfl_sync(kAll, a[c], idx, G);
+    const double pi = 1.0 / (piv != 0.0 ? piv : 1.0);
+    prow[c] = idx;
+    pinv[c] = pi;
+    const bool elim = !used && l != idx;
+    const double m = a[c] * pi;
+#pragma unroll
+    for (int k = c + 1; k < P; ++k) {
+      const double pk = __shfl_sync(kAll, a[k], idx, G);
+      if (elim) a[k] = fma(-m, pk, a[k]);
     }
+    const double pb = __shfl_sync(kAll, b, idx, G);
+    if (elim) b = fma(-m, pb, b);
+    used = used || l == idx;
   }
-  for (int i = P - 1; i >= 0; --i) {
-    double s = b[i];
-    for (int k = i + 1; k < P; ++k) s -= A[i][k] * b[k];
-    b[i] = s / A[i][i];
+  // back substitution in pivot order: row prow[c] holds U[c][c..P-1]; every
+  // lane folds each x_k into its rhs as soon as it is known
+#pragma unroll
+  for (int c = P - 1; c >= 0; --c) {
+    x[c] = __shfl_sync(kAll, b * pinv[c], prow[c], G);
+    b = fma(-a[c], x[c], b);
   }
-  return true;
+  return ok;
 }
 
 // theta (N, P) float64 in the derivative order [I, x, r]; writes theta_new
 // and |dtheta|.  lam (N) adds lam_j to the diagonal.  mask (nullable): atoms
-// with mask[j] == 0 keep their parameters.
-template <int P, int D>
-__global__ void gr_newton_solve_kernel(int n, int iso, const double *g, const double *H,
-                                       const double *lam, const double *theta,
-                                       const unsigned char *mask, double *theta_new,
-                                       double *step_norm, int *fail, AtomOut ao) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  // Cholesky of the damped block (the common case) in registers; the full
-  // block is re-read for the LU fallback only when it is not positive definite
-  double L[P * (P + 1) / 2], b[P];
-  const double lj = lam[j];
+// with mask[j] == 0 keep their parameters.  One group of G lanes per atom.
+template <int P, int D, int G>
+__global__ void __launch_bounds__(128)
+    gr_newton_solve_kernel(int n, const double *g, const double *H,
+                           const double *lam, const double *theta,
+                           const unsigned char *mask, double *theta_new,
+                           double *step_norm, int *fail, AtomOut ao) {
+  constexpr unsigned kAll = 0xffffffffu;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((t & ~31) / G >= n) return;       // whole warp past the last atom
+  const int l = t & (G - 1);
+  const int j = t / G;
+  const bool live = j < n;
+  const bool active = live && (mask == nullptr || mask[j] != 0);
+  const bool row = live && l < P;
+  double a[P], b = 0.0, x[P];
+  double lj = row ? lam[j] : 0.0;
+  auto load = [&]() {
 #pragma unroll
-  for (int a = 0; a < P; ++a) {
-    b[a] = -g[(size_t)j * P + a];
+    for (int k = 0; k < P; ++k)
+      a[k] = row ? H[((size_t)j * P + l) * P + k] + (k == l ? lj : 0.0) : (k == l ? 1.0 : 0.0);
+    b = row ? -g[(size_t)j * P + l] : 0.0;
+  };
+  load();
+  bool ok = group_cholesky<P, G>(a, b, l, x);
+  if (__any_sync(kAll, !ok)) {          // some group of this warp is not positive definite
+    const bool chol_ok = ok;
+    load();
+    double xl[P];
+    const bool lu_ok = group_lu<P, G>(a, b, l, xl);
+    if (!chol_ok) {
+      ok = lu_ok;
 #pragma unroll
-    for (int c = 0; c <= a; ++c)
-      L[a * (a + 1) / 2 + c] = H[((size_t)j * P + a) * P + c] + (a == c ? lj : 0.0);
-  }
-  const bool active = mask == nullptr || mask[j] != 0;
-  bool ok = false;
-  if (active) {
-    ok = cholesky_solve_packed<P>(L, b);
-    if (!ok) {
-      double A[P][P];
-      for (int a = 0; a < P; ++a) {
-        b[a] = -g[(size_t)j * P + a];
-        for (int c = 0; c < P; ++c) A[a][c] = H[((size_t)j * P + a) * P + c];
-        A[a][a] += lj;
-      }
-      ok = solve_lu<P>(A, b);
+      for (int k = 0; k < P; ++k) x[k] = xl[k];
     }
   }
-  for (int a = 0; a < P; ++a)
-    if (!(b[a] == b[a]) || fabs(b[a]) > 1e30) ok = false;
-  double nrm = 0.0;
-  double t[P];
-  for (int a = 0; a < P; ++a) {
-    const double d = ok ? b[a] : 0.0;
-    nrm += d * d;
-    t[a] = theta[(size_t)j * P + a] + d;
+  ok = ok && active;
+#pragma unroll
+  for (int k = 0; k < P; ++k)
+    if (!(x[k] == x[k]) || fabs(x[k]) > 1e30) ok = false;
+  double nrm = 0.0, th[P];
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    const double d = ok ? x[k] : 0.0;
+    nrm = fma(d, d, nrm);
+    th[k] = live ? theta[(size_t)j * P + k] : 0.0;
+    th[k] += d;
   }
   if (ok) {
-    t[0] = t[0] < 0.0 ? 0.0 : t[0];
-    if (iso) {
-      t[1 + D] = fabs(t[1 + D]);
-    } else if (D == 2) {
-      double *r = t + 1 + D;
+    th[0] = th[0] < 0.0 ? 0.0 : th[0];
+    // sign flips keeping diag(r) >= 0; P fixes the kind: 4 / 5 isotropic
+    // 2D / 3D, 6 anisotropic 2D, 10 anisotropic 3D
+    double *r = th + 1 + D;
+    if constexpr (P == 4 || P == 5) {
+      r[0] = fabs(r[0]);
+    } else if constexpr (P == 6) {
       if (r[0] < 0) { r[0] = -r[0]; r[2] = -r[2]; }
       if (r[1] < 0) r[1] = -r[1];
     } else {
-      double *r = t + 1 + D;
       if (r[0] < 0) { r[0] = -r[0]; r[3] = -r[3]; r[5] = -r[5]; }
       if (r[1] < 0) { r[1] = -r[1]; r[4] = -r[4]; }
       if (r[2] < 0) r[2] = -r[2];
     }
-  } else {
-    for (int a = 0; a < P; ++a) t[a] = theta[(size_t)j * P + a];
   }
-  for (int a = 0; a < P; ++a) theta_new[(size_t)j * P + a] = t[a];
-  step_norm[j] = sqrt(nrm);
-  if (fail) fail[j] = (active && !ok) ? 1 : 0;
+  if (!row) return;
+  double mine = 0.0;
+#pragma unroll
+  for (int k = 0; k < P; ++k)
+    if (k == l) mine = th[k];
+  theta_new[(size_t)j * P + l] = mine;
+  if (l == 0) {
+    step_norm[j] = sqrt(nrm);
+    if (fail) fail[j] = (active && !ok) ? 1 : 0;
+  }
   if (ao.I) {
     constexpr int PR = P - 1 - D;
-    ao.I[j] = (float)t[0];
-    for (int c = 0; c < D; ++c) ao.x[(size_t)j * D + c] = (float)t[1 + c];
-    for (int q = 0; q < PR; ++q) ao.r[(size_t)j * PR + q] = (float)t[1 + D + q];
+    if (l == 0) ao.I[j] = (float)mine;
+    else if (l <= D) ao.x[(size_t)j * D + l - 1] = (float)mine;
+    else ao.r[(size_t)j * PR + l - 1 - D] = (float)mine;
   }
 }
 
 // Device-side accept/reject of a batched Newton trial (no host round trip):
-// one block; if loss_trial <= loss_cur the trial parameters (FP64 and the
-// float32 atom arrays) become current, loss_cur takes the trial loss and the
-// damping halves, else the damping grows tenfold (both clamped).  Appends
-// (loss_cur, accepted) to the history.
-__global__ void gr_newton_accept_kernel(int n, int P, int pr, int dim,
-                                        double *loss_cur, const double *loss_trial,
-                                        double *theta, const double *theta_trial,
-                                        double *lam, double lam_min, double lam_max,
-                                        AtomOut cur, AtomIn trial, double *hist,
-                                        int *hist_acc, int *counter, int hist_len) {
-  __shared__ int acc;
-  if (threadIdx.x == 0) acc = (*loss_trial <= *loss_cur) ? 1 : 0;
-  __syncthreads();
-  for (int e = threadIdx.x; e < n * P; e += blockDim.x)
-    if (acc) theta[e] = theta_trial[e];
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+// if loss_trial <= loss_cur the trial parameters (FP64 and the float32 atom
+// arrays) become current, loss_cur takes the trial loss and the damping
+// halves, else the damping grows tenfold (both clamped).  Appends
+// (loss_cur, accepted) to the history.  Blocks stride over the atoms; each
+// takes the decision itself.  Block 0 writes loss_cur last, and the decision
+// does not change when another block reads loss_cur after that write (an
+// accepted trial then compares equal; a rejected one leaves it untouched).
+__global__ void __launch_bounds__(256)
+    gr_newton_accept_kernel(int n, int P, int pr, int dim, double *loss_cur,
+                            const double *loss_trial, double *theta,
+                            const double *theta_trial, double *lam, double lam_min,
+                            double lam_max, AtomOut cur, AtomIn trial, double *hist,
+                            int *hist_acc, int *counter, int hist_len) {
+  const bool acc = *loss_trial <= *loss_cur;
+  const int stride = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (acc)
+    for (int e = t0; e < n * P; e += stride) theta[e] = theta_trial[e];
+  for (int j = t0; j < n; j += stride) {
     double l = acc ? lam[j] * 0.5 : lam[j] * 10.0;
     lam[j] = l < lam_min ? lam_min : (l > lam_max ? lam_max : l);
     if (acc) {
@@ -327,13 +378,12 @@ __global__ void gr_newton_accept_kernel(int n, int P, int pr, int dim,
       for (int q = 0; q < pr; ++q) cur.r[(size_t)j * pr + q] = trial.r[(size_t)j * pr + q];
     }
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  if (t0 == 0) {
     if (acc) *loss_cur = *loss_trial;
     const int k = *counter;
     if (k < hist_len) {
       hist[k] = *loss_cur;
-      hist_acc[k] = acc;
+      hist_acc[k] = acc ? 1 : 0;
     }
     *counter = k + 1;
   }
@@ -373,7 +423,9 @@ int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
                          const double *theta_trial, double *lam, double lam_min,
                          double lam_max, AtomOut cur, AtomIn trial, double *hist,
                          int *hist_acc, int *counter, int hist_len, cudaStream_t stream) {
-  gr_newton_accept_kernel<<<1, 256, 0, stream>>>(n, P, pr, dim, loss_cur, loss_trial, theta,
+  int blocks = (n * P + 255) / 256;
+  blocks = blocks < 1 ? 1 : (blocks > 152 * 4 ? 152 * 4 : blocks);
+  gr_newton_accept_kernel<<<blocks, 256, 0, stream>>>(n, P, pr, dim, loss_cur, loss_trial, theta,
                                                  theta_trial, lam, lam_min, lam_max, cur,
                                                  trial, hist, hist_acc, counter, hist_len);
   note_launches(1);
@@ -385,15 +437,15 @@ int launch_newton_solve(int dim, int iso, int n, const double *g, const double *
                         const unsigned char *mask, double *theta_new,
                         double *step_norm, int *fail, AtomOut ao, cudaStream_t stream) {
   if (n <= 0) return kOk;
-  const int blocks = (n + 63) / 64;
+  auto blocks = [n](int G) { return (unsigned)(((size_t)n * G + 127) / 128); };
   if (dim == 2 && iso)
-    gr_newton_solve_kernel<4, 2><<<blocks, 64, 0, stream>>>(n, 1, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<4, 2, 8><<<blocks(8), 128, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else if (dim == 2)
-    gr_newton_solve_kernel<6, 2><<<blocks, 64, 0, stream>>>(n, 0, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<6, 2, 8><<<blocks(8), 128, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else if (iso)
-    gr_newton_solve_kernel<5, 3><<<blocks, 64, 0, stream>>>(n, 1, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<5, 3, 8><<<blocks(8), 128, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else
-    gr_newton_solve_kernel<10, 3><<<blocks, 64, 0, stream>>>(n, 0, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<10, 3, 16><<<blocks(16), 128, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
