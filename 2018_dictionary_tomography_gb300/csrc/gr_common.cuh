@@ -403,4 +403,31 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
+// One warp sums n FP64 partials (written by other blocks before a
+// __threadfence) in a fixed order and writes the total to *out.  A dependent
+// FP64 add takes about 64 cycles on this GPU, so lane l keeps kSums running
+// sums -- element i goes to sum (i / 32) % kSums of lane i % 32 -- and the
+// dependent chain is n / (32 kSums) adds instead of n / 32; the sums are
+// then combined pairwise and across the warp, always in the same order.
+__device__ __forceinline__ void sum_partials_warp(const double *part, int n, double *out,
+                                                  int lane) {
+  constexpr int kSums = 8;
+  double s[kSums];
+#pragma unroll
+  for (int k = 0; k < kSums; ++k) s[k] = 0.0;
+  for (int base = 0; base < n; base += 32 * kSums) {
+#pragma unroll
+    for (int k = 0; k < kSums; ++k) {
+      const int i = base + 32 * k + lane;
+      if (i < n) s[k] += __ldcg(part + i);
+    }
+  }
+#pragma unroll
+  for (int w = 1; w < kSums; w <<= 1)
+#pragma unroll
+    for (int k = 0; k < kSums; k += 2 * w) s[k] += s[k + w];
+  const double t = warp_sum_d(s[0]);
+  if (lane == 0) *out = t;
+}
+
 }  // namespace gr

@@ -619,12 +619,17 @@ int set_tuning(int key, int value) {
     g_proj_form = value;
     return kOk;
   }
+  if (key == 4 && value >= 0) {
+    g_proj_split_cells = value;
+    return kOk;
+  }
   return kErrArg;
 }
 
 int get_tuning(int key) {
   return key == 0 ? g_deriv_target_warps : key == 1 ? g_deriv_min_angles
-         : key == 2 ? g_deriv_atoms_per_warp : key == 3 ? g_proj_form : -1;
+         : key == 2 ? g_deriv_atoms_per_warp : key == 3 ? g_proj_form
+         : key == 4 ? g_proj_split_cells : -1;
 }
 
 size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order) {

@@ -66,6 +66,7 @@ inline size_t align_up(size_t b) { return (b + 255) & ~(size_t)255; }
 
 TileCfg make_tiles(int K, int D0, int D1, int rows);
 extern int g_proj_form;
+extern int g_proj_split_cells;
 size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1);
 int launch_project(const Atoms &at, const Geom &g, const ProjOut &o,
                    double *loss_out, void *ws, size_t ws_bytes,

@@ -85,14 +85,27 @@ struct Proj3Smem {
   static constexpr int kFloats = 2 * kAcc + 32 * 12 + ROWS + 32 + kRing;
 };
 
-template <int ROWS, int S>
+// NW = 1: persistent warps, each (angle, tile) item walked by one warp.
+// NW = kProjWarps: persistent blocks, each item walked by the whole block,
+// warp w taking the atoms of bitmap words [w wq, (w + 1) wq), wq = ceil(W/NW),
+// into its own cell sums; the block then combines the warps' sums per cell
+// in warp order (compensated).  The word ranges depend on W only, so every
+// tiling still gives the same cell sums.  Used when a problem has too few
+// items to keep the SMs busy: the slowest item, not the total, then sets
+// the kernel time, and splitting its atom list cuts that item's latency.
+// With loss_out, the last block (or warp) to finish sums the items' loss
+// partials in item order (no separate finalize launch).
+template <int ROWS, int S, int NW>
 __global__ void __launch_bounds__(kProjWarps * 32)
     gr_project3d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap, int W,
-                        ProjOut out, int *next_item) {
+                        ProjOut out, int *next_item, double *loss_out) {
+  static_assert(NW == 1 || NW == kProjWarps, "a split item takes the whole block");
   using L = Proj3Smem<ROWS, S>;
   constexpr int kRing = L::kRing;
   static_assert((kRing & (kRing - 1)) == 0 && kRing >= 64, "ring");
   extern __shared__ float smem[];
+  __shared__ int s_item;
+  __shared__ double s_loss[NW];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_items = g.n_angles * tc.ntiles;
   float *acc = smem + (size_t)warp * L::kFloats;
@@ -101,16 +114,25 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   float *pc0 = reinterpret_cast<float *>(prm + 32 * 3);
   float *pc1 = pc0 + ROWS;
   int *list = reinterpret_cast<int *>(pc1 + 32);
+  const int wq = (W + NW - 1) / NW;
+  const int w_lo = min(W, warp * wq * (NW > 1)), w_hi = NW > 1 ? min(W, w_lo + wq) : W;
 
-  // persistent warps: each takes the next (angle, tile) item from a counter,
-  // so heavy tiles do not hold a block's other warps idle; what an item
-  // computes does not depend on which warp takes it
+  // persistent warps (blocks): each takes the next (angle, tile) item from a
+  // counter, so heavy tiles do not hold the others idle; what an item
+  // computes does not depend on which warp (block) takes it
   for (;;) {
   int item = 0;
-  if (lane == 0) item = atomicAdd(next_item, 1);
-  item = __shfl_sync(0xffffffffu, item, 0);
-  if (item >= n_items) break;  // whole warp leaves together
-  __syncwarp();  // the previous item's epilogue reads are done
+  if constexpr (NW == 1) {
+    if (lane == 0) item = atomicAdd(next_item, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= n_items) break;  // whole warp leaves together
+    __syncwarp();  // the previous item's epilogue reads are done
+  } else {
+    if (threadIdx.x == 0) s_item = atomicAdd(next_item, 1);
+    __syncthreads();
+    item = s_item;
+    if (item >= n_items) break;  // whole block leaves together
+  }
   const int a = item / tc.ntiles, t = item - a * tc.ntiles;
   const int tr = t / tc.nt1, tcix = t - tr * tc.nt1;
   const int r0 = tr * ROWS, c0 = tcix * 32;
@@ -127,16 +149,16 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   load_frame<2>(g.frames, a, f);
   __syncwarp();
 
-  // The tile's atoms, in index order, pass through a ring list: a refill
-  // reads 32 bitmap words (one per lane) and appends the atoms of as many
-  // whole words as fit, so every batch but the last holds 32 atoms however
-  // sparse the bitmap is.
+  // The warp's atoms of the tile, in index order, pass through a ring list:
+  // a refill reads 32 bitmap words (one per lane) and appends the atoms of as
+  // many whole words as fit, so every batch but the last holds 32 atoms
+  // however sparse the bitmap is.
   const uint32_t *words = bitmap + (size_t)item * W;
-  int head = 0, count = 0, wb = 0;
+  int head = 0, count = 0, wb = w_lo;
   while (true) {
-    while (count < 32 && wb < W) {
+    while (count < 32 && wb < w_hi) {
       const int wi = wb + lane;
-      uint32_t wd = wi < W ? words[wi] : 0u;
+      uint32_t wd = wi < w_hi ? words[wi] : 0u;
       const int cnt = __popc(wd);
       int incl = cnt;
 #pragma unroll
@@ -217,16 +239,32 @@ __global__ void __launch_bounds__(kProjWarps * 32)
       }
     }
   }
-  __syncwarp();
+  if constexpr (NW == 1) __syncwarp();
+  else __syncthreads();
 
-  // epilogue: write the tile, fused fit fields and loss partial
+  // epilogue: write the tile, fused fit fields and loss partial; a split
+  // item's cells combine the warps' sums in warp order
   float lsum = 0.f, lcmp = 0.f;
-  for (int e = lane; e < ROWS * 32; e += 32) {
+  for (int e = (NW == 1 ? lane : (int)threadIdx.x); e < ROWS * 32; e += NW * 32) {
     const int lr = e >> 5;
     const int row = r0 + lr, col = c0 + lane;
     if (row >= D0 || col >= D1) continue;
     const int ci = lr * S + lane;
-    const float v = acc[ci] + cmp[ci];
+    float v;
+    if constexpr (NW == 1) {
+      v = acc[ci] + cmp[ci];
+    } else {
+      float s0 = 0.f, c0s = 0.f;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        const float *aw = smem + (size_t)w * L::kFloats;
+        const float x = aw[ci] + aw[L::kAcc + ci];
+        const float tt = s0 + x;
+        c0s += (fabsf(s0) >= fabsf(x)) ? ((s0 - tt) + x) : ((x - tt) + s0);
+        s0 = tt;
+      }
+      v = s0 + c0s;
+    }
     const size_t gi = ((size_t)a * D0 + row) * D1 + col;
     if (out.R) out.R[gi] = v;
     float l = 0.f;
@@ -248,8 +286,35 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   }
   if (out.loss_part) {
     double d = warp_sum_d((double)lsum + (double)lcmp);
-    if (lane == 0) out.loss_part[item] = d;
+    if constexpr (NW == 1) {
+      if (lane == 0) out.loss_part[item] = d;
+    } else {
+      if (lane == 0) s_loss[warp] = d;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double tl = 0.0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) tl += s_loss[w];
+        out.loss_part[item] = tl;
+      }
+    }
   }
+  if constexpr (NW > 1) __syncthreads();  // cell sums and s_item are reused
+  }
+
+  if (loss_out && out.loss_part) {
+    // the last warp (block) to finish sums the items' partials in item order
+    const int units = NW == 1 ? (int)gridDim.x * kProjWarps : (int)gridDim.x;
+    if (NW > 1 && warp != 0) return;
+    int last = 0;
+    if (lane == 0) {
+      __threadfence();
+      last = atomicAdd(next_item + 1, 1) == units - 1;
+    }
+    if (__shfl_sync(0xffffffffu, last, 0)) {
+      __threadfence();
+      sum_partials_warp(out.loss_part, n_items, loss_out, lane);
+    }
   }
 }
 
@@ -384,11 +449,7 @@ __global__ void __launch_bounds__(NW * 32)
       }
       if (__shfl_sync(0xffffffffu, last, 0)) {
         __threadfence();
-        const volatile double *lp = out.loss_part;
-        double t = 0.0;
-        for (int i = lane; i < (int)gridDim.x; i += 32) t += lp[i];
-        t = warp_sum_d(t);
-        if (lane == 0) loss_out[0] = t;
+        sum_partials_warp(out.loss_part, (int)gridDim.x, loss_out, lane);
       }
     }
   }
@@ -629,17 +690,25 @@ int g_proj_form = 1;
 
 static int proj_rows(int form) { return form == 2 ? kTileDim0 : 16; }
 
-constexpr size_t kFusedLossItems = 65536;
+// Loss partials of up to this many items are summed by the projection's
+// last warp or block (sum_partials_warp: a chain of n / 256 FP64 adds);
+// above it the 1024-thread gr_loss_finalize_kernel does it.
+constexpr size_t kFusedLossItems = 8192;
 
-template <int ROWS, int S>
-static void launch_project3d(int blocks, const Atoms &at, const Geom &g, const TileCfg &tc,
+// 3D problems of fewer detector cells (all angles) than this split every
+// tile's atoms over a block's warps (gr_set_tuning key 4; 0: never).
+int g_proj_split_cells = 4 << 20;
+
+template <int ROWS, int S, int NW>
+static void launch_project3d(size_t items, const Atoms &at, const Geom &g, const TileCfg &tc,
                              const uint32_t *bitmap, int W, const ProjOut &o, int *next_item,
-                             cudaStream_t stream) {
+                             double *loss_out, cudaStream_t stream) {
   constexpr size_t smem = kProjWarps * Proj3Smem<ROWS, S>::kFloats * sizeof(float);
-  // below the 48 KB that needs no opt-in, so no function attribute is set
-  // (safe under stream capture)
-  static_assert(smem <= 48 * 1024, "smem");
-  // persistent grid: the resident blocks of every SM, at most one per 4 items
+  // with the few static bytes, below the 48 KB that needs no opt-in, so no
+  // function attribute is set (safe under stream capture)
+  static_assert(smem + 64 <= 48 * 1024, "smem");
+  // persistent grid: the resident blocks of every SM, at most the blocks
+  // that have an item to take
   static int resident[64] = {0};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -647,13 +716,14 @@ static void launch_project3d(int blocks, const Atoms &at, const Geom &g, const T
   if (resident[dev] == 0) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gr_project3d_kernel<ROWS, S>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gr_project3d_kernel<ROWS, S, NW>,
                                                   kProjWarps * 32, smem);
     resident[dev] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   }
-  const int grid = blocks < resident[dev] ? blocks : resident[dev];
-  gr_project3d_kernel<ROWS, S><<<grid, kProjWarps * 32, smem, stream>>>(at, g, tc, bitmap, W, o,
-                                                                        next_item);
+  const size_t want = NW == 1 ? (items + kProjWarps - 1) / kProjWarps : items;
+  const int grid = (int)(want < (size_t)resident[dev] ? want : (size_t)resident[dev]);
+  gr_project3d_kernel<ROWS, S, NW><<<grid, kProjWarps * 32, smem, stream>>>(
+      at, g, tc, bitmap, W, o, next_item, loss_out);
 }
 
 TileCfg make_tiles(int K, int D0, int D1, int rows) {
@@ -747,10 +817,20 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
     else
       gr_project1d_kernel<true, kProjWarps><<<(unsigned)items, kProjWarps * 32, 0, stream>>>(
           at, g, tc, bitmap, W, o, lo, next_item + 1);
-  } else if (form == 2) {
-    launch_project3d<32, 34>(blocks, at, g, tc, bitmap, W, o, next_item, stream);
   } else {
-    launch_project3d<16, 37>(blocks, at, g, tc, bitmap, W, o, next_item, stream);
+    // the split is chosen from the problem's size alone (not from the
+    // tiling), so both tilings keep giving the same cell sums
+    const bool split = g_proj_split_cells > 0 && W >= kProjWarps &&
+                       (size_t)g.n_angles * D0 * D1 < (size_t)g_proj_split_cells;
+    fused_loss = loss_out != nullptr && items <= kFusedLossItems;
+    double *lo = fused_loss ? loss_out : nullptr;
+    if (form == 2) {
+      if (split) launch_project3d<32, 34, kProjWarps>(items, at, g, tc, bitmap, W, o, next_item, lo, stream);
+      else launch_project3d<32, 34, 1>(items, at, g, tc, bitmap, W, o, next_item, lo, stream);
+    } else {
+      if (split) launch_project3d<16, 37, kProjWarps>(items, at, g, tc, bitmap, W, o, next_item, lo, stream);
+      else launch_project3d<16, 37, 1>(items, at, g, tc, bitmap, W, o, next_item, lo, stream);
+    }
   }
   timer_mark(1, 1, stream);
   note_launches(1);

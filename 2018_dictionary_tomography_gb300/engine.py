@@ -80,9 +80,21 @@ class DeviceAtoms:
         else:
             x = x.reshape(0, x.shape[-1] if x.dim() > 1 else 0)
             r = r.reshape(0, r.shape[-1] if r.dim() > 1 else 1)
-        self.iso = r.shape[1] == 1
-        if self.iso:
+        if r.shape[1] == 1:
             r = r.reshape(n).contiguous()
+        self._bind(I, x, r, device, order)
+
+    @classmethod
+    def wrap(cls, I, x, r):
+        """Atoms over float32 device tensors I (n,), x (n, dim) and r (n,)
+        (isotropic) or (n, 3 | 6), used in place: no allocation, no copy."""
+        self = cls.__new__(cls)
+        self._bind(I, x, r, I.device, None)
+        return self
+
+    def _bind(self, I, x, r, device, order):
+        n = I.numel()
+        self.iso = r.dim() == 1
         self.I, self.x, self.r = I, x, r
         self.n = n
         self.dim = x.shape[1] if n > 0 else 0

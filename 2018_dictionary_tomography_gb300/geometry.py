@@ -111,16 +111,36 @@ class DeviceGeometry:
 
     def __init__(self, orientations, ortho, detector, device=None):
         device = torch.device(device or "cuda")
+        detector, rec, kdet = self.host_records(orientations, ortho, detector)
+        frames = torch.from_numpy(rec).to(device)
+        det = [torch.from_numpy(d.copy()).to(device) for d in detector]
+        self._bind(rec, kdet, detector, frames, det, device)
+
+    @staticmethod
+    def host_records(orientations, ortho, detector):
+        """(detector coordinate arrays, frame records, kdet) on the host."""
         detector = [np.asarray(_np(d), dtype=np.float32).reshape(-1) for d in detector]
         rec, kdet = frame_records(orientations, ortho, len(detector))
         if len(detector) != kdet:
             raise ValueError("detector must have %d coordinate vectors" % kdet)
+        return detector, rec, kdet
+
+    @classmethod
+    def bound(cls, rec, kdet, detector, frames, det, device):
+        """A geometry over device buffers that hold (or will hold, by a copy
+        queued before any use) the frame records ``rec`` and the detector
+        coordinates: no allocation, no copy."""
+        self = cls.__new__(cls)
+        self._bind(rec, kdet, detector, frames, det, torch.device(device))
+        return self
+
+    def _bind(self, rec, kdet, detector, frames, det, device):
         self.kdet = kdet
         self.dim = kdet + 1
         self.n_angles = rec.shape[0]
         self.frames_host = rec
-        self.frames = torch.from_numpy(rec).to(device)
-        self.det = [torch.from_numpy(d.copy()).to(device) for d in detector]
+        self.frames = frames
+        self.det = det
         self.grid = [uniform_grid(d, "detector axis %d" % k) for k, d in enumerate(detector)]
         self.shape = (self.n_angles,) + tuple(int(d.size) for d in detector)
         self.device = device

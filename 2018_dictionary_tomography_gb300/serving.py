@@ -33,12 +33,15 @@ buffers of a new request are built on a separate setup stream; finished
 loop graphs are destroyed only when no fit runs (destroying an executable
 graph waits for the device to idle); pinned host buffers are pooled.  Among
 requests that have arrived, the largest are admitted first, so the longest
-fits start early.
+fits start early.  A request is admitted only onto a stream with no fit in
+flight (``exclusive_streams``): a stream runs its work in order, and a
+whole fit is one graph launch, so a request queued behind another on the
+same stream would wait for that entire fit however little work it has.
 
 The process should give every stream its own hardware work queue
-(environment ``CUDA_DEVICE_MAX_CONNECTIONS`` >= n_streams + 1, set before CUDA
-starts): with fewer, streams share queues and a request's set-up can wait
-behind another request's whole fit.
+(environment ``CUDA_DEVICE_MAX_CONNECTIONS`` >= n_streams + 1, at most 32,
+set before CUDA starts): streams that share a queue are serialised the same
+way.
 
 ``serve_plain`` is the baseline: the same fits one after another with the
 eager host-driven loop, one host sync per iteration.
@@ -91,74 +94,155 @@ class FitRequest:
         self.size_hint = (n, cells)
 
 
+_ALIGN = 256
+_TORCH_DTYPE = {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64,
+                np.dtype(np.int32): torch.int32, np.dtype(np.uint8): torch.uint8}
+
+
+def _layout(items):
+    """Byte layout of (name, dtype, shape) buffers packed at 256-byte
+    offsets: ({name: (offset, dtype, shape, nbytes)}, total bytes)."""
+    out, off = {}, 0
+    for name, dt, shape in items:
+        dt = np.dtype(dt)
+        nb = int(np.prod(shape, dtype=np.int64)) * dt.itemsize
+        out[name] = (off, dt, tuple(int(v) for v in shape), nb)
+        off += (nb + _ALIGN - 1) // _ALIGN * _ALIGN
+    return out, max(off, _ALIGN)
+
+
+def _view(buf, spec):
+    """Typed view of a uint8 torch buffer (device or host)."""
+    off, dt, shape, nb = spec
+    return buf[off:off + nb].view(_TORCH_DTYPE[dt]).view(shape)
+
+
+def _host_view(arr, spec):
+    """Typed view of a uint8 numpy array."""
+    off, dt, shape, nb = spec
+    return arr[off:off + nb].view(dt).reshape(shape)
+
+
+# Pinned host buffers, pooled by power-of-two capacity for the life of the
+# process: pinning memory is a slow driver call, and a request needs two
+# buffers (input staging, results).
+_pinned_free = {}
+
+
+def _pinned_take(nbytes):
+    cap = 1 << max(12, int(nbytes - 1).bit_length())
+    free = _pinned_free.get(cap)
+    if free:
+        return free.pop()
+    return torch.empty(cap, dtype=torch.uint8, pin_memory=True)
+
+
+def _pinned_give(buf):
+    _pinned_free.setdefault(buf.numel(), []).append(buf)
+
+
 class _Slot:
     """Device state of one admitted request."""
 
     def __init__(self, req, stream, device, use_graph=True, iters_per_launch=4,
-                 device_loop=True, setup_stream=None, pinned=None):
+                 device_loop=True, setup_stream=None):
         self.req = req
         self.stream = stream
         self.dev = device
         self.k = iters_per_launch
         # Buffers are built and filled on a setup stream: the compute stream
-        # may still hold queued fits of earlier requests.
+        # may still hold queued fits of earlier requests.  A request's device
+        # state is two allocations: an input arena, filled from one pinned
+        # staging buffer by one copy, and a work arena (fit fields,
+        # derivatives, workspaces); every buffer is a view of one of them.
         setup = setup_stream if setup_stream is not None else stream
         t_start = time.perf_counter()
+        I0, x0, r0 = (np.asarray(v) for v in req.init)
+        n = len(I0)
+        det_h, rec, kdet = DeviceGeometry.host_records(req.orientations, req.ortho,
+                                                       req.detector)
+        dim = kdet + 1
+        I32 = I0.astype(np.float32).reshape(n)
+        x32 = x0.astype(np.float32).reshape(n, dim)
+        r32 = r0.astype(np.float32).reshape(n, -1)
+        iso = r32.shape[1] == 1
+        if iso:
+            r32 = r32.reshape(n)
+        P = (2 + dim) if iso else (1 + dim + (3 if dim == 2 else 6))
+        theta = np.concatenate([I32.reshape(n, 1), x32, r32.reshape(n, -1)], 1).astype(np.float64)
+        L = req.max_iter + MAX_BACKTRACK + 8
+        lay, n_in = _layout([("frames", np.float32, rec.shape)] +
+                            [("det%d" % k, np.float32, d.shape) for k, d in enumerate(det_h)] +
+                            [("I", np.float32, I32.shape), ("x", np.float32, x32.shape),
+                             ("r", np.float32, r32.shape), ("tI", np.float32, I32.shape),
+                             ("tx", np.float32, x32.shape), ("tr", np.float32, r32.shape),
+                             ("theta", np.float64, (n, P)), ("theta_t", np.float64, (n, P)),
+                             ("lam", np.float64, (n,)), ("loss", np.float64, (2,)),
+                             ("hist", np.float64, (L,)), ("acc", np.int32, (L,)),
+                             ("counter", np.int32, (1,))])
+        self.staging = _pinned_take(n_in)
+        host = self.staging.numpy()
+        host[:n_in] = 0
+        for name, val in (("frames", rec), ("I", I32), ("x", x32), ("r", r32), ("tI", I32),
+                          ("tx", x32), ("tr", r32), ("theta", theta), ("theta_t", theta),
+                          ("lam", np.full(n, float(req.lam0)))):
+            _host_view(host, lay[name])[...] = val
+        for k, d in enumerate(det_h):
+            _host_view(host, lay["det%d" % k])[...] = d
+        self.arena_in = torch.empty(n_in, dtype=torch.uint8, device=device)
         with torch.cuda.stream(setup):
-            self.geom = DeviceGeometry(req.orientations, req.ortho, req.detector, device)
-            I0, x0, r0 = req.init
-            n = len(I0)
-            self.cur = engine.DeviceAtoms(I0, x0, r0, device)
-            self.trial = engine.DeviceAtoms(I0, x0, r0, device)
-            self.dim, self.iso = self.cur.dim, self.cur.iso
-            self.P = self.cur.n_params()
-            self.theta = torch.cat([self.cur.I.double().reshape(-1, 1), self.cur.x.double(),
-                                    self.cur.r.double().reshape(n, -1)], 1).contiguous()
-            self.theta_trial = self.theta.clone()
-            self.lam = torch.full((n,), float(req.lam0), dtype=torch.float64, device=device)
-            shape = self.geom.shape
-            self.data = req.device_data(self.geom, device, setup)
-            self.alpha = torch.empty(shape, dtype=torch.float32, device=device)
-            self.beta = (torch.empty(shape, dtype=torch.float32, device=device)
-                         if req.fit == "kl" else None)
-            # the trial's fit fields (adopted when the trial is accepted)
-            self.alpha_t = torch.empty(shape, dtype=torch.float32, device=device)
-            self.beta_t = (torch.empty(shape, dtype=torch.float32, device=device)
-                           if req.fit == "kl" else None)
-            self.loss_cur = torch.zeros((), dtype=torch.float64, device=device)
-            self.loss_trial = torch.zeros((), dtype=torch.float64, device=device)
-            self.f = torch.empty(n, dtype=torch.float64, device=device)
-            self.g = torch.empty((n, self.P), dtype=torch.float64, device=device)
-            self.H = torch.empty((n, self.P, self.P), dtype=torch.float64, device=device)
-            self.step = torch.empty(n, dtype=torch.float64, device=device)
-            self.ws_p = torch.empty(max(256, engine.workspace_bytes(_lib.GR_OP_PROJECT, self.cur, self.geom)),
-                                    dtype=torch.uint8, device=device)
-            self.ws_d = torch.empty(max(256, engine.workspace_bytes(_lib.GR_OP_DERIVS_2, self.cur, self.geom)),
-                                    dtype=torch.uint8, device=device)
-            L = req.max_iter + MAX_BACKTRACK + 8
-            self.hist = torch.zeros(L, dtype=torch.float64, device=device)
-            self.hist_acc = torch.zeros(L, dtype=torch.int32, device=device)
-            self.counter = torch.zeros(1, dtype=torch.int32, device=device)
-            if pinned is None:
-                pinned = (torch.zeros(L, dtype=torch.float64).pin_memory(),
-                          torch.zeros(L, dtype=torch.int32).pin_memory(),
-                          torch.zeros(1, dtype=torch.int32).pin_memory())
-            self.pinned = pinned
-            self.h_hist, self.h_acc, self.h_counter = pinned
+            self.arena_in.copy_(self.staging[:n_in], non_blocking=True)
+        v = lambda name: _view(self.arena_in, lay[name])
+        self.geom = DeviceGeometry.bound(rec, kdet, det_h, v("frames"),
+                                         [v("det%d" % k) for k in range(kdet)], device)
+        self.cur = engine.DeviceAtoms.wrap(v("I"), v("x"), v("r"))
+        self.trial = engine.DeviceAtoms.wrap(v("tI"), v("tx"), v("tr"))
+        self.dim, self.iso, self.P = dim, iso, P
+        self.theta, self.theta_trial, self.lam = v("theta"), v("theta_t"), v("lam")
+        loss = v("loss")
+        self.loss_cur, self.loss_trial = loss[0], loss[1]
+        self.hist, self.hist_acc, self.counter = v("hist"), v("acc"), v("counter")
+        shape = self.geom.shape
+        kl = req.fit == "kl"
+        ws_p = max(256, engine.workspace_bytes(_lib.GR_OP_PROJECT, self.cur, self.geom))
+        ws_d = max(256, engine.workspace_bytes(_lib.GR_OP_DERIVS_2, self.cur, self.geom))
+        wl, n_work = _layout([("data", np.float32, shape), ("alpha", np.float32, shape),
+                              ("alpha_t", np.float32, shape)] +
+                             ([("beta", np.float32, shape), ("beta_t", np.float32, shape)]
+                              if kl else []) +
+                             [("f", np.float64, (n,)), ("g", np.float64, (n, P)),
+                              ("H", np.float64, (n, P, P)), ("step", np.float64, (n,)),
+                              ("ws_p", np.uint8, (ws_p,)), ("ws_d", np.uint8, (ws_d,))])
+        self.arena_work = torch.empty(n_work, dtype=torch.uint8, device=device)
+        w = lambda name: _view(self.arena_work, wl[name])
+        self.data = w("data")
+        with torch.cuda.stream(setup):
+            if req.data_host is not None:
+                self.data.copy_(req.data_host.reshape(shape), non_blocking=True)
+            else:
+                self.data.copy_(req.make_data(self.geom, device, setup))
+        self.alpha, self.alpha_t = w("alpha"), w("alpha_t")
+        self.beta, self.beta_t = (w("beta"), w("beta_t")) if kl else (None, None)
+        self.f, self.g, self.H, self.step = w("f"), w("g"), w("H"), w("step")
+        self.ws_p, self.ws_d = w("ws_p"), w("ws_d")
+        # results come back into pinned memory: history, counter, parameters
+        # and loss, read after the completion event without a stream sync
+        self.res_layout, n_res = _layout([("hist", np.float64, (L,)), ("acc", np.int32, (L,)),
+                                          ("counter", np.int32, (1,)),
+                                          ("theta", np.float64, (n, P)),
+                                          ("loss", np.float64, (1,))])
+        self.results = _pinned_take(n_res)
+        r = lambda name: _view(self.results, self.res_layout[name])
+        self.h_hist, self.h_acc, self.h_counter = r("hist"), r("acc"), r("counter")
+        self.h_theta, self.h_loss = r("theta"), r("loss")
         t_bufs = time.perf_counter()
         if setup is not stream:
             ready = torch.cuda.Event()
             ready.record(setup)
             stream.wait_event(ready)
-            for t in (self.geom.frames, self.geom.det, self.cur.I, self.cur.x,
-                      self.cur.r, self.trial.I, self.trial.x, self.trial.r, self.theta,
-                      self.theta_trial, self.lam, self.data, self.alpha, self.beta,
-                      self.alpha_t, self.beta_t,
-                      self.loss_cur, self.loss_trial, self.f, self.g, self.H, self.step,
-                      self.ws_p, self.ws_d, self.hist, self.hist_acc, self.counter):
-                for u in (t if isinstance(t, (list, tuple)) else (t,)):
-                    if u is not None:
-                        u.record_stream(stream)
+            # the arenas' memory is in use on the compute stream from here
+            self.arena_in.record_stream(stream)
+            self.arena_work.record_stream(stream)
         t_cap = time.perf_counter()
         with torch.cuda.stream(stream):
             self.event = torch.cuda.Event()
@@ -198,10 +282,15 @@ class _Slot:
         self.iterations_launched = 1
 
     def bytes(self):
-        tensors = [self.data, self.alpha, self.beta, self.alpha_t, self.beta_t, self.g,
-                   self.H, self.ws_p, self.ws_d,
-                   self.theta, self.theta_trial]
-        return sum(t.numel() * t.element_size() for t in tensors if t is not None)
+        return self.arena_in.numel() + self.arena_work.numel()
+
+    def release(self):
+        """Return the pinned buffers to the pool (the request is finished:
+        its copies completed before its last event)."""
+        for b in (self.staging, self.results):
+            if b is not None:
+                _pinned_give(b)
+        self.staging = self.results = None
 
     def prologue(self):
         """Fit fields and loss of the starting atoms (once per fit)."""
@@ -232,6 +321,8 @@ class _Slot:
         self.h_counter.copy_(self.counter, non_blocking=True)
         self.h_hist.copy_(self.hist, non_blocking=True)
         self.h_acc.copy_(self.hist_acc, non_blocking=True)
+        self.h_theta.copy_(self.theta, non_blocking=True)
+        self.h_loss.copy_(self.loss_cur.reshape(1), non_blocking=True)
         self.event.record(self.stream)
 
     def launch(self):
@@ -276,12 +367,12 @@ class _Slot:
         return False
 
     def result(self):
-        self.stream.synchronize()
+        """Parameters, loss and iteration count from the pinned copies (call
+        after the completion event: no stream sync, so other requests
+        queued on the same stream are not waited for)."""
         c = int(self.h_counter[0])
-        with torch.cuda.stream(self.stream):
-            theta = self.theta.cpu().numpy()
-            loss = float(self.loss_cur.item())
-        return {"theta": theta, "loss": loss, "iterations": min(c, self.req.max_iter)}
+        return {"theta": self.h_theta.numpy().copy(), "loss": float(self.h_loss[0]),
+                "iterations": min(c, self.req.max_iter)}
 
 
 _warmed = set()
@@ -319,7 +410,7 @@ class GaussFitServer:
 
     def __init__(self, device=None, max_slots=32, n_streams=16, hbm_budget=None,
                  hbm_reserve=4 << 30, use_graphs=True, iters_per_launch=4, device_loop=True,
-                 largest_first=True):
+                 largest_first=True, exclusive_streams=True):
         self.dev = torch.device(device or "cuda")
         engine._require_cuda(self.dev)
         self.max_slots = max_slots
@@ -331,6 +422,7 @@ class GaussFitServer:
         self.k = iters_per_launch
         self.device_loop = device_loop
         self.largest_first = largest_first
+        self.exclusive_streams = exclusive_streams
         self.pending = collections.deque()
         self.active = []
         self.results = {}
@@ -344,7 +436,6 @@ class GaussFitServer:
         # destroying an executable graph waits for the whole device to idle,
         # which would stall the host loop behind every fit in flight.
         self._retired_loops = []
-        self._pinned = {}            # history length -> free pinned host buffers
         _warm_engine(self.dev)
 
     @staticmethod
@@ -377,6 +468,9 @@ class GaussFitServer:
             req = self.pending[0]
             if req.arrival > now:
                 break
+            si = int(np.argmin(self.stream_busy))
+            if self.exclusive_streams and self.stream_busy[si] > 0:
+                break                            # wait for a stream of its own
             need = self.estimate_bytes(req)
             if self.in_use + need > self.budget:
                 if not self.active:
@@ -384,15 +478,12 @@ class GaussFitServer:
                                       % (req.id, need, self.budget))
                 break
             self.pending.popleft()
-            si = int(np.argmin(self.stream_busy))
             self.stream_busy[si] += 1
             if self.active:
                 self.admitted_while_busy += 1
             ta = time.perf_counter()
-            L = req.max_iter + MAX_BACKTRACK + 8
-            free = self._pinned.get(L)
             slot = _Slot(req, self.streams[si], self.dev, self.use_graphs, self.k,
-                         self.device_loop, self.setup_stream, free.pop() if free else None)
+                         self.device_loop, self.setup_stream)
             self.admit_seconds += time.perf_counter() - ta
             phases = dict(slot.phase_seconds)
             if slot.loop is not None:
@@ -432,7 +523,7 @@ class GaussFitServer:
                     if slot.loop is not None:
                         self._retired_loops.append(slot.loop)
                         slot.loop = None
-                    self._pinned.setdefault(len(slot.h_hist), []).append(slot.pinned)
+                    slot.release()
                     if on_done:
                         on_done(slot.req, res)
                     del slot

@@ -35,6 +35,16 @@ def set_projection_tiling(form):
     _lib.check(_lib.load().gr_set_tuning(3, int(form)), "gr_set_tuning")
 
 
+def set_projection_split(cells):
+    """3D problems with fewer detector cells (all angles) than ``cells``
+    split each tile's atoms over a block's warps (0: never)."""
+    _lib.check(_lib.load().gr_set_tuning(4, int(cells)), "gr_set_tuning")
+
+
+def get_projection_split():
+    return int(_lib.load().gr_get_tuning(4))
+
+
 def get_split():
     lib = _lib.load()
     return int(lib.gr_get_tuning(0)), int(lib.gr_get_tuning(1)), int(lib.gr_get_tuning(2))

@@ -518,7 +518,7 @@ def run_serving(args):
     # graph instantiations in a process is paid here, as by a running server)
     warm = wl.config3_requests(n=64, rate=1e9, seed=99, atoms=(16, 64), angles=(10, 20),
                                det=(32, 48), max_iter=4)
-    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=16)
+    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31)
     for r in warm:
         srv.submit(r)
     srv.run()
@@ -531,7 +531,7 @@ def run_serving(args):
     for r in cmp_reqs:
         r.arrival = 0.0
     t0 = time.perf_counter()
-    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=16)
+    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31)
     for r in cmp_reqs:
         srv.submit(r)
     served_cmp = srv.run(t0=t0)
@@ -552,7 +552,7 @@ def run_serving(args):
     sampler = ClockSampler(local)
     sampler.start()
     t0 = time.perf_counter()
-    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=16)
+    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31)
     for r in stream_reqs:
         srv.submit(r)
     res = srv.run(t0=t0)

@@ -254,10 +254,15 @@ unsigned long long gr_launch_count(void);
  * atoms (default 0: automatic, one atom per warp for Hessians and for series
  * of 1024 or more angles, else four).  GR_TUNE_PROJ_TILING: tiles of the
  * point-sampled 3D projection, 1 = 16 x 32 cells (default, more resident
- * warps), 2 = 32 x 32 (fewer atoms cut by tile edges).  Set them before
+ * warps), 2 = 32 x 32 (fewer atoms cut by tile edges).
+ * GR_TUNE_PROJ_SPLIT_CELLS: 3D problems with fewer detector cells over all
+ * angles than this (default 4194304; 0 = never) split each tile's atoms over
+ * the four warps of a block, which shortens the slowest tile when there are
+ * too few tiles to fill the GPU.  Set them before
  * gr_workspace_bytes and keep them fixed while launches that used the old
  * values are in flight.  Results do not depend on them beyond FP rounding of
- * the derivative chunk sums (the tiling leaves projections bitwise equal).  gr_set_tuning returns
+ * the derivative chunk sums and of a split tile's combined cell sums (the
+ * tiling leaves projections bitwise equal).  gr_set_tuning returns
  * GR_ERR_ARG for an unknown key or out-of-range value; gr_get_tuning returns
  * the current value (-1 for an unknown key).
  */
@@ -265,7 +270,8 @@ enum {
   GR_TUNE_DERIV_WARPS = 0,
   GR_TUNE_DERIV_MIN_ANGLES = 1,
   GR_TUNE_DERIV_ATOMS_PER_WARP = 2,
-  GR_TUNE_PROJ_TILING = 3
+  GR_TUNE_PROJ_TILING = 3,
+  GR_TUNE_PROJ_SPLIT_CELLS = 4
 };
 int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);

@@ -210,3 +210,37 @@ def test_projection_tiling_is_bitwise_neutral(eng, cuda_ready):
         tuning.set_projection_tiling(1)
     assert torch.equal(outs[0][0], outs[1][0])
     assert relerr(outs[0][0].cpu().numpy(), go.radproj(I, x, r, g)) < TOL
+
+
+def test_projection_split_over_warps(eng, cuda_ready):
+    """Small 3D problems split each tile's atoms over a block's warps; that
+    changes only the rounding of the combined cell sums, both tilings still
+    agree bitwise, and the projection still matches the oracle."""
+    import importlib
+    tuning = importlib.import_module("2018_dictionary_tomography_gb300.tuning")
+    g = make_geometry("3d", 12, 40, 44)
+    I, x, r = make_atoms(3, 300, 33, rdiag=(6.0, 12.0), box=0.7)
+    geom, atoms = engine_geometry(g), engine_atoms(I, x, r)
+    Ro = go.radproj(I, x, r, g)
+    data = torch.from_numpy(Ro * 1.1).float().cuda()
+    saved = tuning.get_projection_split()
+    outs = {}
+    try:
+        for split in (1 << 30, 0):
+            tuning.set_projection_split(split)
+            for form in (1, 2):
+                tuning.set_projection_tiling(form)
+                fw = eng.fit_forward(atoms, geom, data, "l2", want_R=True)
+                outs[(split, form)] = (fw["R"].clone(), float(fw["loss"].item()))
+    finally:
+        tuning.set_projection_tiling(1)
+        tuning.set_projection_split(saved)
+    Rs, Ru = outs[(1 << 30, 1)][0], outs[(0, 1)][0]
+    assert torch.equal(Rs, outs[(1 << 30, 2)][0])
+    assert torch.equal(Ru, outs[(0, 2)][0])
+    assert relerr(Rs.cpu().numpy(), Ru.cpu().numpy()) < 1e-6
+    assert relerr(Rs.cpu().numpy(), Ro) < TOL
+    d32 = (Ro * 1.1).astype(np.float32).astype(np.float64)
+    lo = 0.5 * float(np.sum((Ro - d32) ** 2))
+    for key, (_R, loss) in outs.items():
+        assert abs(loss - lo) <= TOL * lo, key
