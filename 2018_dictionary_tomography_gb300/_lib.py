@@ -38,7 +38,7 @@ class EngineError(RuntimeError):
     pass
 
 
-EXPORTS = ("gr_version", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
+EXPORTS = ("gr_version", "gr_preload", "gr_status_string", "gr_workspace_bytes", "gr_radproj",
            "gr_fit_forward", "gr_atom_derivs", "gr_count_support", "gr_probe_ex2",
            "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj", "gr_newton_accept",
            "gr_psf_radproj", "gr_psf_fit_forward", "gr_psf_atom_derivs", "gr_psf_volproj",
@@ -69,6 +69,8 @@ def load(build_if_missing=True):
         lib = ctypes.CDLL(path)
         P = ctypes.POINTER
         lib.gr_version.restype = ctypes.c_int
+        lib.gr_preload.restype = ctypes.c_int
+        lib.gr_preload.argtypes = []
         lib.gr_status_string.restype = ctypes.c_char_p
         lib.gr_status_string.argtypes = [ctypes.c_int]
         lib.gr_workspace_bytes.restype = ctypes.c_size_t

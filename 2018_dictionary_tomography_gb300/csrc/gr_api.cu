@@ -46,6 +46,12 @@ extern "C" {
 
 int gr_version(void) { return 10000; }
 
+int gr_preload(void) {
+  const int bad = preload_project() + preload_derivs() + preload_update() + preload_loop() +
+                  preload_moments() + preload_reg() + preload_volume();
+  return bad ? GR_ERR_LAUNCH : GR_OK;
+}
+
 const char *gr_status_string(int status) {
   switch (status) {
     case GR_OK: return "ok";

@@ -693,4 +693,13 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
+int preload_derivs() {
+  return preload_fn(gr_deriv_kernel<1, 1>) + preload_fn(gr_deriv_kernel<1, 2>) +
+         preload_fn(gr_deriv_kernel<2, 1>) + preload_fn(gr_deriv_kernel<2, 2>) +
+         preload_fn(gr_psf_deriv_kernel<1, 1>) + preload_fn(gr_psf_deriv_kernel<1, 2>) +
+         preload_fn(gr_psf_deriv_kernel<2, 1>) + preload_fn(gr_psf_deriv_kernel<2, 2>) +
+         preload_fn(gr_deriv_finalize_kernel<1>) + preload_fn(gr_deriv_finalize_kernel<2>) +
+         preload_fn(gr_sumsq_kernel) + preload_fn(gr_sumsq_finalize_kernel);
+}
+
 }  // namespace gr

@@ -113,6 +113,24 @@ int get_tuning(int key);
 
 // host-side count of kernels launched by this library
 void note_launches(int n);
+
+// Loads a kernel's code now.  Module loading is lazy by default, so a
+// kernel's first launch -- or the first instantiation of a graph holding it
+// -- would otherwise pay the load while other work waits.  Returns 1 on
+// failure.
+template <typename F>
+inline int preload_fn(F f) {
+  cudaFuncAttributes a;
+  return cudaFuncGetAttributes(&a, f) == cudaSuccess ? 0 : 1;
+}
+// per-file preloads of every kernel a file launches (failure counts)
+int preload_project();
+int preload_derivs();
+int preload_update();
+int preload_loop();
+int preload_moments();
+int preload_reg();
+int preload_volume();
 int launch_accept_fields(const double *loss_cur, const double *loss_trial, const float *alpha_t,
                          float *alpha, const float *beta_t, float *beta, size_t n,
                          cudaStream_t stream);

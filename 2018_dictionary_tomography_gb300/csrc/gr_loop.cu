@@ -158,6 +158,8 @@ int fit_loop_destroy(FitLoop *L) {
   return kOk;
 }
 
+int preload_loop() { return preload_fn(gr_fit_loop_stop_kernel); }
+
 }  // namespace gr
 
 extern "C" {

@@ -83,4 +83,8 @@ int launch_moments(const Geom &g, const float *res, const float *rr, float t, fl
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
+int preload_moments() {
+  return preload_fn(gr_moments_kernel<1>) + preload_fn(gr_moments_kernel<2>);
+}
+
 }  // namespace gr

@@ -841,4 +841,17 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
+int preload_project() {
+  return preload_fn(gr_bin_kernel<1>) + preload_fn(gr_bin_kernel<2>) +
+         preload_fn(gr_psf_bin_kernel<1>) + preload_fn(gr_psf_bin_kernel<2>) +
+         preload_fn(gr_project3d_kernel<16, 37, 1>) +
+         preload_fn(gr_project3d_kernel<16, 37, kProjWarps>) +
+         preload_fn(gr_project3d_kernel<32, 34, 1>) +
+         preload_fn(gr_project3d_kernel<32, 34, kProjWarps>) +
+         preload_fn(gr_project1d_kernel<true, 8>) +
+         preload_fn(gr_project1d_kernel<true, kProjWarps>) +
+         preload_fn(gr_psf_project_kernel<1>) + preload_fn(gr_psf_project_kernel<2>) +
+         preload_fn(gr_loss_finalize_kernel);
+}
+
 }  // namespace gr

@@ -205,6 +205,8 @@ int launch_regulariser(int kind, const RegParams &prm, int dim, int iso, int n,
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
+int preload_reg() { return preload_fn(gr_reg_kernel<2>) + preload_fn(gr_reg_kernel<3>); }
+
 }  // namespace gr
 
 extern "C" int gr_regulariser(int kind, const double *params, int n_params,

@@ -17,6 +17,7 @@
 //    in NewtonGaussian.py:74), one group of lanes per atom, then the reference's parameter update with its
 //    clamps: I >= 0, and sign flips keeping diag(r) >= 0 (GD_lib.py:504-522).
 #include "gr_kernels.cuh"
+#include "gr_dfloat.cuh"
 
 namespace gr {
 
@@ -153,15 +154,16 @@ int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int 
 // ---------------------------------------------------------------------------
 // batched damped Newton step
 // ---------------------------------------------------------------------------
-// FP64 arithmetic is a narrow pipe on this GPU, so a P x P factorisation run
-// by one thread is one long chain of dependent FP64 operations (about a
-// thousand for P = 10, divisions and square roots included) and its latency,
-// not its work, sets the kernel time.  Here a group of G lanes (G a power of
-// two >= P) shares one atom: lane l holds row l of the damped block in
-// registers, columns are broadcast with shuffles, and each column costs one
-// reciprocal square root (Cholesky) or one reciprocal (LU), after which the
-// lanes update their rows independently.  The dependent chain per column is
-// a broadcast, the reciprocal and two multiply-adds.
+// On this GPU an FP64 instruction holds the SM's FP64 pipe for 16 cycles per
+// warp and a dependent FP64 operation takes about 64 cycles, so a P x P
+// factorisation in FP64 is slow twice over: by the length of its dependent
+// chain and by the pipe.  Here a group of G lanes (G a power of two >= P)
+// shares one atom, lane l holding row l of the damped block, and the
+// arithmetic is double-float (pairs of floats, about 48 significant bits,
+// gr_dfloat.cuh) on the FP32 pipe; FP64 is used only to read the FP64
+// inputs and to form the FP64 outputs.  Columns are broadcast with shuffles;
+// each column costs one reciprocal square root (Cholesky) or one reciprocal
+// (LU), after which the lanes update their rows independently.
 //
 // Every lane of a warp executes every shuffle (no lane leaves early), so a
 // group whose atom is out of range or masked runs on an identity block and
@@ -172,44 +174,42 @@ int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int 
 // Returns (identically on all lanes of the group) whether every pivot was
 // positive; x[] receives the solution on every lane.
 template <int P, int G>
-__device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l,
-                                               double (&x)[P]) {
-  constexpr unsigned kAll = 0xffffffffu;
-  double inv[P], col[P];
+__device__ __forceinline__ bool group_cholesky(dfl (&a)[P], dfl b, int l, dfl (&x)[P]) {
+  dfl inv[P], col[P];
   bool spd = true;
 #pragma unroll
-  for (int k = 0; k < P; ++k) col[k] = 0.0;
+  for (int k = 0; k < P; ++k) col[k] = df_make(0.f);
 #pragma unroll
   for (int j = 0; j < P; ++j) {
-    const double piv = __shfl_sync(kAll, a[j], j, G);
-    spd = spd && (piv > 0.0);
-    const double ij = rsqrt(piv > 0.0 ? piv : 1.0);
+    const dfl piv = df_shfl(a[j], j, G);
+    const bool pos = piv.hi > 0.f;
+    spd = spd && pos;
+    const dfl ij = df_rsqrt(pos ? piv : df_make(1.f));
     inv[j] = ij;
-    const double lij = (l == j) ? piv * ij : a[j] * ij;   // L[l][j] for l >= j
+    const dfl lij = df_mul(l == j ? piv : a[j], ij);  // L[l][j] for l >= j
     a[j] = lij;
 #pragma unroll
     for (int k = j + 1; k < P; ++k) {
-      const double lkj = __shfl_sync(kAll, lij, k, G);
-      if (l == j) col[k] = lkj;         // lane j keeps column j of L
-      a[k] = fma(-lij, lkj, a[k]);      // trailing rows (only k <= l is used)
+      const dfl lkj = df_shfl(lij, k, G);
+      if (l == j) col[k] = lkj;          // lane j keeps column j of L
+      a[k] = df_fms(a[k], lij, lkj);     // trailing rows (only k <= l is used)
     }
   }
   // forward: y_j = (b_j - sum_{k<j} L[j][k] y_k) / L[j][j]; lane l folds
   // each y_j into its own b as soon as it is known
-  double y[P];
+  dfl y[P];
 #pragma unroll
   for (int j = 0; j < P; ++j) {
-    y[j] = __shfl_sync(kAll, b, j, G) * inv[j];
-    b = fma(-a[j], y[j], b);
+    y[j] = df_mul(df_shfl(b, j, G), inv[j]);
+    b = df_fms(b, a[j], y[j]);
   }
   // backward: x_i = (y_i - sum_{k>i} L[k][i] x_k) / L[i][i]; lane i holds
   // column i of L below the diagonal in col[]
-  double acc = 0.0;
+  dfl acc = df_make(0.f);
 #pragma unroll
   for (int k = P - 1; k >= 0; --k) {
-    const double v = (y[k] - acc) * inv[k];
-    x[k] = __shfl_sync(kAll, v, k, G);
-    acc = fma(col[k], x[k], acc);
+    x[k] = df_shfl(df_mul(df_sub(y[k], acc), inv[k]), k, G);
+    acc = df_add(acc, df_mul(col[k], x[k]));
   }
   return spd;
 }
@@ -221,54 +221,54 @@ __device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l,
 // column c with the multiplier a[c] * (1 / pivot).  Returns false for a
 // zero pivot column.
 template <int P, int G>
-__device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, double (&x)[P]) {
-  constexpr unsigned kAll = 0xffffffffu;
+__device__ __forceinline__ bool group_lu(dfl (&a)[P], dfl b, int l, dfl (&x)[P]) {
   bool used = l >= P;                   // padding lanes never pivot
   bool ok = true;
   int prow[P];
-  double pinv[P];
+  dfl pinv[P];
 #pragma unroll
   for (int c = 0; c < P; ++c) {
-    double v = used ? -1.0 : fabs(a[c]);
+    float v = used ? -1.f : fabsf(a[c].hi);
     int idx = l;
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) {
-      const double ov = __shfl_xor_sync(kAll, v, off, G);
-      const int oi = __shfl_xor_sync(kAll, idx, off, G);
+      const float ov = __shfl_xor_sync(0xffffffffu, v, off, G);
+      const int oi = __shfl_xor_sync(0xffffffffu, idx, off, G);
       if (ov > v || (ov == v && oi < idx)) {
         v = ov;
         idx = oi;
       }
     }
-    ok = ok && (v > 0.0);
-    const double piv = __shfl_sync(kAll, a[c], idx, G);
-    const double pi = 1.0 / (piv != 0.0 ? piv : 1.0);
+    ok = ok && (v > 0.f);
+    const dfl piv = df_shfl(a[c], idx, G);
+    const dfl pi = df_rcp(piv.hi != 0.f ? piv : df_make(1.f));
     prow[c] = idx;
     pinv[c] = pi;
     const bool elim = !used && l != idx;
-    const double m = a[c] * pi;
+    const dfl m = df_mul(a[c], pi);
 #pragma unroll
     for (int k = c + 1; k < P; ++k) {
-      const double pk = __shfl_sync(kAll, a[k], idx, G);
-      if (elim) a[k] = fma(-m, pk, a[k]);
+      const dfl pk = df_shfl(a[k], idx, G);
+      if (elim) a[k] = df_fms(a[k], m, pk);
     }
-    const double pb = __shfl_sync(kAll, b, idx, G);
-    if (elim) b = fma(-m, pb, b);
+    const dfl pb = df_shfl(b, idx, G);
+    if (elim) b = df_fms(b, m, pb);
     used = used || l == idx;
   }
   // back substitution in pivot order: row prow[c] holds U[c][c..P-1]; every
   // lane folds each x_k into its rhs as soon as it is known
 #pragma unroll
   for (int c = P - 1; c >= 0; --c) {
-    x[c] = __shfl_sync(kAll, b * pinv[c], prow[c], G);
-    b = fma(-a[c], x[c], b);
+    x[c] = df_shfl(df_mul(b, pinv[c]), prow[c], G);
+    b = df_fms(b, a[c], x[c]);
   }
   return ok;
 }
 
 // theta (N, P) float64 in the derivative order [I, x, r]; writes theta_new
 // and |dtheta|.  lam (N) adds lam_j to the diagonal.  mask (nullable): atoms
-// with mask[j] == 0 keep their parameters.  One group of G lanes per atom.
+// with mask[j] == 0 keep their parameters.  One group of G lanes per atom;
+// after the solve lane l forms parameter l only.
 template <int P, int D, int G>
 __global__ void __launch_bounds__(128)
     gr_newton_solve_kernel(int n, const double *g, const double *H,
@@ -283,20 +283,24 @@ __global__ void __launch_bounds__(128)
   const bool live = j < n;
   const bool active = live && (mask == nullptr || mask[j] != 0);
   const bool row = live && l < P;
-  double a[P], b = 0.0, x[P];
-  double lj = row ? lam[j] : 0.0;
+  dfl a[P], b, x[P];
+  // the damped diagonal entry of row l, formed once
+  const dfl diag = row ? df_add(df_from_double(H[((size_t)j * P + l) * P + l]),
+                                df_from_double(lam[j]))
+                       : df_make(1.f);
   auto load = [&]() {
 #pragma unroll
     for (int k = 0; k < P; ++k)
-      a[k] = row ? H[((size_t)j * P + l) * P + k] + (k == l ? lj : 0.0) : (k == l ? 1.0 : 0.0);
-    b = row ? -g[(size_t)j * P + l] : 0.0;
+      a[k] = k == l ? diag
+                    : (row ? df_from_double(H[((size_t)j * P + l) * P + k]) : df_make(0.f));
+    b = row ? df_neg(df_from_double(g[(size_t)j * P + l])) : df_make(0.f);
   };
   load();
   bool ok = group_cholesky<P, G>(a, b, l, x);
   if (__any_sync(kAll, !ok)) {          // some group of this warp is not positive definite
     const bool chol_ok = ok;
     load();
-    double xl[P];
+    dfl xl[P];
     const bool lu_ok = group_lu<P, G>(a, b, l, xl);
     if (!chol_ok) {
       ok = lu_ok;
@@ -304,49 +308,54 @@ __global__ void __launch_bounds__(128)
       for (int k = 0; k < P; ++k) x[k] = xl[k];
     }
   }
-  ok = ok && active;
 #pragma unroll
   for (int k = 0; k < P; ++k)
-    if (!(x[k] == x[k]) || fabs(x[k]) > 1e30) ok = false;
-  double nrm = 0.0, th[P];
+    if (!(x[k].hi == x[k].hi) || fabsf(x[k].hi) > 1e30f) ok = false;
+  ok = ok && active;
+  // lane l: its step component and parameter
+  dfl mine = df_make(0.f);
 #pragma unroll
-  for (int k = 0; k < P; ++k) {
-    const double d = ok ? x[k] : 0.0;
-    nrm = fma(d, d, nrm);
-    th[k] = live ? theta[(size_t)j * P + k] : 0.0;
-    th[k] += d;
-  }
+  for (int k = 0; k < P; ++k)
+    if (k == l) mine = x[k];
+  const double d = (ok && row) ? df_to_double(mine) : 0.0;
+  double th = row ? theta[(size_t)j * P + l] : 0.0;
+  th += d;
+  // |dtheta| over the group, fixed butterfly order
+  double nrm = d * d;
+#pragma unroll
+  for (int off = 1; off < G; off <<= 1) nrm += __shfl_xor_sync(kAll, nrm, off, G);
+  // clamps of the reference's update: I >= 0, sign flips keeping
+  // diag(r) >= 0 (P fixes the kind: 4 / 5 isotropic 2D / 3D, 6 anisotropic
+  // 2D, 10 anisotropic 3D); a flip of r's diagonal entry i negates row i
+  const unsigned neg = __ballot_sync(kAll, th < 0.0) >> (t & 31 & ~(G - 1));
   if (ok) {
-    th[0] = th[0] < 0.0 ? 0.0 : th[0];
-    // sign flips keeping diag(r) >= 0; P fixes the kind: 4 / 5 isotropic
-    // 2D / 3D, 6 anisotropic 2D, 10 anisotropic 3D
-    double *r = th + 1 + D;
+    const int q = l - 1 - D;             // index in packed r
+    auto negr = [&](int i) { return ((neg >> (1 + D + i)) & 1u) != 0u; };
+    if (l == 0 && th < 0.0) th = 0.0;
     if constexpr (P == 4 || P == 5) {
-      r[0] = fabs(r[0]);
+      if (q == 0) th = fabs(th);
     } else if constexpr (P == 6) {
-      if (r[0] < 0) { r[0] = -r[0]; r[2] = -r[2]; }
-      if (r[1] < 0) r[1] = -r[1];
+      // packed [r00 r11 r01]: row 0 holds r00, r01
+      if ((q == 0 || q == 2) && negr(0)) th = -th;
+      if (q == 1 && negr(1)) th = -th;
     } else {
-      if (r[0] < 0) { r[0] = -r[0]; r[3] = -r[3]; r[5] = -r[5]; }
-      if (r[1] < 0) { r[1] = -r[1]; r[4] = -r[4]; }
-      if (r[2] < 0) r[2] = -r[2];
+      // packed [r00 r11 r22 r01 r12 r02]: row 0 holds r00 r01 r02, row 1 r11 r12
+      if ((q == 0 || q == 3 || q == 5) && negr(0)) th = -th;
+      if ((q == 1 || q == 4) && negr(1)) th = -th;
+      if (q == 2 && negr(2)) th = -th;
     }
   }
   if (!row) return;
-  double mine = 0.0;
-#pragma unroll
-  for (int k = 0; k < P; ++k)
-    if (k == l) mine = th[k];
-  theta_new[(size_t)j * P + l] = mine;
+  theta_new[(size_t)j * P + l] = th;
   if (l == 0) {
     step_norm[j] = sqrt(nrm);
     if (fail) fail[j] = (active && !ok) ? 1 : 0;
   }
   if (ao.I) {
     constexpr int PR = P - 1 - D;
-    if (l == 0) ao.I[j] = (float)mine;
-    else if (l <= D) ao.x[(size_t)j * D + l - 1] = (float)mine;
-    else ao.r[(size_t)j * PR + l - 1 - D] = (float)mine;
+    if (l == 0) ao.I[j] = (float)th;
+    else if (l <= D) ao.x[(size_t)j * D + l - 1] = (float)th;
+    else ao.r[(size_t)j * PR + l - 1 - D] = (float)th;
   }
 }
 
@@ -448,6 +457,15 @@ int launch_newton_solve(int dim, int iso, int n, const double *g, const double *
     gr_newton_solve_kernel<10, 3, 16><<<blocks(16), 128, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
+int preload_update() {
+  return preload_fn(gr_atom_update_kernel<1>) + preload_fn(gr_atom_update_kernel<2>) +
+         preload_fn(gr_sum_partials_kernel) + preload_fn(gr_newton_solve_kernel<4, 2, 8>) +
+         preload_fn(gr_newton_solve_kernel<6, 2, 8>) +
+         preload_fn(gr_newton_solve_kernel<5, 3, 8>) +
+         preload_fn(gr_newton_solve_kernel<10, 3, 16>) + preload_fn(gr_newton_accept_kernel) +
+         preload_fn(gr_accept_fields_kernel);
 }
 
 }  // namespace gr

@@ -241,4 +241,9 @@ int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
+int preload_volume() {
+  return preload_fn(gr_volproj_kernel<2, false>) + preload_fn(gr_volproj_kernel<3, false>) +
+         preload_fn(gr_volproj_kernel<2, true>) + preload_fn(gr_volproj_kernel<3, true>);
+}
+
 }  // namespace gr

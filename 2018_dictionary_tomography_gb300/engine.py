@@ -321,6 +321,14 @@ def newton_solve(dim, iso, g, H, lam, theta, mask=None):
 # ---------------------------------------------------------------------------
 # allocation-free forms with caller-owned buffers (CUDA-graph capturable)
 # ---------------------------------------------------------------------------
+def preload(device=None):
+    """Load every kernel of the library on ``device`` now (see gr_preload)."""
+    device = torch.device(device or "cuda")
+    _require_cuda(device)
+    with torch.cuda.device(device):
+        _lib.check(_lib.load().gr_preload(), "gr_preload")
+
+
 def workspace_bytes(op, atoms, geom):
     return int(_lib.load().gr_workspace_bytes(op, ctypes.byref(atoms.struct),
                                               ctypes.byref(geom.struct)))

@@ -384,6 +384,7 @@ def _warm_engine(device):
     capture."""
     if device in _warmed:
         return
+    engine.preload(device)
     for dim in (2, 3):
         th = np.linspace(0, 3, 3)
         T = np.stack([np.cos(th), np.sin(th)], 1)

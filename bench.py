@@ -530,6 +530,13 @@ def run_serving(args):
     cmp_reqs = wl.materialize_data(wl.config3_requests(n=args.compare, seed=3), dev)
     for r in cmp_reqs:
         r.arrival = 0.0
+    # one untimed pass of the same mix first: the first graph instantiations
+    # made while the GPU is loaded grow the driver's pools (about 1 ms each,
+    # once per process), which a running server has long paid
+    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31)
+    for r in cmp_reqs:
+        srv.submit(r)
+    srv.run()
     t0 = time.perf_counter()
     srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31)
     for r in cmp_reqs:

@@ -86,6 +86,14 @@ enum { GR_OP_PROJECT = 0, GR_OP_DERIVS_1 = 1, GR_OP_DERIVS_2 = 2, GR_OP_ATOM_STE
 /* Library version (major*10000 + minor*100 + patch). */
 int gr_version(void);
 
+/* Loads the code of every kernel of the library on the current device now.
+ * CUDA loads modules lazily by default, so without this a kernel's first
+ * launch, or the first instantiation of a graph that holds it, pays the load
+ * while the caller's other work waits (a serving process calls it once at
+ * start).  No reference counterpart: the reference compiles its kernels on
+ * first call instead.  GR_ERR_LAUNCH if a kernel cannot be loaded. */
+int gr_preload(void);
+
 /* Static description of a status code. */
 const char *gr_status_string(int status);
 
