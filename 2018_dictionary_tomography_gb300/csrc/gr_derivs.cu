@@ -22,7 +22,7 @@
 // angles of each atom split over several lanes), and loops over a chunk of
 // angles.  Gradients are accumulated per lane with compensated FP32 sums,
 // Hessians in FP32; lanes sharing an atom are combined by a fixed-order
-// butterfly; chunk partials are summed in FP64 in chunk order by
+// butterfly; chunk partials are summed (compensated) in chunk order by
 // gr_deriv_finalize_kernel, which also applies the isotropic chain rule.
 // No float atomics anywhere: results are bitwise reproducible.
 #include "gr_assembly.cuh"
@@ -494,10 +494,10 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// Sum chunk partials (FP64) in chunk order, expand the packed Hessian and
+// Sum chunk partials (compensated) in chunk order, expand the packed Hessian and
 // apply the isotropic chain rule r_aniso = (s, .., s, 0, ..).  A block covers
 // 32 atoms; its 8 warps share out the partial values (reads of consecutive
-// atoms are coalesced), then warp 0 finishes the atoms.
+// atoms are coalesced), then all its threads write the atoms' outputs.
 constexpr int kRedSlices = 8;
 template <int K>
 __global__ void __launch_bounds__(32 * kRedSlices)
@@ -507,59 +507,86 @@ __global__ void __launch_bounds__(32 * kRedSlices)
   constexpr int D = K + 1;
   constexpr int P = n_par<K>();
   constexpr int QN = 1 + P + P * (P + 1) / 2;
-  // chunk sums in FP64 in chunk order: thread (atom, ty) sums values
-  // q = ty, ty + kRedSlices, ... of its atom, all loads independent
+  // chunk sums in chunk order: thread (atom, ty) sums values q = ty,
+  // ty + kRedSlices, ... of its atom, all loads independent.  The sum is
+  // compensated (Neumaier) in FP32 and carried as a float pair, about twice
+  // FP32 precision, then converted to FP64 once: an FP64 add per partial
+  // would queue on the SM's narrow FP64 pipe (16 cycles per warp
+  // instruction on this GPU).
   __shared__ double vs[QN][32];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int slot = blockIdx.x * 32 + tx;
   if (slot < n)
     for (int q = ty; q < cfg.qn; q += kRedSlices) {
-      double t = 0.0;
+      float sm = 0.f, cm = 0.f;
 #pragma unroll 4
-      for (int c = 0; c < cfg.nchunks; ++c) t += (double)part[((size_t)c * cfg.qn + q) * n + slot];
-      vs[q][tx] = t;
+      for (int c = 0; c < cfg.nchunks; ++c) {
+        const float v = part[((size_t)c * cfg.qn + q) * n + slot];
+        const float tt = __fadd_rn(sm, v);
+        cm += (fabsf(sm) >= fabsf(v)) ? __fadd_rn(__fsub_rn(sm, tt), v)
+                                      : __fadd_rn(__fsub_rn(v, tt), sm);
+        sm = tt;
+      }
+      vs[q][tx] = (double)sm + (double)cm;
     }
   __syncthreads();
-  if (ty != 0 || slot >= n) return;
-  double v[QN];
-  for (int q = 0; q < cfg.qn; ++q) v[q] = vs[q][tx];
-  const int j = order ? order[slot] : slot;  // atom of the slot
-  double f = v[0] + (f_extra ? f_extra[0] : 0.0);
-  double H[P][P];
-  if (deriv_order > 1) {
-    int o = 1 + P;
-    for (int a = 0; a < P; ++a)
-      for (int b = a; b < P; ++b, ++o) {
-        H[a][b] = v[o];
-        H[b][a] = v[o];
-      }
-  }
-  out.f[j] = f;
+  // outputs of the block's atoms, written by all threads from the sums
+  // (consecutive threads write consecutive entries of an atom's block)
+  const int nb = min(32, n - (int)blockIdx.x * 32);
+  auto atom_of = [&](int t) {
+    const int sl = blockIdx.x * 32 + t;
+    return order ? order[sl] : sl;
+  };
+  // entry (a, b) of the full Hessian from the packed upper triangle
+  auto hv = [&](int a, int b, int t) -> double {
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    return vs[1 + P + lo * P - lo * (lo - 1) / 2 + (hi - lo)][t];
+  };
+  const double fx = f_extra ? f_extra[0] : 0.0;
   if (!r_iso) {
-    for (int a = 0; a < P; ++a) out.g[(size_t)j * P + a] = v[1 + a];
+    for (int e = threadIdx.x; e < nb * (1 + P); e += blockDim.x) {
+      const int t = e / (1 + P), q = e - t * (1 + P);
+      const int j = atom_of(t);
+      if (q == 0) out.f[j] = vs[0][t] + fx;
+      else out.g[(size_t)j * P + q - 1] = vs[q][t];
+    }
     if (deriv_order > 1)
-      for (int a = 0; a < P; ++a)
-        for (int b = 0; b < P; ++b) out.H[((size_t)j * P + a) * P + b] = H[a][b];
+      for (int e = threadIdx.x; e < nb * P * P; e += blockDim.x) {
+        const int t = e / (P * P), ab = e - t * (P * P), a = ab / P, b = ab - a * P;
+        out.H[(size_t)atom_of(t) * P * P + ab] = hv(a, b, t);
+      }
     return;
   }
   // isotropic: parameters (I, x, s); s maps to the D diagonal r entries
+  // (r_aniso = (s, .., s, 0, ..)), so its derivatives sum those entries'
   constexpr int PI = 2 + D;
-  double gi[PI];
-  for (int a = 0; a <= D; ++a) gi[a] = v[1 + a];
-  gi[1 + D] = 0.0;
-  for (int q = 0; q < D; ++q) gi[1 + D] += v[1 + 1 + D + q];
-  for (int a = 0; a < PI; ++a) out.g[(size_t)j * PI + a] = gi[a];
-  if (deriv_order > 1) {
-    auto src = [&](int a, int q) { return a < 1 + D ? a : 1 + D + q; };
-    for (int a = 0; a < PI; ++a)
-      for (int b = 0; b < PI; ++b) {
-        const int na = a < 1 + D ? 1 : D, nb = b < 1 + D ? 1 : D;
-        double s = 0.0;
-        for (int qa = 0; qa < na; ++qa)
-          for (int qb = 0; qb < nb; ++qb) s += H[src(a, qa)][src(b, qb)];
-        out.H[((size_t)j * PI + a) * PI + b] = s;
+  auto src = [](int a, int q) { return a < 1 + D ? a : 1 + D + q; };
+  for (int e = threadIdx.x; e < nb * (1 + PI); e += blockDim.x) {
+    const int t = e / (1 + PI), q = e - t * (1 + PI);
+    const int j = atom_of(t);
+    if (q == 0) {
+      out.f[j] = vs[0][t] + fx;
+    } else {
+      const int a = q - 1;
+      double gsum = 0.0;
+      if (a <= D) {
+        gsum = vs[1 + a][t];
+      } else {
+#pragma unroll
+        for (int qq = 0; qq < D; ++qq) gsum += vs[1 + 1 + D + qq][t];
       }
+      out.g[(size_t)j * PI + a] = gsum;
+    }
   }
+  if (deriv_order > 1)
+    for (int e = threadIdx.x; e < nb * PI * PI; e += blockDim.x) {
+      const int t = e / (PI * PI), ab = e - t * (PI * PI), a = ab / PI, b = ab - a * PI;
+      const int na = a < 1 + D ? 1 : D, nbb = b < 1 + D ? 1 : D;
+      double hs = 0.0;
+      for (int qa = 0; qa < na; ++qa)
+        for (int qb = 0; qb < nbb; ++qb) hs += hv(src(a, qa), src(b, qb), t);
+      out.H[(size_t)atom_of(t) * PI * PI + ab] = hs;
+    }
 }
 
 // 1/2 sum C^2 helper: block partial sums (FP32 compensated per thread, FP64
