@@ -235,8 +235,14 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
   }
 }
 
-template <int K, int ORDER>
-__global__ void __launch_bounds__(128, ORDER == 1 ? 5 : 1)
+// ONE: the work split gives every lane at most one angle of its atom (every
+// Hessian split of up to ~32 angles per chunk, which covers the tilt series
+// and the served fits): the angle loop runs at most once, so the per-lane
+// accumulators need not live across the whole pair computation, which cuts
+// the Hessian kernel from 255 to 168 registers (3 resident blocks per SM
+// instead of 2).
+template <int K, int ORDER, bool ONE>
+__global__ void __launch_bounds__(128, ORDER == 1 ? 5 : (ONE ? 3 : 1))
     gr_deriv_kernel(Atoms at, Geom g, DerivIn in, DerivCfg cfg, float *part) {
   constexpr int D = K + 1;
   constexpr int PR = n_rparam<K>();
@@ -288,6 +294,7 @@ __global__ void __launch_bounds__(128, ORDER == 1 ? 5 : 1)
       float Z[NPSI][NPSI];
       accumulate_pair<K, ORDER>(p, fr, I, Aa, Z, Z, gacc, hacc);
     }
+    if constexpr (ONE) break;
   }
 
   // combine lanes sharing an atom (fixed butterfly order), then write
@@ -701,12 +708,27 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
       if (in.order == 1) gr_psf_deriv_kernel<2, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part, s);
       else gr_psf_deriv_kernel<2, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part, s);
     }
-  } else if (K == 1) {
-    if (in.order == 1) gr_deriv_kernel<1, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
-    else gr_deriv_kernel<1, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
   } else {
-    if (in.order == 1) gr_deriv_kernel<2, 1><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
-    else gr_deriv_kernel<2, 2><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+    // at most one angle per lane: a lane's angles a_lo + sub + k sg lie
+    // below a_lo + ch
+    const bool one = c.ch <= c.sg;
+    if (K == 1) {
+      if (in.order == 1) {
+        if (one) gr_deriv_kernel<1, 1, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+        else gr_deriv_kernel<1, 1, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+      } else {
+        if (one) gr_deriv_kernel<1, 2, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+        else gr_deriv_kernel<1, 2, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+      }
+    } else {
+      if (in.order == 1) {
+        if (one) gr_deriv_kernel<2, 1, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+        else gr_deriv_kernel<2, 1, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+      } else {
+        if (one) gr_deriv_kernel<2, 2, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+        else gr_deriv_kernel<2, 2, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+      }
+    }
   }
   timer_mark(2, 1, stream);
   const int fblocks = (at.n + 31) / 32;
@@ -721,8 +743,10 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
 }
 
 int preload_derivs() {
-  return preload_fn(gr_deriv_kernel<1, 1>) + preload_fn(gr_deriv_kernel<1, 2>) +
-         preload_fn(gr_deriv_kernel<2, 1>) + preload_fn(gr_deriv_kernel<2, 2>) +
+  return preload_fn(gr_deriv_kernel<1, 1, false>) + preload_fn(gr_deriv_kernel<1, 2, false>) +
+         preload_fn(gr_deriv_kernel<2, 1, false>) + preload_fn(gr_deriv_kernel<2, 2, false>) +
+         preload_fn(gr_deriv_kernel<1, 1, true>) + preload_fn(gr_deriv_kernel<1, 2, true>) +
+         preload_fn(gr_deriv_kernel<2, 1, true>) + preload_fn(gr_deriv_kernel<2, 2, true>) +
          preload_fn(gr_psf_deriv_kernel<1, 1>) + preload_fn(gr_psf_deriv_kernel<1, 2>) +
          preload_fn(gr_psf_deriv_kernel<2, 1>) + preload_fn(gr_psf_deriv_kernel<2, 2>) +
          preload_fn(gr_deriv_finalize_kernel<1>) + preload_fn(gr_deriv_finalize_kernel<2>) +
