@@ -35,6 +35,7 @@ struct DerivCfg {
   int ch;       // angles per chunk
   int nchunks;
   int qn;       // partial values per atom
+  int rs;       // lanes sharing one (atom, angle) pair's cells (power of two)
 };
 
 inline int next_pow2(int v) {
@@ -56,17 +57,30 @@ int g_deriv_min_angles = 1;
 // warp for Hessians and for long angle series, else four (so each lane still
 // has a few angles to amortise the warp's closing reduction).
 int g_deriv_atoms_per_warp = 0;
+// Problems with few (atom, angle) pairs split each pair's cells over rs
+// lanes (rows of a 3D box, chunks of kRowChunk cells of a 2D one), rs the
+// largest power of two up to 8 with pairs * rs <= g_deriv_split_lanes; the
+// lanes' moment sums are combined before one of them does the chain-rule
+// assembly.  A pair's cell walk is otherwise one lane's serial loop, which
+// sets the kernel time when there are too few pairs to fill the GPU and
+// their boxes are large.  0: never split.
+int g_deriv_split_lanes = 65536;
 
-inline DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order) {
+inline DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order, bool split = true) {
   DerivCfg c;
   c.ag = next_pow2(n_atoms < 1 ? 1 : n_atoms);
   const int ag_cap = g_deriv_atoms_per_warp > 0 ? g_deriv_atoms_per_warp
                      : (order > 1 || n_angles >= 1024) ? 1 : 4;
   if (c.ag > ag_cap) c.ag = ag_cap;
   c.sg = 32 / c.ag;
+  const long long pairs = (long long)(n_atoms < 1 ? 1 : n_atoms) * (n_angles < 1 ? 1 : n_angles);
+  c.rs = 1;
+  while (split && g_deriv_split_lanes > 0 && c.rs < 8 && c.rs < c.sg &&
+         pairs * c.rs * 2 <= (long long)g_deriv_split_lanes)
+    c.rs <<= 1;
   const int warps_atoms = (n_atoms + c.ag - 1) / c.ag;
   int nch = (g_deriv_target_warps + warps_atoms - 1) / warps_atoms;
-  const int per = c.sg * (g_deriv_min_angles < 1 ? 1 : g_deriv_min_angles);
+  const int per = (c.sg / c.rs) * (g_deriv_min_angles < 1 ? 1 : g_deriv_min_angles);
   const int max_ch = (n_angles + per - 1) / per;
   if (nch > max_ch) nch = max_ch;
   if (nch < 1) nch = 1;
@@ -89,7 +103,8 @@ struct PairMoments {
 template <int K, int DEG, bool GN>
 __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
                                              const DerivIn &in, int a, float I,
-                                             PairMoments<K, DEG, GN> &mo) {
+                                             PairMoments<K, DEG, GN> &mo, int phase = 0,
+                                             int rs = 1) {
   constexpr int NM = n_mom<K, DEG>();
 #pragma unroll
   for (int i = 0; i < NM; ++i) {
@@ -120,7 +135,7 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
     // values and coordinates are loaded together first (one cell per load
     // round trip would leave the lane waiting on every cell)
     const int c_hi = p.hi[0];
-    for (int kb = p.lo[0]; kb <= c_hi; kb += kRowChunk) {
+    for (int kb = p.lo[0] + phase * kRowChunk; kb <= c_hi; kb += rs * kRowChunk) {
       float cv[kRowChunk], pv[kRowChunk], bv[GN ? kRowChunk : 1];
 #pragma unroll
       for (int i = 0; i < kRowChunk; ++i) {
@@ -160,7 +175,7 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
       }
     }
   } else {
-    for (int k0 = p.lo[0]; k0 <= p.hi[0]; ++k0) {
+    for (int k0 = p.lo[0] + phase; k0 <= p.hi[0]; k0 += rs) {
       const float d0 = (__ldg(g.ax[0].coords + k0) - p.qh[0]) - p.ql[0];
       {
         const float t0 = p.G[0] * d0 * d0;
@@ -273,26 +288,42 @@ __global__ void __launch_bounds__(128, ORDER == 1 ? 5 : (ONE ? 3 : 1))
 #pragma unroll
   for (int i = 0; i < (ORDER > 1 ? NH : 1); ++i) hacc[i] = 0.f;
 
-  for (int a = a_lo + sub; a < a_hi && valid; a += cfg.sg) {
+  // lanes sharing a pair (cfg.rs of them, sub = s rs + phase) walk its rows
+  // phase, phase + rs, ... and combine their moment sums
+  const int phase = sub & (cfg.rs - 1);
+  unsigned gmask = 0u;
+  for (int o = 0; o < cfg.rs; ++o) gmask |= 1u << (lane + (o - phase) * cfg.ag);
+  for (int a = a_lo + sub / cfg.rs; a < a_hi && valid; a += cfg.sg / cfg.rs) {
     Frame<K> fr;
     load_frame<K>(g.frames, a, fr);
     Pair<K> p;
     pair_setup<K>(at, jj, fr, g, p);
     PairMoments<K, DEG, GN> mo;
-    pair_moments<K, DEG, GN>(p, g, in, a, I, mo);
-    float Aa[NPSI];
-    first_psi<K, n_mom<K, DEG>()>(mo.Ma, p.G, Aa);
-    // value
-    if (in.mode == kModeInner) f += I * mo.Ma[0];
-    else if (in.mode == kModeL2Atom) f += I * (0.5f * I * mo.Y0 - mo.X0);
-    if constexpr (ORDER > 1) {
-      float Ba[NPSI][NPSI], Bb[NPSI][NPSI];
-      psi_gram<K, true>(mo.Ma, p.G, Ba);
-      psi_gram<K, false>(mo.Mb, p.G, Bb);
-      accumulate_pair<K, ORDER>(p, fr, I, Aa, Ba, Bb, gacc, hacc);
-    } else {
-      float Z[NPSI][NPSI];
-      accumulate_pair<K, ORDER>(p, fr, I, Aa, Z, Z, gacc, hacc);
+    pair_moments<K, DEG, GN>(p, g, in, a, I, mo, phase, cfg.rs);
+    for (int o = 1; o < cfg.rs; o <<= 1) {
+#pragma unroll
+      for (int q = 0; q < n_mom<K, DEG>(); ++q) {
+        mo.Ma[q] += __shfl_xor_sync(gmask, mo.Ma[q], o * cfg.ag);
+        if (GN) mo.Mb[q] += __shfl_xor_sync(gmask, mo.Mb[q], o * cfg.ag);
+      }
+      mo.X0 += __shfl_xor_sync(gmask, mo.X0, o * cfg.ag);
+      mo.Y0 += __shfl_xor_sync(gmask, mo.Y0, o * cfg.ag);
+    }
+    if (phase == 0) {
+      float Aa[NPSI];
+      first_psi<K, n_mom<K, DEG>()>(mo.Ma, p.G, Aa);
+      // value
+      if (in.mode == kModeInner) f += I * mo.Ma[0];
+      else if (in.mode == kModeL2Atom) f += I * (0.5f * I * mo.Y0 - mo.X0);
+      if constexpr (ORDER > 1) {
+        float Ba[NPSI][NPSI], Bb[NPSI][NPSI];
+        psi_gram<K, true>(mo.Ma, p.G, Ba);
+        psi_gram<K, false>(mo.Mb, p.G, Bb);
+        accumulate_pair<K, ORDER>(p, fr, I, Aa, Ba, Bb, gacc, hacc);
+      } else {
+        float Z[NPSI][NPSI];
+        accumulate_pair<K, ORDER>(p, fr, I, Aa, Z, Z, gacc, hacc);
+      }
     }
     if constexpr (ONE) break;
   }
@@ -657,13 +688,18 @@ int set_tuning(int key, int value) {
     g_proj_split_cells = value;
     return kOk;
   }
+  if (key == 6 && value >= 0) {
+    g_deriv_split_lanes = value;
+    return kOk;
+  }
   return kErrArg;
 }
 
 int get_tuning(int key) {
   return key == 0 ? g_deriv_target_warps : key == 1 ? g_deriv_min_angles
          : key == 2 ? g_deriv_atoms_per_warp : key == 3 ? g_proj_form
-         : key == 4 ? g_proj_split_cells : -1;
+         : key == 4 ? g_proj_split_cells
+         : key == 6 ? g_deriv_split_lanes : -1;
 }
 
 size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order) {
@@ -679,7 +715,9 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
   const int K = g.K;
   if (at.n <= 0) return kOk;
   if (in.order < 1 || in.order > 2) return kErrArg;
-  DerivCfg c = deriv_cfg(K, at.n, g.n_angles, in.order);
+  // the pixel-integrated kernel walks whole pairs per lane (no cell split);
+  // its chunking never needs more workspace than the split one
+  DerivCfg c = deriv_cfg(K, at.n, g.n_angles, in.order, !in.psf);
   if (ws == nullptr || ws_bytes < derivs_workspace_bytes(K, at.n, g.n_angles, in.order))
     return kErrWorkspace;
   char *wp = static_cast<char *>(ws);
@@ -711,7 +749,7 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
   } else {
     // at most one angle per lane: a lane's angles a_lo + sub + k sg lie
     // below a_lo + ch
-    const bool one = c.ch <= c.sg;
+    const bool one = c.ch <= c.sg / c.rs;
     if (K == 1) {
       if (in.order == 1) {
         if (one) gr_deriv_kernel<1, 1, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);

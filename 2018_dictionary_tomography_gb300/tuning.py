@@ -41,6 +41,16 @@ def set_projection_split(cells):
     _lib.check(_lib.load().gr_set_tuning(4, int(cells)), "gr_set_tuning")
 
 
+def set_derivative_split(lanes):
+    """Problems with fewer (atom, angle) pairs than ``lanes`` split each
+    pair's cells over 2, 4 or 8 lanes of the derivative kernel (0: never)."""
+    _lib.check(_lib.load().gr_set_tuning(6, int(lanes)), "gr_set_tuning")
+
+
+def get_derivative_split():
+    return int(_lib.load().gr_get_tuning(6))
+
+
 def get_projection_split():
     return int(_lib.load().gr_get_tuning(4))
 

@@ -266,10 +266,13 @@ unsigned long long gr_launch_count(void);
  * GR_TUNE_PROJ_SPLIT_CELLS: 3D problems with fewer detector cells over all
  * angles than this (default 4194304; 0 = never) split each tile's atoms over
  * the four warps of a block, which shortens the slowest tile when there are
- * too few tiles to fill the GPU.  Set them before
+ * too few tiles to fill the GPU.  GR_TUNE_DERIV_SPLIT_LANES: problems with
+ * fewer (atom, angle) pairs than this split each pair's cells over 2, 4 or 8
+ * lanes of the point-sampled derivative kernel (the largest split with
+ * pairs x lanes <= value; default 65536; 0 = never).  Set them before
  * gr_workspace_bytes and keep them fixed while launches that used the old
  * values are in flight.  Results do not depend on them beyond FP rounding of
- * the derivative chunk sums and of a split tile's combined cell sums (the
+ * the derivative chunk and lane sums and of a split tile's combined cell sums (the
  * tiling leaves projections bitwise equal).  gr_set_tuning returns
  * GR_ERR_ARG for an unknown key or out-of-range value; gr_get_tuning returns
  * the current value (-1 for an unknown key).
@@ -279,7 +282,8 @@ enum {
   GR_TUNE_DERIV_MIN_ANGLES = 1,
   GR_TUNE_DERIV_ATOMS_PER_WARP = 2,
   GR_TUNE_PROJ_TILING = 3,
-  GR_TUNE_PROJ_SPLIT_CELLS = 4
+  GR_TUNE_PROJ_SPLIT_CELLS = 4,
+  GR_TUNE_DERIV_SPLIT_LANES = 6
 };
 int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);

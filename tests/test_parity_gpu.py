@@ -181,6 +181,7 @@ def test_work_split_does_not_change_results(eng, cuda_ready, case):
     geom, atoms = engine_geometry(g), engine_atoms(I, x, r)
     field = torch.from_numpy(go.radproj(I, x, r, g) * 0.9).float().cuda()
     saved = tuning.get_split()
+    saved_lanes = tuning.get_derivative_split()
     try:
         f0, g0, H0 = eng.atom_derivs(atoms, geom, "inner", field, order=2)
         for split in ((1024, 1, 1), (32768, 2, 2), (4096, 1, 8), (65536, 4, 0)):
@@ -188,8 +189,18 @@ def test_work_split_does_not_change_results(eng, cuda_ready, case):
             f1, g1, H1 = eng.atom_derivs(atoms, geom, "inner", field, order=2)
             assert entry_relerr(g1.cpu().numpy(), g0.cpu().numpy()) < 1e-6
             assert entry_relerr(H1.cpu().numpy(), H0.cpu().numpy()) < 1e-6
+        tuning.set_split(*saved)
+        # cells of a pair walked by 8 (default here), 2 or 1 lanes
+        npairs = len(I) * g.shape[0]
+        for lanes in (0, 2 * npairs):
+            tuning.set_derivative_split(lanes)
+            f1, g1, H1 = eng.atom_derivs(atoms, geom, "inner", field, order=2)
+            assert relerr(f1.cpu().numpy(), f0.cpu().numpy()) < 1e-6
+            assert entry_relerr(g1.cpu().numpy(), g0.cpu().numpy()) < 1e-6
+            assert entry_relerr(H1.cpu().numpy(), H0.cpu().numpy()) < 1e-6
     finally:
         tuning.set_split(*saved)
+        tuning.set_derivative_split(saved_lanes)
 
 
 def test_projection_tiling_is_bitwise_neutral(eng, cuda_ready):
