@@ -47,6 +47,16 @@ def set_derivative_split(lanes):
     _lib.check(_lib.load().gr_set_tuning(6, int(lanes)), "gr_set_tuning")
 
 
+def set_one_angle_budget(mb):
+    """Give every derivative lane at most one angle whenever the chunk
+    partials then fit in ``mb`` MB (0: keep the target-warps split)."""
+    _lib.check(_lib.load().gr_set_tuning(7, int(mb)), "gr_set_tuning")
+
+
+def get_one_angle_budget():
+    return int(_lib.load().gr_get_tuning(7))
+
+
 def get_derivative_split():
     return int(_lib.load().gr_get_tuning(6))
 

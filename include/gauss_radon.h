@@ -269,7 +269,10 @@ unsigned long long gr_launch_count(void);
  * too few tiles to fill the GPU.  GR_TUNE_DERIV_SPLIT_LANES: problems with
  * fewer (atom, angle) pairs than this split each pair's cells over 2, 4 or 8
  * lanes of the point-sampled derivative kernel (the largest split with
- * pairs x lanes <= value; default 65536; 0 = never).  Set them before
+ * pairs x lanes <= value; default 65536; 0 = never).  GR_TUNE_DERIV_ONE_MB:
+ * take enough angle chunks that every lane has at most one angle whenever the
+ * chunk partials then fit in this many MB of workspace (default 1024; 0 =
+ * keep GR_TUNE_DERIV_WARPS).  Set them before
  * gr_workspace_bytes and keep them fixed while launches that used the old
  * values are in flight.  Results do not depend on them beyond FP rounding of
  * the derivative chunk and lane sums and of a split tile's combined cell sums (the
@@ -283,7 +286,8 @@ enum {
   GR_TUNE_DERIV_ATOMS_PER_WARP = 2,
   GR_TUNE_PROJ_TILING = 3,
   GR_TUNE_PROJ_SPLIT_CELLS = 4,
-  GR_TUNE_DERIV_SPLIT_LANES = 6
+  GR_TUNE_DERIV_SPLIT_LANES = 6,
+  GR_TUNE_DERIV_ONE_MB = 7
 };
 int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);

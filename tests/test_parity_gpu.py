@@ -182,8 +182,10 @@ def test_work_split_does_not_change_results(eng, cuda_ready, case):
     field = torch.from_numpy(go.radproj(I, x, r, g) * 0.9).float().cuda()
     saved = tuning.get_split()
     saved_lanes = tuning.get_derivative_split()
+    saved_one = tuning.get_one_angle_budget()
     try:
         f0, g0, H0 = eng.atom_derivs(atoms, geom, "inner", field, order=2)
+        tuning.set_one_angle_budget(0)          # let the target-warps splits take effect
         for split in ((1024, 1, 1), (32768, 2, 2), (4096, 1, 8), (65536, 4, 0)):
             tuning.set_split(*split)
             f1, g1, H1 = eng.atom_derivs(atoms, geom, "inner", field, order=2)
@@ -201,6 +203,7 @@ def test_work_split_does_not_change_results(eng, cuda_ready, case):
     finally:
         tuning.set_split(*saved)
         tuning.set_derivative_split(saved_lanes)
+        tuning.set_one_angle_budget(saved_one)
 
 
 def test_projection_tiling_is_bitwise_neutral(eng, cuda_ready):
