@@ -430,4 +430,36 @@ __device__ __forceinline__ void sum_partials_warp(const double *part, int n, dou
   if (lane == 0) *out = t;
 }
 
+// The same with all NW warps of a block (every thread calls it): thread k
+// keeps 4 running sums over elements k + NW*32*(4 i + s); the threads' sums
+// are combined pairwise, across each warp, then across the warps in order.
+template <int NW>
+__device__ __forceinline__ void sum_partials_block(const double *part, int n, double *out) {
+  constexpr int T = NW * 32;
+  constexpr int kSums = 4;
+  __shared__ double ws[NW];
+  const int tid = threadIdx.x;
+  double s[kSums];
+#pragma unroll
+  for (int k = 0; k < kSums; ++k) s[k] = 0.0;
+  for (int base = 0; base < n; base += T * kSums) {
+#pragma unroll
+    for (int k = 0; k < kSums; ++k) {
+      const int i = base + T * k + tid;
+      if (i < n) s[k] += __ldcg(part + i);
+    }
+  }
+  s[0] += s[1];
+  s[2] += s[3];
+  const double t = warp_sum_d(s[0] + s[2]);
+  if ((tid & 31) == 0) ws[tid >> 5] = t;
+  __syncthreads();
+  if (tid == 0) {
+    double tot = 0.0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) tot += ws[w];
+    *out = tot;
+  }
+}
+
 }  // namespace gr

@@ -319,24 +319,25 @@ __global__ void __launch_bounds__(kProjWarps * 32)
 }
 
 // 2D sinograms: atom footprints are a few cells wide, so a block owns a tile
-// of 32 consecutive cells of one angle, one cell per lane.  The tile's
-// bitmap words are split into NW consecutive ranges, one per warp (4 warps,
-// 8 for long atom lists), so a tile's atoms are walked by NW warps at once; each warp keeps its
-// partial cell sums in registers.  Pair data of up to 32 listed atoms is
-// computed in parallel (one atom per lane) and staged in shared memory; every
-// lane then walks the batch in atom order and adds the atoms whose support
-// box holds its cell.  The warps' partial sums are combined in warp order
-// with a compensated sum: results are bitwise reproducible.
+// of 32 consecutive cells of one angle, one cell per lane of every warp.  The
+// tile's atoms come from its bitmap in index order, in passes: a pass lists
+// as many whole bitmap words as fit in NW*32 entries (block-wide prefix sum
+// of the words' bit counts), every thread sets up the pair data of one listed
+// atom in shared memory, and warp w adds the atoms of the w-th of NW
+// contiguous slices of the pass's list to its lane's cell, in list order, in
+// registers (compensated).  The warps' partial sums are combined in warp
+// order: results depend only on the atoms listed, bitwise reproducible.
 template <bool KAHAN, int NW>
 __global__ void __launch_bounds__(NW * 32)
     gr_project1d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
                         int W, ProjOut out, double *loss_out, int *done) {
-  __shared__ float4 prm[NW][32][2];
-  __shared__ int lists[NW][kListWords * 32];
+  constexpr int T = NW * 32;
+  __shared__ float4 prm[T][2];
+  __shared__ int list[T];
+  __shared__ int wsum[NW];
   __shared__ float parts[NW][2][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int item = blockIdx.x;
-  int *list = lists[warp];
   const int a = item / tc.ntiles, t = item - a * tc.ntiles;
   const int D0 = g.ax[0].n;
   const int cell = t * tc.t0 + lane;
@@ -346,113 +347,121 @@ __global__ void __launch_bounds__(NW * 32)
   float acc = 0.f, cmp = 0.f;
 
   const uint32_t *words = bitmap + (size_t)item * W;
-  const int wq = (W + NW - 1) / NW;
-  const int w_lo = warp * wq, w_hi = min(W, w_lo + wq);
-  for (int wb = w_lo; wb < w_hi; wb += kListWords) {
-    const int wi = wb + (lane < kListWords ? lane : 0);
-    uint32_t wd = (lane < kListWords && wi < w_hi) ? words[wi] : 0u;
-    int cnt = __popc(wd), incl = cnt;
+  for (int wb = 0; wb < W;) {
+    // thread k holds word wb + k; inclusive prefix of the bit counts
+    const int wi = wb + (int)threadIdx.x;
+    uint32_t wd = wi < W ? words[wi] : 0u;
+    const int cnt = __popc(wd);
+    int incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      int v = __shfl_up_sync(0xffffffffu, incl, o);
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += v;
     }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    int pos = incl - cnt;
-    while (wd) {
-      const int b = __ffs(wd) - 1;
-      list[pos++] = (wi << 5) + b;
-      wd &= wd - 1;
-    }
-    __syncwarp();
-    for (int bs = 0; bs < total; bs += 32) {
-      const int idx = bs + lane;
-      float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f);
-      float4 p1 = make_float4(__int_as_float(1), __int_as_float(0), 0.f, 0.f);
-      if (idx < total) {
-        Pair<1> p;
-        pair_setup<1>(at, list[idx], f, g, p);
-        p0 = make_float4(p.qh[0], p.ql[0], p.G[0], p.l2amp);
-        p1 = make_float4(__int_as_float(p.lo[0]), __int_as_float(p.hi[0]), p.sgn, 0.f);
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < NW; ++w)
+      if (w < warp) incl += wsum[w];
+    // the words that fit form a prefix (incl never decreases); one word
+    // always fits (a word holds at most 32 <= T atoms)
+    const bool take = incl <= T;
+    const int pos = incl - cnt;
+    if (take)
+      for (int p = pos; wd; ++p) {
+        list[p] = (wi << 5) + (__ffs(wd) - 1);
+        wd &= wd - 1;
       }
-      prm[warp][lane][0] = p0;
-      prm[warp][lane][1] = p1;
-      __syncwarp();
-      const int nb = min(32, total - bs);
+    const int ntake = __syncthreads_count(take && wi < W);
+    // entries listed: the inclusive count of the last word taken
+    int total = 0;
+    if (ntake > 0 && (int)threadIdx.x == ntake - 1) wsum[0] = incl;
+    __syncthreads();
+    total = wsum[0];
+    wb += ntake > 0 ? ntake : W;   // ntake = 0 only past the last word
+    // pair data of the listed atoms, one per thread
+    if ((int)threadIdx.x < total) {
+      Pair<1> p;
+      pair_setup<1>(at, list[threadIdx.x], f, g, p);
+      prm[threadIdx.x][0] = make_float4(p.qh[0], p.ql[0], p.G[0], p.l2amp);
+      prm[threadIdx.x][1] = make_float4(__int_as_float(p.lo[0]), __int_as_float(p.hi[0]), p.sgn, 0.f);
+    }
+    __syncthreads();
+    // warp w: slice [w total / NW, (w + 1) total / NW) in list order
+    const int s_lo = (warp * total) / NW, s_hi = ((warp + 1) * total) / NW;
 #pragma unroll 4
-      for (int s2 = 0; s2 < nb; ++s2) {
-        const float4 q0 = prm[warp][s2][0];
-        const float4 q1 = prm[warp][s2][1];
-        const int lo = __float_as_int(q1.x), hi = __float_as_int(q1.y);
-        if (cell >= lo && cell <= hi) {
-          const float d = (pc - q0.x) - q0.y;
-          const float m = q0.z * d * d;
-          if (m <= 1.f) {
-            const float v = q1.z * ex2_approx(fmaf(m, kNegThirtyLog2e, q0.w));
-            if (KAHAN) {
-              const float tt = acc + v;
-              cmp += (fabsf(acc) >= fabsf(v)) ? ((acc - tt) + v) : ((v - tt) + acc);
-              acc = tt;
-            } else {
-              acc += v;
-            }
+    for (int s2 = s_lo; s2 < s_hi; ++s2) {
+      const float4 q0 = prm[s2][0];
+      const float4 q1 = prm[s2][1];
+      const int lo = __float_as_int(q1.x), hi = __float_as_int(q1.y);
+      if (cell >= lo && cell <= hi) {
+        const float d = (pc - q0.x) - q0.y;
+        const float m = q0.z * d * d;
+        if (m <= 1.f) {
+          const float v = q1.z * ex2_approx(fmaf(m, kNegThirtyLog2e, q0.w));
+          if (KAHAN) {
+            const float tt = acc + v;
+            cmp += (fabsf(acc) >= fabsf(v)) ? ((acc - tt) + v) : ((v - tt) + acc);
+            acc = tt;
+          } else {
+            acc += v;
           }
         }
       }
-      __syncwarp();
     }
+    __syncthreads();  // list, prm and wsum are reused by the next pass
   }
   parts[warp][0][lane] = acc;
   parts[warp][1][lane] = cmp;
   __syncthreads();
-  if (warp != 0) return;
-  // combine the warps' partial sums in warp order (compensated)
-  float s0 = 0.f, c0 = 0.f;
+  __shared__ int s_last;
+  if (warp == 0) {
+    // combine the warps' partial sums in warp order (compensated)
+    float s0 = 0.f, c0 = 0.f;
 #pragma unroll
-  for (int w = 0; w < NW; ++w) {
+    for (int w = 0; w < NW; ++w) {
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const float v = parts[w][h][lane];
-      const float tt = s0 + v;
-      c0 += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
-      s0 = tt;
+      for (int h = 0; h < 2; ++h) {
+        const float v = parts[w][h][lane];
+        const float tt = s0 + v;
+        c0 += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
+        s0 = tt;
+      }
     }
-  }
 
-  float l = 0.f;
-  if (cell < D0) {
-    const float v = s0 + c0;
-    const size_t gi = (size_t)a * D0 + cell;
-    if (out.R) out.R[gi] = v;
-    if (out.epilogue == kEpiL2) {
-      const float res = v - out.data[gi];
-      if (out.alpha) out.alpha[gi] = res;
-      l = 0.5f * res * res;
-    } else if (out.epilogue == kEpiKL) {
-      const float fo = out.data[gi];
-      const float gg = v + out.bg;
-      const float ig = 1.f / gg;
-      if (out.alpha) out.alpha[gi] = 1.f - fo * ig;
-      if (out.beta) out.beta[gi] = fo * ig * ig;
-      l = kl_term(fo, gg);
-    }
-  }
-  if (out.loss_part) {
-    const double d = warp_sum_d((double)l);
-    if (lane == 0) out.loss_part[item] = d;
-    if (loss_out) {
-      // the last block to finish sums the per-tile partials in tile order
-      int last = 0;
-      if (lane == 0) {
-        __threadfence();
-        last = atomicAdd(done, 1) == (int)gridDim.x - 1;
-      }
-      if (__shfl_sync(0xffffffffu, last, 0)) {
-        __threadfence();
-        sum_partials_warp(out.loss_part, (int)gridDim.x, loss_out, lane);
+    float l = 0.f;
+    if (cell < D0) {
+      const float v = s0 + c0;
+      const size_t gi = (size_t)a * D0 + cell;
+      if (out.R) out.R[gi] = v;
+      if (out.epilogue == kEpiL2) {
+        const float res = v - out.data[gi];
+        if (out.alpha) out.alpha[gi] = res;
+        l = 0.5f * res * res;
+      } else if (out.epilogue == kEpiKL) {
+        const float fo = out.data[gi];
+        const float gg = v + out.bg;
+        const float ig = 1.f / gg;
+        if (out.alpha) out.alpha[gi] = 1.f - fo * ig;
+        if (out.beta) out.beta[gi] = fo * ig * ig;
+        l = kl_term(fo, gg);
       }
     }
-  }
+    if (out.loss_part) {
+      const double d = warp_sum_d((double)l);
+      if (lane == 0) out.loss_part[item] = d;
+      if (loss_out && lane == 0) {
+        __threadfence();
+        s_last = atomicAdd(done, 1) == (int)gridDim.x - 1;
+      }
+    }
+  }  // warp 0
+  if (!out.loss_part || !loss_out) return;
+  __syncthreads();
+  if (!s_last) return;
+  // the last block to finish sums the per-tile partials, all its threads
+  __threadfence();
+  sum_partials_block<NW>(out.loss_part, (int)gridDim.x, loss_out);
 }
 
 // ---- pixel-integrated operator: binning and projection -------------------
