@@ -820,7 +820,7 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
     // last block also sums the loss partials (no separate finalize launch)
     fused_loss = loss_out != nullptr && items <= kFusedLossItems;
     double *lo = fused_loss ? loss_out : nullptr;
-    if (W >= 16)  // long atom lists: 8 warps share a tile's bitmap words
+    if (W >= 8)  // 8 warps share a tile's atoms from 8 bitmap words (256 atoms) up
       gr_project1d_kernel<true, 8><<<(unsigned)items, 8 * 32, 0, stream>>>(
           at, g, tc, bitmap, W, o, lo, next_item + 1);
     else
