@@ -187,8 +187,10 @@ __global__ void __launch_bounds__(kProjWarps * 32)
     {
       __syncwarp();  // every lane is done with the previous batch's data
       const int nb = min(32, count);
+      // C.y: the tile-local clipped box as first row | first column << 8 |
+      // width << 16 | rows << 24 (0: empty), C.z: 1 / width; both formed
+      // here, one atom per lane, rather than by the whole warp per atom
       float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A, C = A;
-      C.y = __int_as_float(0x000000ff);  // empty box: rows 255..0
       if (lane < nb) {
         Pair<2> p;
         pair_setup<2>(at, list[(head + lane) & (kRing - 1)], f, g, p);
@@ -198,8 +200,11 @@ __global__ void __launch_bounds__(kProjWarps * 32)
         A = make_float4(p.qh[0], p.ql[0], p.qh[1], p.ql[1]);
         B = make_float4(p.G[0], 2.f * p.G[1], p.G[2], p.l2amp);
         C.x = p.sgn;
-        C.y = __int_as_float(empty ? 0x000000ff
-                                   : (lr0 | (lr1 << 8) | (lc0 << 16) | (lc1 << 24)));
+        const int bw = lc1 - lc0 + 1;
+        C.y = __uint_as_float(empty ? 0u
+                                    : (unsigned)(lr0 | (lc0 << 8) | (bw << 16) |
+                                                 ((lr1 - lr0 + 1) << 24)));
+        C.z = empty ? 0.f : __frcp_rn((float)bw);
       }
       head += nb;
       count -= nb;
@@ -209,14 +214,12 @@ __global__ void __launch_bounds__(kProjWarps * 32)
       __syncwarp();
       for (int sI = 0; sI < nb; ++sI) {
         const float4 qC = prm[sI * 3 + 2];
-        const unsigned box = (unsigned)__float_as_int(qC.y);
-        const int lr0 = box & 0xff, lr1 = (box >> 8) & 0xff;
-        const int lc0 = (box >> 16) & 0xff, lc1 = box >> 24;
-        if (lr0 > lr1) continue;  // warp-uniform
+        const unsigned box = __float_as_uint(qC.y);
+        if (box == 0u) continue;  // warp-uniform
+        const int lr0 = box & 0xff, lc0 = (box >> 8) & 0xff, bw = (box >> 16) & 0xff;
+        const int ncell = (int)(box >> 24) * bw;
+        const float inv_bw = qC.z;
         const float4 qA = prm[sI * 3 + 0], qB = prm[sI * 3 + 1];
-        const int bw = lc1 - lc0 + 1;
-        const int ncell = (lr1 - lr0 + 1) * bw;
-        const float inv_bw = __frcp_rn((float)bw);
         for (int e = lane; e < ncell; e += 32) {
           // (e + 1/2) / bw is at least 1/(2 bw) from an integer, far more
           // than the rounding of the product: the row index is exact
