@@ -11,6 +11,7 @@ geometry is a :class:`DeviceGeometry`.
 import ctypes
 import threading
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -387,6 +388,23 @@ def newton_accept_into(dim, iso, loss_cur, loss_trial, theta, theta_trial, lam, 
     _lib.check(st, "gr_newton_accept")
 
 
+def _pack(items, align=64):
+    """Element offsets of (name, shape) buffers packed at ``align``-element
+    boundaries: ({name: (offset, shape)}, total elements)."""
+    out, off = {}, 0
+    for name, shape in items:
+        k = int(np.prod(shape, dtype=np.int64)) if len(shape) else 1
+        out[name] = (off, shape)
+        off += (k + align - 1) // align * align
+    return out, max(off, align)
+
+
+def _packed_view(buf, spec):
+    off, shape = spec
+    k = int(np.prod(shape, dtype=np.int64)) if len(shape) else 1
+    return buf[off:off + k].view(shape)
+
+
 class FitStep:
     """One fit evaluation from host inputs to host results, as a CUDA graph.
 
@@ -411,37 +429,43 @@ class FitStep:
         self.background = float(background)
         n, d = int(n_atoms), geom.dim
         pr = 1 if iso else (3 if d == 2 else 6)
-        pin = dict(dtype=torch.float32, pin_memory=True)
-        self.I_h = torch.zeros(n, **pin)
-        self.x_h = torch.zeros(n, d, **pin)
-        self.r_h = torch.ones(n, pr, **pin)
-        self.data_h = torch.zeros(geom.shape, **pin)
-        self.I_d = torch.zeros(n, device=dev)
-        self.x_d = torch.zeros(n, d, device=dev)
-        self.r_d = torch.ones(n, pr, device=dev)
-        self.data_d = torch.zeros(geom.shape, device=dev)
-        self.atoms = DeviceAtoms(self.I_d, self.x_d, self.r_d, dev)
-        P = self.atoms.n_params()
+        P = (2 + d) if iso else (1 + d + (3 if d == 2 else 6))
+        # inputs (atoms, data) and outputs (loss, gradient, Hessian) each live
+        # in one arena, on the device and pinned on the host, so a step moves
+        # each way with a single copy; every buffer is a view
+        ishape = [("I", (n,)), ("x", (n, d)), ("r", (n, pr)), ("data", tuple(geom.shape))]
+        oshape = [("loss", ()), ("g", (n, P))] + ([("H", (n, P, P))] if self.order > 1 else [])
+        ilay, ni = _pack(ishape)
+        olay, no = _pack(oshape)
+        self.in_h = torch.zeros(ni, dtype=torch.float32, pin_memory=True)
+        self.in_d = torch.zeros(ni, dtype=torch.float32, device=dev)
+        self.out_h = torch.zeros(no, dtype=torch.float64, pin_memory=True)
+        self.out_d = torch.zeros(no, dtype=torch.float64, device=dev)
+        self.I_h, self.x_h, self.r_h, self.data_h = (_packed_view(self.in_h, ilay[k])
+                                                     for k, _ in ishape)
+        self.I_d, self.x_d, self.r_d, self.data_d = (_packed_view(self.in_d, ilay[k])
+                                                     for k, _ in ishape)
+        self.r_h.fill_(1.0)
+        self.r_d.fill_(1.0)
+        self.atoms = DeviceAtoms.wrap(self.I_d, self.x_d, self.r_d.reshape(n) if iso else self.r_d)
         f32 = dict(dtype=torch.float32, device=dev)
         self.alpha = torch.empty(geom.shape, **f32)
         self.beta = torch.empty(geom.shape, **f32) if fit == "kl" else None
         f64 = dict(dtype=torch.float64, device=dev)
-        self.loss = torch.zeros((), **f64)
         self.f = torch.zeros(n, **f64)
-        self.g = torch.zeros(n, P, **f64)
-        self.H = torch.zeros(n, P, P, **f64) if self.order > 1 else None
-        self.loss_h = torch.zeros((), dtype=torch.float64, pin_memory=True)
-        self.g_h = torch.zeros(n, P, dtype=torch.float64, pin_memory=True)
-        self.H_h = (torch.zeros(n, P, P, dtype=torch.float64, pin_memory=True)
-                    if self.order > 1 else None)
+        self.loss = _packed_view(self.out_d, olay["loss"])
+        self.g = _packed_view(self.out_d, olay["g"])
+        self.H = _packed_view(self.out_d, olay["H"]) if self.order > 1 else None
+        self.loss_h = _packed_view(self.out_h, olay["loss"])
+        self.g_h = _packed_view(self.out_h, olay["g"])
+        self.H_h = _packed_view(self.out_h, olay["H"]) if self.order > 1 else None
         nb = max(workspace_bytes(_lib.GR_OP_PROJECT, self.atoms, geom),
                  workspace_bytes(_lib.GR_OP_DERIVS_2 if self.order > 1 else _lib.GR_OP_DERIVS_1,
                                  self.atoms, geom))
         self.ws = torch.empty(max(nb, 256), dtype=torch.uint8, device=dev)
-        self.h2d_bytes = sum(t.numel() * t.element_size()
-                             for t in (self.I_h, self.x_h, self.r_h, self.data_h))
-        self.d2h_bytes = sum(t.numel() * t.element_size()
-                             for t in (self.loss_h, self.g_h, self.H_h) if t is not None)
+        # the bytes each step copies (the arenas, with their alignment gaps)
+        self.h2d_bytes = self.in_h.numel() * self.in_h.element_size()
+        self.d2h_bytes = self.out_h.numel() * self.out_h.element_size()
         stream = torch.cuda.Stream(dev)
         stream.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(stream):
@@ -453,19 +477,13 @@ class FitStep:
         torch.cuda.synchronize(dev)
 
     def _body(self):
-        self.I_d.copy_(self.I_h, non_blocking=True)
-        self.x_d.copy_(self.x_h, non_blocking=True)
-        self.r_d.copy_(self.r_h, non_blocking=True)
-        self.data_d.copy_(self.data_h, non_blocking=True)
+        self.in_d.copy_(self.in_h, non_blocking=True)
         fit_forward_into(self.atoms, self.geom, self.data_d, self.fit, self.background, None,
                          self.alpha, self.beta, self.loss, self.ws, psf=self.psf)
         bc = 1.0 if self.fit == "l2" else 0.0
         atom_derivs_into(self.atoms, self.geom, "field", self.alpha, self.beta, bc, self.order,
                          self.f, self.g, self.H, self.ws, psf=self.psf)
-        self.loss_h.copy_(self.loss, non_blocking=True)
-        self.g_h.copy_(self.g, non_blocking=True)
-        if self.H_h is not None:
-            self.H_h.copy_(self.H, non_blocking=True)
+        self.out_h.copy_(self.out_d, non_blocking=True)
 
     def set_inputs(self, I=None, x=None, r=None, data=None):
         """Copy new atoms and/or data into the pinned input buffers."""
