@@ -397,6 +397,23 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// Reduce-scatter of 32 values over the warp (recursive halving): on return
+// v[0] of lane l is the sum over all lanes of their v[l].  At the step with
+// offset m each lane keeps the half of its remaining values whose index bit m
+// matches its lane bit and receives the partner's copy of that half.
+__device__ __forceinline__ void warp_reduce_scatter32(float (&v)[32], int lane) {
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    const bool up = (lane & m) != 0;
+#pragma unroll
+    for (int k = 0; k < m; ++k) {
+      const float keep = up ? v[k + m] : v[k];
+      const float give = up ? v[k] : v[k + m];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, give, m);
+    }
+  }
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -340,11 +340,33 @@ __global__ void __launch_bounds__(128, ORDER == 1 ? 5 : (ONE ? 3 : 1))
     if constexpr (ONE) break;
   }
 
-  // combine lanes sharing an atom (fixed butterfly order), then write
+  // combine lanes sharing an atom, then write
   float vals_f = f;
   float gv[P];
 #pragma unroll
   for (int i = 0; i < P; ++i) gv[i] = gacc[i].get();
+  if (ORDER > 1 && cfg.ag == 1) {
+    // one atom per warp: a reduce-scatter leaves the warp sum of value
+    // 32 c + lane of the atom's qn values in lane `lane` (chunk c), so every
+    // lane stores one value; a full butterfly of every value on every lane
+    // would cost qn * 5 shuffles per lane instead of 31 per 32 values
+    constexpr int QN = 1 + P + (ORDER > 1 ? NH : 0);
+    constexpr int NC = (QN + 31) / 32;
+    float *dst = part + (size_t)chunk * cfg.qn * at.n + j;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      float v[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const int q = 32 * c + k;
+        v[k] = q == 0 ? vals_f : (q <= P ? gv[q - 1] : (q < QN ? hacc[q - 1 - P] : 0.f));
+      }
+      warp_reduce_scatter32(v, lane);
+      const int q = 32 * c + lane;
+      if (valid && q < QN) dst[(size_t)q * at.n] = v[0];
+    }
+    return;
+  }
   for (int off = cfg.ag; off < 32; off <<= 1) {
     vals_f += __shfl_xor_sync(0xffffffffu, vals_f, off);
 #pragma unroll
