@@ -45,7 +45,7 @@ EXPORTS = ("gr_version", "gr_preload", "gr_status_string", "gr_workspace_bytes",
            "gr_set_tuning", "gr_get_tuning", "gr_kernel_timer", "gr_kernel_timer_read",
            "gr_fit_loop_begin", "gr_fit_loop_end", "gr_fit_loop_instantiate",
            "gr_fit_loop_launch", "gr_fit_loop_destroy", "gr_regulariser",
-           "gr_sino_moments", "gr_accept_fields")
+           "gr_sino_moments", "gr_accept_fields", "gr_newton_accept_fields")
 
 _lock = threading.Lock()
 _lib = None
@@ -111,6 +111,11 @@ def load(build_if_missing=True):
         lib.gr_newton_accept.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_void_p] * 5 +
                                          [ctypes.c_double] * 2 + [ctypes.c_void_p] * 9 +
                                          [ctypes.c_int, ctypes.c_void_p])
+        lib.gr_newton_accept_fields.restype = ctypes.c_int
+        lib.gr_newton_accept_fields.argtypes = (
+            [ctypes.c_int] * 3 + [ctypes.c_void_p] * 5 + [ctypes.c_double] * 2 +
+            [ctypes.c_void_p] * 9 + [ctypes.c_int] + [ctypes.c_void_p] * 4 +
+            [ctypes.c_size_t, ctypes.c_void_p])
         lib.gr_volproj.restype = ctypes.c_int
         lib.gr_volproj.argtypes = [P(GrAtoms), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p]

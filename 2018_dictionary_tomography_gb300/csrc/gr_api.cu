@@ -214,12 +214,13 @@ int gr_newton_solve(int dim, int iso, int n_atoms, const double *g, const double
                              step_norm, fail, ao, static_cast<cudaStream_t>(stream));
 }
 
-int gr_newton_accept(int dim, int iso, int n_atoms, double *loss_cur,
-                     const double *loss_trial, double *theta, const double *theta_trial,
-                     double *lam, double lam_min, double lam_max, float *I, float *x,
-                     float *r, const float *I_trial, const float *x_trial,
-                     const float *r_trial, double *hist, int *hist_accepted,
-                     int *counter, int hist_len, void *stream) {
+static int newton_accept_impl(int dim, int iso, int n_atoms, double *loss_cur,
+                              const double *loss_trial, double *theta,
+                              const double *theta_trial, double *lam, double lam_min,
+                              double lam_max, float *I, float *x, float *r,
+                              const float *I_trial, const float *x_trial,
+                              const float *r_trial, double *hist, int *hist_accepted,
+                              int *counter, int hist_len, FieldCopy fc, void *stream) {
   if ((dim != 2 && dim != 3) || n_atoms < 0 || !loss_cur || !loss_trial || !counter)
     return GR_ERR_ARG;
   if (n_atoms > 0 && (!theta || !theta_trial || !lam || !I || !x || !r || !I_trial ||
@@ -231,7 +232,34 @@ int gr_newton_accept(int dim, int iso, int n_atoms, double *loss_cur,
   return launch_newton_accept(n_atoms, P, pr, dim, loss_cur, loss_trial, theta, theta_trial,
                               lam, lam_min, lam_max, AtomOut{I, x, r},
                               AtomIn{I_trial, x_trial, r_trial}, hist, hist_accepted,
-                              counter, hist_len, static_cast<cudaStream_t>(stream));
+                              counter, hist_len, fc, static_cast<cudaStream_t>(stream));
+}
+
+int gr_newton_accept(int dim, int iso, int n_atoms, double *loss_cur,
+                     const double *loss_trial, double *theta, const double *theta_trial,
+                     double *lam, double lam_min, double lam_max, float *I, float *x,
+                     float *r, const float *I_trial, const float *x_trial,
+                     const float *r_trial, double *hist, int *hist_accepted,
+                     int *counter, int hist_len, void *stream) {
+  return newton_accept_impl(dim, iso, n_atoms, loss_cur, loss_trial, theta, theta_trial, lam,
+                            lam_min, lam_max, I, x, r, I_trial, x_trial, r_trial, hist,
+                            hist_accepted, counter, hist_len,
+                            FieldCopy{nullptr, nullptr, nullptr, nullptr, 0}, stream);
+}
+
+int gr_newton_accept_fields(int dim, int iso, int n_atoms, double *loss_cur,
+                            const double *loss_trial, double *theta,
+                            const double *theta_trial, double *lam, double lam_min,
+                            double lam_max, float *I, float *x, float *r,
+                            const float *I_trial, const float *x_trial, const float *r_trial,
+                            double *hist, int *hist_accepted, int *counter, int hist_len,
+                            const float *alpha_trial, float *alpha, const float *beta_trial,
+                            float *beta, size_t n_cells, void *stream) {
+  if (!alpha_trial || !alpha || (beta && !beta_trial)) return GR_ERR_ARG;
+  return newton_accept_impl(dim, iso, n_atoms, loss_cur, loss_trial, theta, theta_trial, lam,
+                            lam_min, lam_max, I, x, r, I_trial, x_trial, r_trial, hist,
+                            hist_accepted, counter, hist_len,
+                            FieldCopy{alpha_trial, alpha, beta_trial, beta, n_cells}, stream);
 }
 
 static int volproj_impl(const gr_atoms *atoms, int dim, const int *n_vox,

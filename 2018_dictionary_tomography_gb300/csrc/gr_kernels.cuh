@@ -99,11 +99,20 @@ int launch_newton_solve(int dim, int iso, int n, const double *g, const double *
                         const double *lam, const double *theta,
                         const unsigned char *mask, double *theta_new,
                         double *step_norm, int *fail, AtomOut ao, cudaStream_t stream);
+// fit fields adopted with an accepted trial (all null: none)
+struct FieldCopy {
+  const float *alpha_t;
+  float *alpha;
+  const float *beta_t;
+  float *beta;
+  size_t n;
+};
 int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
                          const double *loss_trial, double *theta,
                          const double *theta_trial, double *lam, double lam_min,
                          double lam_max, AtomOut cur, AtomIn trial, double *hist,
-                         int *hist_acc, int *counter, int hist_len, cudaStream_t stream);
+                         int *hist_acc, int *counter, int hist_len, FieldCopy fc,
+                         cudaStream_t stream);
 
 int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y,
                    float *u, int psf, float s, cudaStream_t stream);

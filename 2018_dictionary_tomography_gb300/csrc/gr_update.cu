@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(256)
                             const double *loss_trial, double *theta,
                             const double *theta_trial, double *lam, double lam_min,
                             double lam_max, AtomOut cur, AtomIn trial, double *hist,
-                            int *hist_acc, int *counter, int hist_len) {
+                            int *hist_acc, int *counter, int hist_len, FieldCopy fc) {
   const bool acc = *loss_trial <= *loss_cur;
   const int stride = gridDim.x * blockDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -387,6 +387,13 @@ __global__ void __launch_bounds__(256)
       for (int q = 0; q < pr; ++q) cur.r[(size_t)j * pr + q] = trial.r[(size_t)j * pr + q];
     }
   }
+  // an accepted trial's fit fields become the current ones (so the next
+  // iteration needs no projection of the current atoms)
+  if (acc && fc.alpha)
+    for (size_t e = t0; e < fc.n; e += stride) {
+      fc.alpha[e] = fc.alpha_t[e];
+      if (fc.beta) fc.beta[e] = fc.beta_t[e];
+    }
   if (t0 == 0) {
     if (acc) *loss_cur = *loss_trial;
     const int k = *counter;
@@ -431,12 +438,15 @@ int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
                          const double *loss_trial, double *theta,
                          const double *theta_trial, double *lam, double lam_min,
                          double lam_max, AtomOut cur, AtomIn trial, double *hist,
-                         int *hist_acc, int *counter, int hist_len, cudaStream_t stream) {
-  int blocks = (n * P + 255) / 256;
-  blocks = blocks < 1 ? 1 : (blocks > 152 * 4 ? 152 * 4 : blocks);
-  gr_newton_accept_kernel<<<blocks, 256, 0, stream>>>(n, P, pr, dim, loss_cur, loss_trial, theta,
-                                                 theta_trial, lam, lam_min, lam_max, cur,
-                                                 trial, hist, hist_acc, counter, hist_len);
+                         int *hist_acc, int *counter, int hist_len, FieldCopy fc,
+                         cudaStream_t stream) {
+  if (fc.alpha && (!fc.alpha_t || (fc.beta && !fc.beta_t))) return kErrArg;
+  const size_t work = (size_t)n * P > fc.n / 4 ? (size_t)n * P : fc.n / 4;
+  size_t blocks = (work + 255) / 256;
+  blocks = blocks < 1 ? 1 : (blocks > 152 * 8 ? 152 * 8 : blocks);
+  gr_newton_accept_kernel<<<(unsigned)blocks, 256, 0, stream>>>(
+      n, P, pr, dim, loss_cur, loss_trial, theta, theta_trial, lam, lam_min, lam_max, cur,
+      trial, hist, hist_acc, counter, hist_len, fc);
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }

@@ -377,15 +377,25 @@ def accept_fields_into(loss_cur, loss_trial, alpha_t, alpha, beta_t, beta, devic
 
 
 def newton_accept_into(dim, iso, loss_cur, loss_trial, theta, theta_trial, lam, lam_min,
-                       lam_max, cur_atoms, trial_atoms, hist, hist_acc, counter, device):
-    st = _lib.load().gr_newton_accept(
-        int(dim), 1 if iso else 0, int(theta.shape[0]), loss_cur.data_ptr(),
-        loss_trial.data_ptr(), theta.data_ptr(), theta_trial.data_ptr(), lam.data_ptr(),
-        float(lam_min), float(lam_max), cur_atoms.I.data_ptr(), cur_atoms.x.data_ptr(),
-        cur_atoms.r.data_ptr(), trial_atoms.I.data_ptr(), trial_atoms.x.data_ptr(),
-        trial_atoms.r.data_ptr(), hist.data_ptr(), hist_acc.data_ptr(), counter.data_ptr(),
-        int(hist.numel()), _stream_handle(device))
-    _lib.check(st, "gr_newton_accept")
+                       lam_max, cur_atoms, trial_atoms, hist, hist_acc, counter, device,
+                       fields=None):
+    """Device-side accept/reject; ``fields = (alpha_t, alpha, beta_t, beta)``
+    also adopts the trial's fit fields when it is accepted (one launch)."""
+    args = (int(dim), 1 if iso else 0, int(theta.shape[0]), loss_cur.data_ptr(),
+            loss_trial.data_ptr(), theta.data_ptr(), theta_trial.data_ptr(), lam.data_ptr(),
+            float(lam_min), float(lam_max), cur_atoms.I.data_ptr(), cur_atoms.x.data_ptr(),
+            cur_atoms.r.data_ptr(), trial_atoms.I.data_ptr(), trial_atoms.x.data_ptr(),
+            trial_atoms.r.data_ptr(), hist.data_ptr(), hist_acc.data_ptr(), counter.data_ptr(),
+            int(hist.numel()))
+    if fields is None:
+        st = _lib.load().gr_newton_accept(*args, _stream_handle(device))
+        _lib.check(st, "gr_newton_accept")
+        return
+    alpha_t, alpha, beta_t, beta = fields
+    st = _lib.load().gr_newton_accept_fields(
+        *args, alpha_t.data_ptr(), alpha.data_ptr(), _ptr(beta_t), _ptr(beta),
+        int(alpha.numel()), _stream_handle(device))
+    _lib.check(st, "gr_newton_accept_fields")
 
 
 def _pack(items, align=64):

@@ -7,11 +7,11 @@ fitted; every admitted request owns its device buffers and a CUDA stream, and
 one damped-Newton iteration
 
   gr_atom_derivs(all atoms)      -> gradient and Hessian blocks
-  gr_newton_solve                -> trial parameters (FP64 solves on the device)
+  gr_newton_solve                -> trial parameters (double-float block solves)
   gr_fit_forward(trial atoms)    -> trial fit fields, trial loss
-  gr_newton_accept               -> device-side accept/reject, damping update,
-                                    loss history
-  gr_accept_fields               -> an accepted trial's fields become current
+  gr_newton_accept_fields        -> device-side accept/reject, damping update,
+                                    loss history; an accepted trial's fields
+                                    become current (one launch)
 
 (one projection per iteration: the current atoms' fields come from the
 prologue's gr_fit_forward, an accepted trial, or stay after a rejection)
@@ -313,9 +313,8 @@ class _Slot:
         engine.newton_accept_into(self.dim, self.iso, self.loss_cur, self.loss_trial,
                                   self.theta, self.theta_trial, self.lam, 1e-4, 1e4,
                                   self.cur, self.trial, self.hist, self.hist_acc,
-                                  self.counter, self.dev)
-        engine.accept_fields_into(self.loss_cur, self.loss_trial, self.alpha_t, self.alpha,
-                                  self.beta_t, self.beta, self.dev)
+                                  self.counter, self.dev,
+                                  fields=(self.alpha_t, self.alpha, self.beta_t, self.beta))
 
     def _copy_back(self):
         self.h_counter.copy_(self.counter, non_blocking=True)

@@ -235,6 +235,22 @@ int gr_newton_accept(int dim, int iso, int n_atoms, double *loss_cur,
                      const float *r_trial, double *hist, int *hist_accepted,
                      int *counter, int hist_len, void *stream);
 
+/* gr_newton_accept plus, when the trial is accepted, the adoption of the
+ * trial's fit fields (alpha_trial -> alpha and, for KL, beta_trial -> beta;
+ * n_cells each), in one launch: the accept/reject step of the device-resident
+ * fitting loop, where the trial's forward wrote its fields so that the next
+ * iteration needs no projection of the current atoms.  Equivalent to
+ * gr_newton_accept followed by gr_accept_fields.  GR_ERR_ARG as
+ * gr_newton_accept, or for missing field pointers. */
+int gr_newton_accept_fields(int dim, int iso, int n_atoms, double *loss_cur,
+                            const double *loss_trial, double *theta,
+                            const double *theta_trial, double *lam, double lam_min,
+                            double lam_max, float *I, float *x, float *r,
+                            const float *I_trial, const float *x_trial, const float *r_trial,
+                            double *hist, int *hist_accepted, int *counter, int hist_len,
+                            const float *alpha_trial, float *alpha, const float *beta_trial,
+                            float *beta, size_t n_cells, void *stream);
+
 /*
  * Measurement helpers (no counterpart in the reference, which has no
  * benchmarks).

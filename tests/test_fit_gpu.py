@@ -226,3 +226,57 @@ def test_fit_step_graph_matches_direct_calls(eng, cuda_ready, case):
     atoms2 = engine_atoms(I * 0.9, x, r)
     fw2 = eng.fit_forward(atoms2, geom, d, fit, bg)
     assert loss2 == fw2["loss"].item()
+
+
+@pytest.mark.parametrize("accepted", [True, False])
+def test_newton_accept_fields_equals_two_launches(eng, cuda_ready, accepted):
+    """gr_newton_accept_fields (one launch) leaves every buffer exactly as
+    gr_newton_accept followed by gr_accept_fields."""
+    rng = np.random.default_rng(8)
+    dev = torch.device("cuda")
+    n, dim, P = 37, 3, 10
+
+    def state():
+        t = lambda a, dt=torch.float64: torch.tensor(a, dtype=dt, device=dev)
+        cur = eng.DeviceAtoms(rng.uniform(0.5, 1, n), rng.normal(size=(n, 3)),
+                              rng.uniform(5, 9, (n, 6)), dev)
+        trial = eng.DeviceAtoms(rng.uniform(0.5, 1, n), rng.normal(size=(n, 3)),
+                                rng.uniform(5, 9, (n, 6)), dev)
+        return dict(cur=cur, trial=trial, theta=t(rng.normal(size=(n, P))),
+                    theta_t=t(rng.normal(size=(n, P))), lam=t(rng.uniform(0.1, 2, n)),
+                    loss_cur=t(2.0), loss_trial=t(1.0 if accepted else 3.0),
+                    hist=torch.zeros(20, dtype=torch.float64, device=dev),
+                    acc=torch.zeros(20, dtype=torch.int32, device=dev),
+                    counter=torch.zeros(1, dtype=torch.int32, device=dev),
+                    alpha=t(rng.normal(size=(7, 11)), torch.float32),
+                    alpha_t=t(rng.normal(size=(7, 11)), torch.float32),
+                    beta=t(rng.normal(size=(7, 11)), torch.float32),
+                    beta_t=t(rng.normal(size=(7, 11)), torch.float32))
+
+    def clone(s):
+        out = {}
+        for k, v in s.items():
+            if isinstance(v, eng.DeviceAtoms):
+                out[k] = eng.DeviceAtoms(v.I.clone(), v.x.clone(), v.r.clone(), dev)
+            else:
+                out[k] = v.clone()
+        return out
+
+    a = state()
+    b = clone(a)
+    for s, fused in ((a, False), (b, True)):
+        eng.newton_accept_into(dim, False, s["loss_cur"], s["loss_trial"], s["theta"],
+                               s["theta_t"], s["lam"], 1e-4, 1e4, s["cur"], s["trial"],
+                               s["hist"], s["acc"], s["counter"], dev,
+                               fields=((s["alpha_t"], s["alpha"], s["beta_t"], s["beta"])
+                                       if fused else None))
+        if not fused:
+            eng.accept_fields_into(s["loss_cur"], s["loss_trial"], s["alpha_t"], s["alpha"],
+                                   s["beta_t"], s["beta"], dev)
+    for k in a:
+        if isinstance(a[k], eng.DeviceAtoms):
+            for f in ("I", "x", "r"):
+                assert torch.equal(getattr(a[k], f), getattr(b[k], f)), (k, f)
+        else:
+            assert torch.equal(a[k], b[k]), k
+    assert torch.equal(b["alpha"], b["alpha_t"]) == accepted
