@@ -61,3 +61,24 @@ def test_morton_order_is_permutation():
     d_curve = np.linalg.norm(np.diff(x[p], axis=0), axis=1).mean()
     d_index = np.linalg.norm(np.diff(x, axis=0), axis=1).mean()
     assert d_curve < 0.5 * d_index
+
+
+def test_tuning_keys_round_trip_without_gpu():
+    """gr_set_tuning / gr_get_tuning: each key keeps a valid value and
+    rejects an invalid one (host-side only)."""
+    lib_mod = importlib.import_module("2018_dictionary_tomography_gb300._lib")
+    lib = lib_mod.load()
+    # key: (a valid value, an invalid value)
+    cases = {0: (65536, 16), 1: (2, 0), 2: (4, 3), 3: (2, 3), 4: (1 << 20, -1),
+             6: (4096, -5), 7: (0, -1)}
+    for key, (good, bad) in cases.items():
+        saved = lib.gr_get_tuning(key)
+        try:
+            assert lib.gr_set_tuning(key, good) == 0, key
+            assert lib.gr_get_tuning(key) == good, key
+            assert lib.gr_set_tuning(key, bad) == -1, key
+            assert lib.gr_get_tuning(key) == good, key
+        finally:
+            assert lib.gr_set_tuning(key, saved) == 0
+    assert lib.gr_get_tuning(99) == -1
+    assert lib.gr_set_tuning(99, 1) == -1
