@@ -22,7 +22,7 @@
 // angles of each atom split over several lanes), and loops over a chunk of
 // angles.  Gradients are accumulated per lane with compensated FP32 sums,
 // Hessians in FP32; lanes sharing an atom are combined by a fixed-order
-// butterfly; chunk partials are summed (compensated) in chunk order by
+// butterfly; chunk partials are summed in FP64 in chunk order by
 // gr_deriv_finalize_kernel, which also applies the isotropic chain rule.
 // No float atomics anywhere: results are bitwise reproducible.
 #include "gr_assembly.cuh"
@@ -566,7 +566,7 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// Sum chunk partials (compensated) in chunk order, expand the packed Hessian and
+// Sum chunk partials (FP64) in chunk order, expand the packed Hessian and
 // apply the isotropic chain rule r_aniso = (s, .., s, 0, ..).  A block covers
 // 32 atoms; its 8 warps share out the partial values (reads of consecutive
 // atoms are coalesced), then all its threads write the atoms' outputs.
@@ -579,27 +579,17 @@ __global__ void __launch_bounds__(32 * kRedSlices)
   constexpr int D = K + 1;
   constexpr int P = n_par<K>();
   constexpr int QN = 1 + P + P * (P + 1) / 2;
-  // chunk sums in chunk order: thread (atom, ty) sums values q = ty,
-  // ty + kRedSlices, ... of its atom, all loads independent.  The sum is
-  // compensated (Neumaier) in FP32 and carried as a float pair, about twice
-  // FP32 precision, then converted to FP64 once: an FP64 add per partial
-  // would queue on the SM's narrow FP64 pipe (16 cycles per warp
-  // instruction on this GPU).
+  // chunk sums in FP64 in chunk order: thread (atom, ty) sums values
+  // q = ty, ty + kRedSlices, ... of its atom, all loads independent
   __shared__ double vs[QN][32];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int slot = blockIdx.x * 32 + tx;
   if (slot < n)
     for (int q = ty; q < cfg.qn; q += kRedSlices) {
-      float sm = 0.f, cm = 0.f;
+      double t = 0.0;
 #pragma unroll 4
-      for (int c = 0; c < cfg.nchunks; ++c) {
-        const float v = part[((size_t)c * cfg.qn + q) * n + slot];
-        const float tt = __fadd_rn(sm, v);
-        cm += (fabsf(sm) >= fabsf(v)) ? __fadd_rn(__fsub_rn(sm, tt), v)
-                                      : __fadd_rn(__fsub_rn(v, tt), sm);
-        sm = tt;
-      }
-      vs[q][tx] = (double)sm + (double)cm;
+      for (int c = 0; c < cfg.nchunks; ++c) t += (double)part[((size_t)c * cfg.qn + q) * n + slot];
+      vs[q][tx] = t;
     }
   __syncthreads();
   // outputs of the block's atoms, written by all threads from the sums

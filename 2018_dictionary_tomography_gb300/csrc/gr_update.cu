@@ -17,7 +17,6 @@
 //    in NewtonGaussian.py:74), one group of lanes per atom, then the reference's parameter update with its
 //    clamps: I >= 0, and sign flips keeping diag(r) >= 0 (GD_lib.py:504-522).
 #include "gr_kernels.cuh"
-#include "gr_dfloat.cuh"
 
 namespace gr {
 
@@ -154,16 +153,16 @@ int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int 
 // ---------------------------------------------------------------------------
 // batched damped Newton step
 // ---------------------------------------------------------------------------
-// On this GPU an FP64 instruction holds the SM's FP64 pipe for 16 cycles per
-// warp and a dependent FP64 operation takes about 64 cycles, so a P x P
-// factorisation in FP64 is slow twice over: by the length of its dependent
-// chain and by the pipe.  Here a group of G lanes (G a power of two >= P)
-// shares one atom, lane l holding row l of the damped block, and the
-// arithmetic is double-float (pairs of floats, about 48 significant bits,
-// gr_dfloat.cuh) on the FP32 pipe; FP64 is used only to read the FP64
-// inputs and to form the FP64 outputs.  Columns are broadcast with shuffles;
-// each column costs one reciprocal square root (Cholesky) or one reciprocal
-// (LU), after which the lanes update their rows independently.
+// The blocks are assembled and solved in FP64.  On this GPU a dependent FP64
+// operation takes about 64 cycles and an FP64 warp instruction holds the
+// SM's FP64 pipe for 16 cycles, so a P x P factorisation run by one thread is
+// one long dependent chain (about a thousand FP64 operations for P = 10, with
+// divisions and square roots; 94 us for one block of 64 atoms).  Here a group
+// of G lanes (G a power of two >= P) shares one atom: lane l holds row l of
+// the damped block, columns are broadcast with shuffles, each column costs
+// one reciprocal square root (Cholesky) or one reciprocal (LU), after which
+// the lanes update their rows independently; the dependent chain per column
+// is a broadcast, the reciprocal and two multiply-adds.
 //
 // Every lane of a warp executes every shuffle (no lane leaves early), so a
 // group whose atom is out of range or masked runs on an identity block and
@@ -174,42 +173,44 @@ int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int 
 // Returns (identically on all lanes of the group) whether every pivot was
 // positive; x[] receives the solution on every lane.
 template <int P, int G>
-__device__ __forceinline__ bool group_cholesky(dfl (&a)[P], dfl b, int l, dfl (&x)[P]) {
-  dfl inv[P], col[P];
+__device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l,
+                                               double (&x)[P]) {
+  constexpr unsigned kAll = 0xffffffffu;
+  double inv[P], col[P];
   bool spd = true;
 #pragma unroll
-  for (int k = 0; k < P; ++k) col[k] = df_make(0.f);
+  for (int k = 0; k < P; ++k) col[k] = 0.0;
 #pragma unroll
   for (int j = 0; j < P; ++j) {
-    const dfl piv = df_shfl(a[j], j, G);
-    const bool pos = piv.hi > 0.f;
-    spd = spd && pos;
-    const dfl ij = df_rsqrt(pos ? piv : df_make(1.f));
+    const double piv = __shfl_sync(kAll, a[j], j, G);
+    spd = spd && (piv > 0.0);
+    const double ij = rsqrt(piv > 0.0 ? piv : 1.0);
     inv[j] = ij;
-    const dfl lij = df_mul(l == j ? piv : a[j], ij);  // L[l][j] for l >= j
+    const double lij = (l == j) ? piv * ij : a[j] * ij;   // L[l][j] for l >= j
     a[j] = lij;
 #pragma unroll
     for (int k = j + 1; k < P; ++k) {
-      const dfl lkj = df_shfl(lij, k, G);
-      if (l == j) col[k] = lkj;          // lane j keeps column j of L
-      a[k] = df_fms(a[k], lij, lkj);     // trailing rows (only k <= l is used)
+      const double lkj = __shfl_sync(kAll, lij, k, G);
+      if (l == j) col[k] = lkj;         // lane j keeps column j of L
+      a[k] = fma(-lij, lkj, a[k]);      // trailing rows (only k <= l is used)
     }
   }
   // forward: y_j = (b_j - sum_{k<j} L[j][k] y_k) / L[j][j]; lane l folds
   // each y_j into its own b as soon as it is known
-  dfl y[P];
+  double y[P];
 #pragma unroll
   for (int j = 0; j < P; ++j) {
-    y[j] = df_mul(df_shfl(b, j, G), inv[j]);
-    b = df_fms(b, a[j], y[j]);
+    y[j] = __shfl_sync(kAll, b, j, G) * inv[j];
+    b = fma(-a[j], y[j], b);
   }
   // backward: x_i = (y_i - sum_{k>i} L[k][i] x_k) / L[i][i]; lane i holds
   // column i of L below the diagonal in col[]
-  dfl acc = df_make(0.f);
+  double acc = 0.0;
 #pragma unroll
   for (int k = P - 1; k >= 0; --k) {
-    x[k] = df_shfl(df_mul(df_sub(y[k], acc), inv[k]), k, G);
-    acc = df_add(acc, df_mul(col[k], x[k]));
+    const double v = (y[k] - acc) * inv[k];
+    x[k] = __shfl_sync(kAll, v, k, G);
+    acc = fma(col[k], x[k], acc);
   }
   return spd;
 }
@@ -221,46 +222,47 @@ __device__ __forceinline__ bool group_cholesky(dfl (&a)[P], dfl b, int l, dfl (&
 // column c with the multiplier a[c] * (1 / pivot).  Returns false for a
 // zero pivot column.
 template <int P, int G>
-__device__ __forceinline__ bool group_lu(dfl (&a)[P], dfl b, int l, dfl (&x)[P]) {
+__device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, double (&x)[P]) {
+  constexpr unsigned kAll = 0xffffffffu;
   bool used = l >= P;                   // padding lanes never pivot
   bool ok = true;
   int prow[P];
-  dfl pinv[P];
+  double pinv[P];
 #pragma unroll
   for (int c = 0; c < P; ++c) {
-    float v = used ? -1.f : fabsf(a[c].hi);
+    double v = used ? -1.0 : fabs(a[c]);
     int idx = l;
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, v, off, G);
-      const int oi = __shfl_xor_sync(0xffffffffu, idx, off, G);
+      const double ov = __shfl_xor_sync(kAll, v, off, G);
+      const int oi = __shfl_xor_sync(kAll, idx, off, G);
       if (ov > v || (ov == v && oi < idx)) {
         v = ov;
         idx = oi;
       }
     }
-    ok = ok && (v > 0.f);
-    const dfl piv = df_shfl(a[c], idx, G);
-    const dfl pi = df_rcp(piv.hi != 0.f ? piv : df_make(1.f));
+    ok = ok && (v > 0.0);
+    const double piv = __shfl_sync(kAll, a[c], idx, G);
+    const double pi = 1.0 / (piv != 0.0 ? piv : 1.0);
     prow[c] = idx;
     pinv[c] = pi;
     const bool elim = !used && l != idx;
-    const dfl m = df_mul(a[c], pi);
+    const double m = a[c] * pi;
 #pragma unroll
     for (int k = c + 1; k < P; ++k) {
-      const dfl pk = df_shfl(a[k], idx, G);
-      if (elim) a[k] = df_fms(a[k], m, pk);
+      const double pk = __shfl_sync(kAll, a[k], idx, G);
+      if (elim) a[k] = fma(-m, pk, a[k]);
     }
-    const dfl pb = df_shfl(b, idx, G);
-    if (elim) b = df_fms(b, m, pb);
+    const double pb = __shfl_sync(kAll, b, idx, G);
+    if (elim) b = fma(-m, pb, b);
     used = used || l == idx;
   }
   // back substitution in pivot order: row prow[c] holds U[c][c..P-1]; every
   // lane folds each x_k into its rhs as soon as it is known
 #pragma unroll
   for (int c = P - 1; c >= 0; --c) {
-    x[c] = df_shfl(df_mul(b, pinv[c]), prow[c], G);
-    b = df_fms(b, a[c], x[c]);
+    x[c] = __shfl_sync(kAll, b * pinv[c], prow[c], G);
+    b = fma(-a[c], x[c], b);
   }
   return ok;
 }
@@ -283,24 +285,21 @@ __global__ void __launch_bounds__(128)
   const bool live = j < n;
   const bool active = live && (mask == nullptr || mask[j] != 0);
   const bool row = live && l < P;
-  dfl a[P], b, x[P];
+  double a[P], b, x[P];
   // the damped diagonal entry of row l, formed once
-  const dfl diag = row ? df_add(df_from_double(H[((size_t)j * P + l) * P + l]),
-                                df_from_double(lam[j]))
-                       : df_make(1.f);
+  const double diag = row ? H[((size_t)j * P + l) * P + l] + lam[j] : 1.0;
   auto load = [&]() {
 #pragma unroll
     for (int k = 0; k < P; ++k)
-      a[k] = k == l ? diag
-                    : (row ? df_from_double(H[((size_t)j * P + l) * P + k]) : df_make(0.f));
-    b = row ? df_neg(df_from_double(g[(size_t)j * P + l])) : df_make(0.f);
+      a[k] = k == l ? diag : (row ? H[((size_t)j * P + l) * P + k] : 0.0);
+    b = row ? -g[(size_t)j * P + l] : 0.0;
   };
   load();
   bool ok = group_cholesky<P, G>(a, b, l, x);
   if (__any_sync(kAll, !ok)) {          // some group of this warp is not positive definite
     const bool chol_ok = ok;
     load();
-    dfl xl[P];
+    double xl[P];
     const bool lu_ok = group_lu<P, G>(a, b, l, xl);
     if (!chol_ok) {
       ok = lu_ok;
@@ -310,14 +309,14 @@ __global__ void __launch_bounds__(128)
   }
 #pragma unroll
   for (int k = 0; k < P; ++k)
-    if (!(x[k].hi == x[k].hi) || fabsf(x[k].hi) > 1e30f) ok = false;
+    if (!(x[k] == x[k]) || fabs(x[k]) > 1e30) ok = false;
   ok = ok && active;
   // lane l: its step component and parameter
-  dfl mine = df_make(0.f);
+  double mine = 0.0;
 #pragma unroll
   for (int k = 0; k < P; ++k)
     if (k == l) mine = x[k];
-  const double d = (ok && row) ? df_to_double(mine) : 0.0;
+  const double d = (ok && row) ? mine : 0.0;
   double th = row ? theta[(size_t)j * P + l] : 0.0;
   th += d;
   // |dtheta| over the group, fixed butterfly order

@@ -7,7 +7,7 @@ fitted; every admitted request owns its device buffers and a CUDA stream, and
 one damped-Newton iteration
 
   gr_atom_derivs(all atoms)      -> gradient and Hessian blocks
-  gr_newton_solve                -> trial parameters (double-float block solves)
+  gr_newton_solve                -> trial parameters (FP64 block solves)
   gr_fit_forward(trial atoms)    -> trial fit fields, trial loss
   gr_newton_accept_fields        -> device-side accept/reject, damping update,
                                     loss history; an accepted trial's fields

@@ -329,7 +329,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (compensated sums; FP64 loss, float-pair chunk sums)", "data": "synthetic (seeded; reference datasets absent)",
+        "dtype": "f32 (FP64 reductions)", "data": "synthetic (seeded; reference datasets absent)",
         "config": {"workload": W.name, "atoms": N, "detector": list(geom.shape),
                    "fit": fit, "order": order, "in_support_pairs_per_pass": S,
                    "dense_pairs_per_pass": dense, "l2": "flushed between steps (256 MB write)",
@@ -571,7 +571,7 @@ def run_serving(args):
     out = {
         "metric": "served fits/s (config 3 stream)", "value": fits_s, "unit": "fits/s",
         "n_gpus": ws, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (FP64 loss reductions, float-pair Newton solves)",
+        "dtype": "f32 (FP64 reductions and Newton solves)",
         "data": "synthetic (seeded per request)",
         "config": {"workload": "config3: %d requests, Poisson 200/s, 2D p=0.6 else 3D tilt, "
                                "atoms log-U[16,4096], angles U[30,180], detector U[64,512]/side, "
