@@ -350,6 +350,7 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(W, args.cpu_seconds)
+        out["parity_vs_fp64_oracle"] = oracle_parity(W, engine, geometry, dev, order)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:
@@ -435,6 +436,106 @@ def cpu_sample(W, budget_s, threads):
         n_done += len(sel)
         n_take = min(2 * n_take, 64)
     return done_pairs, done_t, n_done
+
+
+def _relerr(a, ref):
+    """max |a - ref| / max |ref|"""
+    a, ref = np.asarray(a, dtype=np.float64), np.asarray(ref, dtype=np.float64)
+    scale = np.max(np.abs(ref))
+    return float(np.max(np.abs(a - ref)) / scale) if scale > 0 else float(np.max(np.abs(a)))
+
+
+def _entry_relerr(a, ref):
+    """max over atoms and entries of |a - ref|, each entry scaled by its
+    largest |ref| over the atoms (the overall maximum where that is ~0)"""
+    a, ref = np.asarray(a, dtype=np.float64), np.asarray(ref, dtype=np.float64)
+    tot = np.max(np.abs(ref))
+    scale = np.max(np.abs(ref), axis=0)
+    scale = np.where(scale > 1e-9 * tot, scale, tot)
+    return float(np.max(np.abs(a - ref) / scale)) if tot > 0 else float(np.max(np.abs(a)))
+
+
+def oracle_parity(W, engine, geometry, dev, order, max_dense=6e7):
+    """Max relative error of the GPU engine against the FP64 oracle on the
+    bench workload, on identical (float32-rounded) inputs: sinogram, loss,
+    per-atom gradient and Hessian of the fit, and the damped Newton step
+    (lam = 1) from gr_newton_solve against an FP64 solve of the oracle's
+    blocks.  Where the dense oracle would evaluate more than max_dense (atom,
+    cell) pairs, a seeded sample of atoms and angles is compared."""
+    import torch
+    from oracle import gauss_oracle as go
+    solvers = importlib.import_module(PKG + ".solvers")
+    I, x, r = (np.asarray(v, dtype=np.float32).astype(np.float64) for v in W.init)
+    n, A = len(I), len(W.orientations)
+    cells = int(np.prod([len(d) for d in W.detector]))
+    sel_j, sel_a = np.arange(n), np.arange(A)
+    sample = "full problem (%d atoms, %d angles)" % (n, A)
+    if n * A * cells > max_dense:
+        rng = np.random.default_rng(7)
+        n_j = min(n, 32)
+        n_a = int(max(1, min(A, max_dense // (n_j * cells))))
+        sel_j = np.sort(rng.choice(n, n_j, replace=False))
+        sel_a = np.sort(rng.choice(A, n_a, replace=False))
+        sample = "seeded sample of %d atoms x %d angles" % (n_j, n_a)
+    T = np.asarray(W.orientations)[sel_a]
+    ortho = tuple(np.asarray(o)[sel_a] for o in W.ortho)
+    data = np.asarray(W.data)[sel_a].astype(np.float32)
+    Is, xs, rs = I[sel_j], x[sel_j], r.reshape(n, -1)[sel_j]
+    geom = geometry.DeviceGeometry(T, ortho, W.detector, dev)
+    atoms = engine.DeviceAtoms(Is, xs, rs, dev)
+    data_d = torch.from_numpy(data).to(dev).contiguous()
+    fw = engine.fit_forward(atoms, geom, data_d, W.fit, W.background, want_R=True)
+    bc = 1.0 if W.fit == "l2" else 0.0
+    _f, gg, HH = engine.atom_derivs(atoms, geom, "field", fw["alpha"], fw["beta"], bc, order)
+    sub = type("Sub", (), dict(orientations=T, ortho=ortho, detector=W.detector))
+    og = oracle_geometry(sub)
+    d64 = data.astype(np.float64)
+    Ro = go.radproj(Is, xs, rs, og)
+    if W.fit == "kl":
+        lo = go.kl_value(d64, Ro, W.background)
+        al, be = go.kl_fields(d64, Ro, W.background)
+    else:
+        lo = 0.5 * float(np.sum((Ro - d64) ** 2))
+        al, be = Ro - d64, np.ones(og.shape)
+    _fo, go_, Ho = go.all_atom_derivs("field", Is, xs, rs, og, al, order, beta=be)
+    rep = {"sample": sample,
+           "sinogram": _relerr(fw["R"].cpu().numpy(), Ro),
+           "loss": abs(float(fw["loss"].item()) - lo) / abs(lo),
+           "gradient": _entry_relerr(gg.cpu().numpy(), go_),
+           "definition": "max |gpu - fp64 oracle| / max |oracle| (sinogram); relative "
+                         "(loss); per parameter entry, scaled by its largest |oracle| "
+                         "over the atoms (gradient, Hessian, Newton step). newton_step "
+                         "compares the damped step (lam = 1) from the GPU's blocks with "
+                         "the FP64 step from the oracle's, so it carries cond(H + I) "
+                         "times the blocks' FP32 error; newton_solve_same_blocks solves "
+                         "the GPU's own blocks in FP64 with numpy"}
+    if order > 1:
+        rep["hessian"] = _entry_relerr(HH.cpu().numpy(), Ho)
+        dim, iso = atoms.dim, atoms.iso
+        theta = solvers.theta_of(atoms.I, atoms.x, atoms.r)
+        lam = torch.ones(len(Is), dtype=torch.float64, device=dev)
+        th, _s, _fl = engine.newton_solve(dim, iso, gg.contiguous(), HH.contiguous(), lam, theta)
+        step_gpu = (th - theta).cpu().numpy()
+        th0 = theta.cpu().numpy()
+        P = th0.shape[1]
+
+        def fp64_steps(gv, Hv):
+            out = np.zeros_like(step_gpu)
+            for j in range(len(Is)):
+                d = np.linalg.solve(Hv[j] + np.eye(P), -gv[j])
+                I1, x1, r1 = solvers.step_params(th0[j, 0], th0[j, 1:1 + dim],
+                                                 th0[j, 1 + dim:], d, dim, iso)
+                out[j] = np.concatenate([[I1], x1, np.atleast_1d(r1)]) - th0[j]
+            return out
+        # end to end: the step from the GPU's blocks against the step from the
+        # oracle's (this carries cond(H + I) times the blocks' FP32 error)
+        rep["newton_step"] = _entry_relerr(step_gpu, fp64_steps(go_, Ho))
+        # the solve alone: the same GPU blocks solved by numpy in FP64
+        rep["newton_solve_same_blocks"] = _entry_relerr(
+            step_gpu, fp64_steps(gg.cpu().numpy(), HH.cpu().numpy()))
+        conds = [np.linalg.cond(Ho[j] + np.eye(P)) for j in range(len(Is))]
+        rep["block_condition_number_median"] = float(np.median(conds))
+    return rep
 
 
 def cpu_baseline(W, budget_s):
