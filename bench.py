@@ -328,6 +328,9 @@ def run_ours(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        # one step = one loss + gradient (+ Hessian for order 2) evaluation of
+        # every atom against the whole sinogram
+        "gradient_evaluations_per_s": ws * 1e3 / ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (FP64 reductions)", "data": "synthetic (seeded; reference datasets absent)",
         "config": {"workload": W.name, "atoms": N, "detector": list(geom.shape),
