@@ -99,14 +99,22 @@ _TORCH_DTYPE = {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch
                 np.dtype(np.int32): torch.int32, np.dtype(np.uint8): torch.uint8}
 
 
+_DTYPES = {t: np.dtype(t) for t in (np.float32, np.float64, np.int32, np.uint8)}
+
+
 def _layout(items):
     """Byte layout of (name, dtype, shape) buffers packed at 256-byte
-    offsets: ({name: (offset, dtype, shape, nbytes)}, total bytes)."""
+    offsets: ({name: (offset, dtype, shape, nbytes)}, total bytes).  Plain
+    integer arithmetic: admission runs this for every request."""
     out, off = {}, 0
     for name, dt, shape in items:
-        dt = np.dtype(dt)
-        nb = int(np.prod(shape, dtype=np.int64)) * dt.itemsize
-        out[name] = (off, dt, tuple(int(v) for v in shape), nb)
+        dt = _DTYPES[dt]
+        shape = tuple(int(v) for v in shape)
+        k = 1
+        for v in shape:
+            k *= v
+        nb = k * dt.itemsize
+        out[name] = (off, dt, shape, nb)
         off += (nb + _ALIGN - 1) // _ALIGN * _ALIGN
     return out, max(off, _ALIGN)
 
@@ -189,6 +197,7 @@ class _Slot:
             _host_view(host, lay[name])[...] = val
         for k, d in enumerate(det_h):
             _host_view(host, lay["det%d" % k])[...] = d
+        t_host = time.perf_counter()
         self.arena_in = torch.empty(n_in, dtype=torch.uint8, device=device)
         with torch.cuda.stream(setup):
             self.arena_in.copy_(self.staging[:n_in], non_blocking=True)
@@ -259,7 +268,8 @@ class _Slot:
                 except _lib.EngineError:
                     self.loop = None
             t_loop = time.perf_counter()
-            self.phase_seconds = {"buffers": t_bufs - t_start, "streams": t_cap - t_bufs,
+            self.phase_seconds = {"host_prep": t_host - t_start, "buffers": t_bufs - t_host,
+                                  "streams": t_cap - t_bufs,
                                   "capture": t_loop - t_cap}
             if self.loop is not None:
                 self.iterations_launched = 0
