@@ -133,8 +133,10 @@ def _host_view(arr, spec):
 
 # Pinned host buffers, pooled by power-of-two capacity for the life of the
 # process: pinning memory is a slow driver call, and a request needs two
-# buffers (input staging, results).
+# buffers (input staging, results).  At most _PINNED_KEEP free buffers are
+# kept per capacity; the rest are released.
 _pinned_free = {}
+_PINNED_KEEP = 64
 
 
 def _pinned_take(nbytes):
@@ -146,7 +148,9 @@ def _pinned_take(nbytes):
 
 
 def _pinned_give(buf):
-    _pinned_free.setdefault(buf.numel(), []).append(buf)
+    free = _pinned_free.setdefault(buf.numel(), [])
+    if len(free) < _PINNED_KEEP:
+        free.append(buf)
 
 
 class _Slot:
