@@ -64,6 +64,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, ws, device):
+    """The largest x over the ranks (every rank gets it); x itself at ws = 1.
+    device: where the collective's tensor lives (cuda under NCCL, cpu under
+    gloo)."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_step, steps, ws, total_ms):
+    """Units per second over all ranks: every rank processes units_per_step
+    per step (replicas), and the job takes the slowest rank's total_ms."""
+    return units_per_step * steps * ws / (total_ms * 1e-3)
+
+
 # --------------------------------------------------------------------------
 # clocks sampled during the timed region
 # --------------------------------------------------------------------------
@@ -250,12 +268,9 @@ def run_ours(args):
     t_fwd = [a.elapsed_time(b) for a, b, _ in ev]
     t_der = [b.elapsed_time(c) for _, b, c in ev]
     total_ms = graph_ms
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, ws, dev)
     ms_step = total_ms / args.steps
-    value = S * args.steps * ws / (total_ms * 1e-3)
+    value = whole_job_rate(S, args.steps, ws, total_ms)
 
     # ---- end-to-end through the API with host buffers ----------------------
     # engine.FitStep: every step copies the atoms and data from pinned host
