@@ -340,6 +340,30 @@ def run_ours(args):
         "traffic": traffic,
     }
 
+    # what bounds these kernels: instruction issue (each in-support
+    # evaluation costs one ex2 but 10-30 other instructions).  Issued warp
+    # instructions per launch from the committed ncu capture, over the live
+    # launch time, against every scheduler issuing one per clock
+    instr = profiled_instructions(W.name, dom_kernel)
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    issue_peak = n_sm * 4 * sm_mhz * 1e6
+    roofline_issue = None
+    if instr is not None:
+        roofline_issue = {
+            "bound": "issue",
+            "kernel": dom_kernel,
+            "achieved": instr / (dom_ms * 1e-3) / 1e9,
+            "peak": issue_peak / 1e9,
+            "unit": "G warp instructions/s",
+            "frac": instr / (dom_ms * 1e-3) / issue_peak,
+            "peak_source": "%d SMs x 4 schedulers x 1 warp instruction per clock at the "
+                           "median SM clock sampled in the timed region" % n_sm,
+            "instructions_per_launch": instr,
+            "instructions_source": "ncu smsp__inst_executed.sum of the committed capture "
+                                   "(profiles/instructions.json)",
+        }
+
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -363,7 +387,7 @@ def run_ours(args):
                 "api": "engine.FitStep (one CUDA graph: H2D, fit, derivatives, D2H)",
                 "loss": e2e_loss},
         "gpu_launches": launches, "gpu_launches_per_step": launches / args.steps,
-        "roofline": roofline, "roofline_hbm": roofline_hbm,
+        "roofline": roofline, "roofline_hbm": roofline_hbm, "roofline_issue": roofline_issue,
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -374,6 +398,18 @@ def run_ours(args):
     if ws > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
+
+
+def profiled_instructions(workload, kernel):
+    """Warp instructions per launch of the kernel from the committed ncu
+    summary (profiles/instructions.json), or None when not profiled."""
+    p = os.path.join(ROOT, "profiles", "instructions.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        tab = json.load(f)
+    v = tab.get(workload.split(":")[0], {}).get(kernel)
+    return None if v is None else float(v)
 
 
 def profiled_traffic(workload, kernel):
