@@ -568,11 +568,15 @@ __global__ void __launch_bounds__(128)
 
 // Sum chunk partials (FP64) in chunk order, expand the packed Hessian and
 // apply the isotropic chain rule r_aniso = (s, .., s, 0, ..).  A block covers
-// 32 atoms; its 8 warps share out the partial values (reads of consecutive
-// atoms are coalesced), then all its threads write the atoms' outputs.
+// kFinAtoms atoms; thread t sums values q = t / kFinAtoms, + 32, ... of atom
+// t % kFinAtoms (the loads of consecutive atoms share sectors), then all the
+// block's threads write the atoms' outputs.  Few atoms per block spread the
+// FP64 adds over many SMs' FP64 pipes (16 cycles per warp instruction each).
 constexpr int kRedSlices = 8;
+constexpr int kFinAtoms = 8;
+constexpr int kFinThreads = 32 * kRedSlices;
 template <int K>
-__global__ void __launch_bounds__(32 * kRedSlices)
+__global__ void __launch_bounds__(kFinThreads)
     gr_deriv_finalize_kernel(const float *part, DerivCfg cfg, int n, int deriv_order,
                              int r_iso, DerivOut out, const double *f_extra,
                              const int *order) {
@@ -580,12 +584,12 @@ __global__ void __launch_bounds__(32 * kRedSlices)
   constexpr int P = n_par<K>();
   constexpr int QN = 1 + P + P * (P + 1) / 2;
   // chunk sums in FP64 in chunk order: thread (atom, ty) sums values
-  // q = ty, ty + kRedSlices, ... of its atom, all loads independent
-  __shared__ double vs[QN][32];
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int slot = blockIdx.x * 32 + tx;
+  // q = ty, ty + 32, ... of its atom, all loads independent
+  __shared__ double vs[QN][kFinAtoms];
+  const int tx = threadIdx.x % kFinAtoms, ty = threadIdx.x / kFinAtoms;
+  const int slot = blockIdx.x * kFinAtoms + tx;
   if (slot < n)
-    for (int q = ty; q < cfg.qn; q += kRedSlices) {
+    for (int q = ty; q < cfg.qn; q += kFinThreads / kFinAtoms) {
       double t = 0.0;
 #pragma unroll 4
       for (int c = 0; c < cfg.nchunks; ++c) t += (double)part[((size_t)c * cfg.qn + q) * n + slot];
@@ -594,9 +598,9 @@ __global__ void __launch_bounds__(32 * kRedSlices)
   __syncthreads();
   // outputs of the block's atoms, written by all threads from the sums
   // (consecutive threads write consecutive entries of an atom's block)
-  const int nb = min(32, n - (int)blockIdx.x * 32);
+  const int nb = min(kFinAtoms, n - (int)blockIdx.x * kFinAtoms);
   auto atom_of = [&](int t) {
-    const int sl = blockIdx.x * 32 + t;
+    const int sl = blockIdx.x * kFinAtoms + t;
     return order ? order[sl] : sl;
   };
   // entry (a, b) of the full Hessian from the packed upper triangle
@@ -797,12 +801,12 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
     }
   }
   timer_mark(2, 1, stream);
-  const int fblocks = (at.n + 31) / 32;
+  const int fblocks = (at.n + kFinAtoms - 1) / kFinAtoms;
   if (K == 1)
-    gr_deriv_finalize_kernel<1><<<fblocks, 32 * kRedSlices, 0, stream>>>(
+    gr_deriv_finalize_kernel<1><<<fblocks, kFinThreads, 0, stream>>>(
         part, c, at.n, in.order, at.r_iso, out, fe, at.order);
   else
-    gr_deriv_finalize_kernel<2><<<fblocks, 32 * kRedSlices, 0, stream>>>(
+    gr_deriv_finalize_kernel<2><<<fblocks, kFinThreads, 0, stream>>>(
         part, c, at.n, in.order, at.r_iso, out, fe, at.order);
   note_launches(2);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
