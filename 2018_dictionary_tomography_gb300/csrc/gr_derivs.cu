@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(128)
 // block's threads write the atoms' outputs.  Few atoms per block spread the
 // FP64 adds over many SMs' FP64 pipes (16 cycles per warp instruction each).
 constexpr int kRedSlices = 8;
-constexpr int kFinAtoms = 8;
+constexpr int kFinAtoms = 4;
 constexpr int kFinThreads = 32 * kRedSlices;
 template <int K>
 __global__ void __launch_bounds__(kFinThreads)
