@@ -272,7 +272,7 @@ __device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, double
 // with mask[j] == 0 keep their parameters.  One group of G lanes per atom;
 // after the solve lane l forms parameter l only.
 template <int P, int D, int G>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(32)
     gr_newton_solve_kernel(int n, const double *g, const double *H,
                            const double *lam, const double *theta,
                            const unsigned char *mask, double *theta_new,
@@ -455,15 +455,17 @@ int launch_newton_solve(int dim, int iso, int n, const double *g, const double *
                         const unsigned char *mask, double *theta_new,
                         double *step_norm, int *fail, AtomOut ao, cudaStream_t stream) {
   if (n <= 0) return kOk;
-  auto blocks = [n](int G) { return (unsigned)(((size_t)n * G + 127) / 128); };
+  // one warp per block: the FP64 work of a few atoms per warp then spreads
+  // over as many SMs' FP64 pipes as there are warps
+  auto blocks = [n](int G) { return (unsigned)(((size_t)n * G + 31) / 32); };
   if (dim == 2 && iso)
-    gr_newton_solve_kernel<4, 2, 8><<<blocks(8), 128, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<4, 2, 8><<<blocks(8), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else if (dim == 2)
-    gr_newton_solve_kernel<6, 2, 8><<<blocks(8), 128, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<6, 2, 8><<<blocks(8), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else if (iso)
-    gr_newton_solve_kernel<5, 3, 8><<<blocks(8), 128, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<5, 3, 8><<<blocks(8), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else
-    gr_newton_solve_kernel<10, 3, 16><<<blocks(16), 128, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<10, 3, 16><<<blocks(16), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
