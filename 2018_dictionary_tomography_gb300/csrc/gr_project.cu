@@ -680,13 +680,38 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   }
 }
 
-constexpr int kLossThreads = 1024;
+// Fixed-order FP64 sum of n loss partials over many blocks (one block's FP64
+// pipe, at 16 cycles per warp instruction, would take ~0.3 ms for the 640k
+// partials of 20000 images): block b sums the contiguous segment
+// [b seg, (b + 1) seg), each thread a strided part of it, then a fixed tree;
+// the last block to finish reduces the block sums with a fixed tree.
+// bsum: gridDim.x doubles (<= kLossMaxBlocks); done: a counter zeroed before
+// the launch.
+constexpr int kLossThreads = 256;
+constexpr int kLossMaxBlocks = 256;
 __global__ void __launch_bounds__(kLossThreads)
-    gr_loss_finalize_kernel(const double *part, int n, double *out) {
+    gr_loss_finalize_kernel(const double *part, int n, double *out, double *bsum, int *done) {
   __shared__ double sh[kLossThreads];
+  __shared__ int s_last;
+  const int seg = (n + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int lo = blockIdx.x * seg, hi = min(n, lo + seg);
   double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) s += part[i];
   sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    bsum[blockIdx.x] = sh[0];
+    __threadfence();
+    s_last = atomicAdd(done, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  sh[threadIdx.x] = (int)threadIdx.x < (int)gridDim.x ? __ldcg(bsum + threadIdx.x) : 0.0;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
@@ -766,6 +791,7 @@ size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1)
   size_t bytes = align_up(2 * sizeof(int));
   bytes += align_up(items * W * sizeof(uint32_t));
   bytes += align_up(items * sizeof(double));
+  bytes += align_up(kLossMaxBlocks * sizeof(double));  // block sums of the loss finalize
   return bytes;
 }
 
@@ -847,7 +873,15 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   timer_mark(1, 1, stream);
   note_launches(1);
   if (loss_out && !fused_loss) {
-    gr_loss_finalize_kernel<<<1, kLossThreads, 0, stream>>>(loss_part, (int)items, loss_out);
+    // about 8 partials per thread, at most kLossMaxBlocks blocks; the
+    // finished-block counter (next_item + 1) is unused when the loss is not
+    // fused into the projection
+    size_t lb = (items + kLossThreads * 8 - 1) / (kLossThreads * 8);
+    lb = lb < 1 ? 1 : (lb > kLossMaxBlocks ? kLossMaxBlocks : lb);
+    double *bsum = loss_part + align_up(items * sizeof(double)) / sizeof(double);
+    gr_loss_finalize_kernel<<<(unsigned)lb, kLossThreads, 0, stream>>>(loss_part, (int)items,
+                                                                        loss_out, bsum,
+                                                                        next_item + 1);
     note_launches(1);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
