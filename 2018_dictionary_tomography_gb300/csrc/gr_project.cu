@@ -247,10 +247,29 @@ __global__ void __launch_bounds__(kProjWarps * 32)
 
   // epilogue: write the tile, fused fit fields and loss partial; a split
   // item's cells combine the warps' sums in warp order
+  // The data values of a batch of a thread's cells are loaded before any of
+  // them is written (the output fields may alias nothing, but the compiler
+  // cannot know that), so a batch costs one memory latency, not one per cell.
+  constexpr int kPer = ROWS / NW;                 // cells per thread
+  constexpr int kBatch = kPer < (NW == 1 ? 8 : 4) ? kPer : (NW == 1 ? 8 : 4);
+  static_assert(kPer % kBatch == 0, "batch");
+  const bool want_data = out.epilogue == kEpiL2 || out.epilogue == kEpiKL;
+  const int e0 = NW == 1 ? lane : (int)threadIdx.x;
+  const int col = c0 + lane;
   float lsum = 0.f, lcmp = 0.f;
-  for (int e = (NW == 1 ? lane : (int)threadIdx.x); e < ROWS * 32; e += NW * 32) {
-    const int lr = e >> 5;
-    const int row = r0 + lr, col = c0 + lane;
+  for (int eb = 0; eb < kPer; eb += kBatch) {
+    float dv[kBatch];
+#pragma unroll
+    for (int i = 0; i < kBatch; ++i) {
+      const int row = r0 + ((e0 + (eb + i) * NW * 32) >> 5);
+      dv[i] = (want_data && row < D0 && col < D1)
+                  ? __ldg(out.data + ((size_t)a * D0 + row) * D1 + col)
+                  : 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < kBatch; ++i) {
+    const int lr = (e0 + (eb + i) * NW * 32) >> 5;
+    const int row = r0 + lr;
     if (row >= D0 || col >= D1) continue;
     const int ci = lr * S + lane;
     float v;
@@ -272,11 +291,11 @@ __global__ void __launch_bounds__(kProjWarps * 32)
     if (out.R) out.R[gi] = v;
     float l = 0.f;
     if (out.epilogue == kEpiL2) {
-      const float res = v - out.data[gi];
+      const float res = v - dv[i];
       if (out.alpha) out.alpha[gi] = res;
       l = 0.5f * res * res;
     } else if (out.epilogue == kEpiKL) {
-      const float fo = out.data[gi];
+      const float fo = dv[i];
       const float gg = v + out.bg;
       const float ig = 1.f / gg;
       if (out.alpha) out.alpha[gi] = 1.f - fo * ig;
@@ -286,6 +305,7 @@ __global__ void __launch_bounds__(kProjWarps * 32)
     const float tt = lsum + l;
     lcmp += (fabsf(lsum) >= fabsf(l)) ? ((lsum - tt) + l) : ((l - tt) + lsum);
     lsum = tt;
+    }
   }
   if (out.loss_part) {
     double d = warp_sum_d((double)lsum + (double)lcmp);

@@ -358,6 +358,32 @@ __global__ void __launch_bounds__(32)
   }
 }
 
+// dst[e] = src[e] for e in [0, n), the grid's threads striding from t0 by
+// stride: float4 accesses when both arrays are 16-byte aligned, four of them
+// loaded before any is stored, so a thread keeps 64 bytes in flight (a
+// one-float copy loop keeps one float: the stores may alias the next loads).
+__device__ __forceinline__ void copy_field(const float *__restrict__ src, float *__restrict__ dst,
+                                           size_t n, size_t t0, size_t stride) {
+  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) != 0u) {
+    for (size_t e = t0; e < n; e += stride) dst[e] = src[e];
+    return;
+  }
+  const size_t n4 = n / 4;
+  const float4 *s4 = reinterpret_cast<const float4 *>(src);
+  float4 *d4 = reinterpret_cast<float4 *>(dst);
+  size_t e = t0;
+  for (; e + 3 * stride < n4; e += 4 * stride) {
+    const float4 v0 = __ldcs(s4 + e), v1 = __ldcs(s4 + e + stride);
+    const float4 v2 = __ldcs(s4 + e + 2 * stride), v3 = __ldcs(s4 + e + 3 * stride);
+    d4[e] = v0;
+    d4[e + stride] = v1;
+    d4[e + 2 * stride] = v2;
+    d4[e + 3 * stride] = v3;
+  }
+  for (; e < n4; e += stride) d4[e] = __ldcs(s4 + e);
+  for (size_t i = 4 * n4 + t0; i < n; i += stride) dst[i] = src[i];
+}
+
 // Device-side accept/reject of a batched Newton trial (no host round trip):
 // if loss_trial <= loss_cur the trial parameters (FP64 and the float32 atom
 // arrays) become current, loss_cur takes the trial loss and the damping
@@ -388,11 +414,10 @@ __global__ void __launch_bounds__(256)
   }
   // an accepted trial's fit fields become the current ones (so the next
   // iteration needs no projection of the current atoms)
-  if (acc && fc.alpha)
-    for (size_t e = t0; e < fc.n; e += stride) {
-      fc.alpha[e] = fc.alpha_t[e];
-      if (fc.beta) fc.beta[e] = fc.beta_t[e];
-    }
+  if (acc && fc.alpha) {
+    copy_field(fc.alpha_t, fc.alpha, fc.n, t0, stride);
+    if (fc.beta) copy_field(fc.beta_t, fc.beta, fc.n, t0, stride);
+  }
   if (t0 == 0) {
     if (acc) *loss_cur = *loss_trial;
     const int k = *counter;
@@ -413,11 +438,10 @@ __global__ void __launch_bounds__(256)
                             const float *alpha_t, float *alpha, const float *beta_t,
                             float *beta, size_t n) {
   if (!(*loss_cur == *loss_trial)) return;  // rejected: keep the current fields
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x) {
-    alpha[e] = alpha_t[e];
-    if (beta) beta[e] = beta_t[e];
-  }
+  const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  copy_field(alpha_t, alpha, n, t0, stride);
+  if (beta) copy_field(beta_t, beta, n, t0, stride);
 }
 
 int launch_accept_fields(const double *loss_cur, const double *loss_trial, const float *alpha_t,
@@ -425,8 +449,8 @@ int launch_accept_fields(const double *loss_cur, const double *loss_trial, const
                          cudaStream_t stream) {
   if (!loss_cur || !loss_trial || !alpha_t || !alpha || (beta && !beta_t)) return kErrArg;
   if (n == 0) return kOk;
-  size_t blocks = (n + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  size_t blocks = (n / 4 + 255) / 256;       // a float4 per thread at least
+  blocks = blocks < 1 ? 1 : (blocks > 152 * 16 ? 152 * 16 : blocks);
   gr_accept_fields_kernel<<<(unsigned)blocks, 256, 0, stream>>>(loss_cur, loss_trial, alpha_t,
                                                                 alpha, beta_t, beta, n);
   note_launches(1);
