@@ -43,7 +43,8 @@ EXPORTS = ("gr_version", "gr_preload", "gr_status_string", "gr_workspace_bytes",
            "gr_launch_count", "gr_atom_step", "gr_newton_solve", "gr_volproj", "gr_newton_accept",
            "gr_psf_radproj", "gr_psf_fit_forward", "gr_psf_atom_derivs", "gr_psf_volproj",
            "gr_set_tuning", "gr_get_tuning", "gr_kernel_timer", "gr_kernel_timer_read",
-           "gr_fit_loop_begin", "gr_fit_loop_end", "gr_fit_loop_instantiate",
+           "gr_fit_loop_begin", "gr_fit_loop_end", "gr_fit_loop_gate_begin",
+           "gr_fit_loop_gate_end", "gr_fit_loop_instantiate",
            "gr_fit_loop_launch", "gr_fit_loop_destroy", "gr_regulariser",
            "gr_sino_moments", "gr_accept_fields", "gr_newton_accept_fields")
 
@@ -148,6 +149,10 @@ def load(build_if_missing=True):
         lib.gr_fit_loop_end.restype = ctypes.c_int
         lib.gr_fit_loop_end.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_double, ctypes.c_int, vp]
+        lib.gr_fit_loop_gate_begin.restype = ctypes.c_int
+        lib.gr_fit_loop_gate_begin.argtypes = [vp, vp, vp, vp, ctypes.c_int]
+        lib.gr_fit_loop_gate_end.restype = ctypes.c_int
+        lib.gr_fit_loop_gate_end.argtypes = [vp, vp]
         lib.gr_fit_loop_instantiate.restype = ctypes.c_int
         lib.gr_fit_loop_instantiate.argtypes = [vp]
         lib.gr_fit_loop_launch.restype = ctypes.c_int

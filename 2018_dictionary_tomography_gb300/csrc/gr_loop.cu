@@ -17,6 +17,8 @@
 // history says.
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "gr_kernels.cuh"
 
 namespace gr {
@@ -29,7 +31,25 @@ struct FitLoop {
   int *guard = nullptr;
   bool capturing = false;
   bool captured_ok = false;
+  // an IF node in the body whose work runs only when the atoms moved
+  cudaGraphConditionalHandle gate = 0;
+  cudaGraphNode_t gate_node = nullptr;
+  bool gated = false;          // capturing into the IF node's body now
+  bool failed = false;         // a gate step failed: the capture is unusable
 };
+
+// Before the gated part of an iteration: its work (the derivatives of the
+// current atoms) runs unless the previous trial was rejected, since a
+// rejected trial leaves the atoms, their fit fields and so their
+// derivatives unchanged (recomputing them would give the same bits).
+__global__ void gr_fit_loop_gate_kernel(cudaGraphConditionalHandle gate, const int *hist_acc,
+                                        const int *counter, int hist_len) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int c = counter[0];
+  unsigned run = 1u;
+  if (c > 0 && c <= hist_len) run = hist_acc[c - 1] ? 1u : 0u;
+  cudaGraphSetConditional(gate, run);
+}
 
 // Stop test after an iteration (the same rule as the host-driven loop):
 //   * c >= max_iter iterations done, or
@@ -110,11 +130,93 @@ int fit_loop_begin(cudaStream_t stream, int *guard, FitLoop **out) {
   return kOk;
 }
 
+// The nodes that later captured work on stream depends on.
+static bool capture_deps(cudaStream_t stream, std::vector<cudaGraphNode_t> &deps) {
+  cudaStreamCaptureStatus st;
+  const cudaGraphNode_t *d = nullptr;
+  size_t nd = 0;
+  if (cudaStreamGetCaptureInfo(stream, &st, nullptr, nullptr, &d, nullptr, &nd) != cudaSuccess ||
+      st != cudaStreamCaptureStatusActive)
+    return false;
+  deps.assign(d, d + nd);
+  return true;
+}
+
+// Capture moves into the body of an IF node: a gate kernel (captured into
+// the loop body) sets the IF condition each iteration from the accept
+// history; the work issued on stream until fit_loop_gate_end is captured
+// into the IF node's body.  The capture is ended and restarted around the
+// node, so the body graph is never edited while it is being captured into.
+int fit_loop_gate_begin(FitLoop *L, cudaStream_t stream, const int *hist_acc, const int *counter,
+                        int hist_len) {
+  if (!L || !L->capturing || L->gated || L->gate_node) return kErrArg;
+  if (!hist_acc || !counter || hist_len < 1) return kErrArg;
+  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  std::vector<cudaGraphNode_t> deps;
+  cudaGraph_t g = nullptr;
+  bool ok = capture_deps(stream, deps) && cudaStreamEndCapture(stream, &g) == cudaSuccess;
+  ok = ok && cudaGraphConditionalHandleCreate(&L->gate, L->body, 1u,
+                                              cudaGraphCondAssignDefault) == cudaSuccess;
+  ok = ok && cudaStreamBeginCaptureToGraph(stream, L->body, deps.empty() ? nullptr : deps.data(),
+                                           nullptr, deps.size(), mode) == cudaSuccess;
+  if (ok) {
+    gr_fit_loop_gate_kernel<<<1, 32, 0, stream>>>(L->gate, hist_acc, counter, hist_len);
+    ok = cudaGetLastError() == cudaSuccess && capture_deps(stream, deps) &&
+         cudaStreamEndCapture(stream, &g) == cudaSuccess;
+  }
+  cudaGraphNodeParams p = {};
+  if (ok) {
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = L->gate;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    ok = cudaGraphAddNode(&L->gate_node, L->body, deps.empty() ? nullptr : deps.data(), nullptr,
+                          deps.size(), &p) == cudaSuccess;
+  }
+  ok = ok && cudaStreamBeginCaptureToGraph(stream, p.conditional.phGraph_out[0], nullptr,
+                                           nullptr, 0, mode) == cudaSuccess;
+  if (!ok) {
+    // leave the stream capturing into the loop body so the caller's
+    // fit_loop_end still ends the capture (and reports the failure)
+    cudaStreamCaptureStatus st;
+    if (cudaStreamIsCapturing(stream, &st) != cudaSuccess || st != cudaStreamCaptureStatusActive)
+      cudaStreamBeginCaptureToGraph(stream, L->body, nullptr, nullptr, 0, mode);
+    L->failed = true;
+    return kErrLaunch;
+  }
+  L->gated = true;
+  return kOk;
+}
+
+// Capture returns to the loop body, after the IF node.
+int fit_loop_gate_end(FitLoop *L, cudaStream_t stream) {
+  if (!L || !L->capturing || !L->gated) return kErrArg;
+  L->gated = false;
+  cudaGraph_t g = nullptr;
+  const bool ended = cudaStreamEndCapture(stream, &g) == cudaSuccess;
+  const bool ok = ended && cudaStreamBeginCaptureToGraph(stream, L->body, &L->gate_node, nullptr,
+                                                         1, cudaStreamCaptureModeThreadLocal) ==
+                               cudaSuccess;
+  if (!ok) {
+    cudaStreamCaptureStatus st;
+    if (cudaStreamIsCapturing(stream, &st) != cudaSuccess || st != cudaStreamCaptureStatusActive)
+      cudaStreamBeginCaptureToGraph(stream, L->body, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal);
+    L->failed = true;
+    return kErrLaunch;
+  }
+  return kOk;
+}
+
 int fit_loop_end(FitLoop *L, cudaStream_t stream, const double *hist, const int *hist_acc,
                  const int *counter, int hist_len, int max_iter, int max_reject, double tol,
                  int guard_max, int *stop_flag) {
   if (!L || !L->capturing) return kErrArg;
-  int rc = kOk;
+  int rc = L->failed ? kErrLaunch : kOk;
+  if (L->gated) {              // a gated part left open: close it, fail the loop
+    fit_loop_gate_end(L, stream);
+    rc = kErrArg;
+  }
   if (!hist || !hist_acc || !counter || hist_len < 1 || max_iter < 1 || max_reject < 1 ||
       guard_max < 1)
     rc = kErrArg;
@@ -158,7 +260,9 @@ int fit_loop_destroy(FitLoop *L) {
   return kOk;
 }
 
-int preload_loop() { return preload_fn(gr_fit_loop_stop_kernel); }
+int preload_loop() {
+  return preload_fn(gr_fit_loop_stop_kernel) + preload_fn(gr_fit_loop_gate_kernel);
+}
 
 }  // namespace gr
 
@@ -177,6 +281,17 @@ int gr_fit_loop_end(void *loop, void *stream, const double *hist, const int *his
   return gr::fit_loop_end(static_cast<gr::FitLoop *>(loop), static_cast<cudaStream_t>(stream),
                           hist, hist_acc, counter, hist_len, max_iter, max_reject, tol, guard_max,
                           stop_flag);
+}
+
+int gr_fit_loop_gate_begin(void *loop, void *stream, const int *hist_acc, const int *counter,
+                           int hist_len) {
+  return gr::fit_loop_gate_begin(static_cast<gr::FitLoop *>(loop),
+                                 static_cast<cudaStream_t>(stream), hist_acc, counter, hist_len);
+}
+
+int gr_fit_loop_gate_end(void *loop, void *stream) {
+  return gr::fit_loop_gate_end(static_cast<gr::FitLoop *>(loop),
+                               static_cast<cudaStream_t>(stream));
 }
 
 int gr_fit_loop_instantiate(void *loop) {

@@ -8,6 +8,7 @@ is missing.
 Atoms are ``(I (N,), x (N, d), r (N, P_r) or (N,) / (N, 1) isotropic)``;
 geometry is a :class:`DeviceGeometry`.
 """
+import contextlib
 import ctypes
 import threading
 
@@ -530,7 +531,7 @@ class FitLoop:
     """
 
     def __init__(self, stream, capture_iteration, hist, hist_acc, counter, max_iter,
-                 max_reject, tol, device):
+                 max_reject, tol, device, pass_loop=False):
         lib = _lib.load()
         self._lib = lib
         self.stream = stream
@@ -548,7 +549,10 @@ class FitLoop:
             self.handle = h
             t1 = time.perf_counter()
             try:
-                capture_iteration()
+                if pass_loop:
+                    capture_iteration(self)
+                else:
+                    capture_iteration()
             finally:
                 t2 = time.perf_counter()
                 rc = lib.gr_fit_loop_end(
@@ -564,6 +568,23 @@ class FitLoop:
         if rc != 0:
             self.close()
             _lib.check(rc, "gr_fit_loop_end")
+
+    @contextlib.contextmanager
+    def unless_rejected(self):
+        """During the capture (``pass_loop=True``): the work issued inside
+        runs on an iteration only if the previous trial was accepted (or on
+        the first iteration).  A rejected trial leaves the atoms and their
+        fit fields unchanged, so derivatives issued here would reproduce
+        the previous outputs bit for bit (``gr_fit_loop_gate_begin``)."""
+        _hist, hist_acc, counter = self._keep
+        sh = ctypes.c_void_p(self.stream.cuda_stream)
+        _lib.check(self._lib.gr_fit_loop_gate_begin(self.handle, sh, hist_acc.data_ptr(),
+                                                    counter.data_ptr(), int(hist_acc.numel())),
+                   "gr_fit_loop_gate_begin")
+        try:
+            yield
+        finally:
+            _lib.check(self._lib.gr_fit_loop_gate_end(self.handle, sh), "gr_fit_loop_gate_end")
 
     def launch(self):
         _lib.check(self._lib.gr_fit_loop_launch(self.handle,

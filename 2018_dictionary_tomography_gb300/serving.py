@@ -47,6 +47,7 @@ way.
 eager host-driven loop, one host sync per iteration.
 """
 import collections
+import contextlib
 import time
 
 import numpy as np
@@ -268,7 +269,7 @@ class _Slot:
                 try:
                     self.loop = engine.FitLoop(stream, self.iterate, self.hist, self.hist_acc,
                                                self.counter, req.max_iter, MAX_BACKTRACK,
-                                               req.tol, device)
+                                               req.tol, device, pass_loop=True)
                 except _lib.EngineError:
                     self.loop = None
             t_loop = time.perf_counter()
@@ -312,14 +313,17 @@ class _Slot:
         engine.fit_forward_into(self.cur, self.geom, self.data, r.fit, r.background, None,
                                 self.alpha, self.beta, self.loss_cur, self.ws_p)
 
-    def iterate(self):
+    def iterate(self, loop=None):
         """One damped-Newton iteration.  The current atoms' fields are always
         valid here (from the prologue, an accepted trial, or unchanged after
-        a rejected one), so only the trial is projected."""
+        a rejected one), so only the trial is projected.  Captured into a
+        device loop (``loop``), the derivatives are skipped after a rejected
+        trial: the atoms did not move, so g and H still hold their values."""
         r = self.req
         beta_c = 1.0 if r.fit == "l2" else 0.0
-        engine.atom_derivs_into(self.cur, self.geom, "field", self.alpha, self.beta, beta_c, 2,
-                                self.f, self.g, self.H, self.ws_d)
+        with (loop.unless_rejected() if loop is not None else contextlib.nullcontext()):
+            engine.atom_derivs_into(self.cur, self.geom, "field", self.alpha, self.beta, beta_c,
+                                    2, self.f, self.g, self.H, self.ws_d)
         engine.newton_solve_into(self.dim, self.iso, self.g, self.H, self.lam, self.theta,
                                  self.theta_trial, self.step, self.trial, self.dev)
         engine.fit_forward_into(self.trial, self.geom, self.data, r.fit, r.background, None,

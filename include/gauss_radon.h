@@ -381,6 +381,14 @@ int gr_accept_fields(const double *loss_cur, const double *loss_trial, const flo
  *       gr_atom_derivs, gr_newton_solve, gr_fit_forward of the trial atoms,
  *       gr_newton_accept; no other stream, no host synchronisation, no
  *       allocation);
+ *   inside that iteration, gr_fit_loop_gate_begin(loop, stream, hist_acc,
+ *       counter, hist_len) ... gr_fit_loop_gate_end(loop, stream) may
+ *       bracket the derivative evaluation of the current atoms: the work
+ *       issued between them goes into the body of an IF node that runs
+ *       unless the previous trial was rejected (hist_acc[counter - 1] == 0),
+ *       whose atoms, fit fields and derivatives are unchanged, so the
+ *       previous outputs stand bit for bit.  At most one gated part per
+ *       loop; an unclosed one makes gr_fit_loop_end fail with GR_ERR_ARG;
  *   gr_fit_loop_end(loop, stream, hist, hist_acc, counter, hist_len,
  *       max_iter, max_reject, tol, guard_max, stop_flag) appends the stop
  *       test and ends the capture;
@@ -405,6 +413,9 @@ int gr_fit_loop_begin(void *stream, int *guard, void **loop);
 int gr_fit_loop_end(void *loop, void *stream, const double *hist, const int *hist_acc,
                     const int *counter, int hist_len, int max_iter, int max_reject,
                     double tol, int guard_max, int *stop_flag);
+int gr_fit_loop_gate_begin(void *loop, void *stream, const int *hist_acc, const int *counter,
+                           int hist_len);
+int gr_fit_loop_gate_end(void *loop, void *stream);
 int gr_fit_loop_instantiate(void *loop);
 int gr_fit_loop_launch(void *loop, void *stream);
 int gr_fit_loop_destroy(void *loop);

@@ -104,3 +104,37 @@ def test_device_loop_matches_host_stepped_graphs(cuda_ready):
     for k in dev:
         assert dev[k]["iterations"] == host[k]["iterations"]
         assert np.array_equal(dev[k]["theta"], host[k]["theta"])
+
+
+def test_gated_derivatives_match_eager_loop_after_rejections(cuda_ready):
+    """In the device loop the derivative launches sit in an IF node that
+    skips them after a rejected trial (the atoms did not move).  On a fit
+    that rejects trials, the result equals bit for bit the eager loop, which
+    evaluates the derivatives at every iteration."""
+    dev = torch.device("cuda")
+    reqs = workloads.config3_requests(n=48, seed=3)
+    # a 2D request of 40 atoms that rejects about a quarter of its trials
+    req = [r for r in reqs if len(r.init[1][0]) == 2 and r.size_hint[0] == 40][0]
+    workloads.materialize_data([req], dev)
+    srv = serving.GaussFitServer(dev, max_slots=2, n_streams=1)
+    st = srv.streams[0]
+    s = serving._Slot(req, st, dev, True, 4, True, srv.setup_stream)
+    assert s.loop is not None
+    with torch.cuda.stream(st):
+        s.launch()
+    torch.cuda.synchronize()
+    gated = s.result()
+    acc = s.h_acc.numpy()[:gated["iterations"]]
+    assert (acc == 0).any() and (acc == 1).any()
+    e = serving._Slot(req, st, dev, False, 1, False, srv.setup_stream)
+    assert e.loop is None
+    while True:
+        torch.cuda.synchronize()
+        if e.done():
+            break
+        e.launch()
+    eager = e.result()
+    assert gated["iterations"] == eager["iterations"]
+    assert np.array_equal(gated["theta"], eager["theta"])
+    assert gated["loss"] == eager["loss"]
+    s.loop.close()
