@@ -82,3 +82,18 @@ def test_tuning_keys_round_trip_without_gpu():
             assert lib.gr_set_tuning(key, saved) == 0
     assert lib.gr_get_tuning(99) == -1
     assert lib.gr_set_tuning(99, 1) == -1
+
+
+def test_fit_loop_calls_reject_bad_arguments_without_gpu():
+    """The device-loop calls check their arguments before any CUDA call: a
+    null loop is GR_ERR_ARG for every step, including the gated section."""
+    lib_mod = importlib.import_module("2018_dictionary_tomography_gb300._lib")
+    lib = lib_mod.load()
+    err = lib_mod.GR_OK - 1  # GR_ERR_ARG
+    assert lib.gr_fit_loop_gate_begin(None, None, None, None, 1) == err
+    assert lib.gr_fit_loop_gate_end(None, None) == err
+    assert lib.gr_fit_loop_end(None, None, None, None, None, 1, 1, 1, 0.0, 1, None) == err
+    assert lib.gr_fit_loop_instantiate(None) == err
+    assert lib.gr_fit_loop_launch(None, None) == err
+    assert lib.gr_fit_loop_destroy(None) == lib_mod.GR_OK
+    assert lib.gr_fit_loop_begin(None, None, None) == err
