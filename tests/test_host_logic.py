@@ -1,0 +1,109 @@
+"""Host-side logic of the serving path and the fit-step graph, on the CPU:
+arena layouts and views, the memory estimate used for admission, and the
+seeded served-stream generator."""
+import importlib
+
+import numpy as np
+import torch
+
+PKG = "2018_dictionary_tomography_gb300"
+serving = importlib.import_module(PKG + ".serving")
+engine = importlib.import_module(PKG + ".engine")
+workloads = importlib.import_module(PKG + ".workloads")
+
+
+def _items():
+    return [("theta", np.float64, (37, 10)), ("flags", np.uint8, (5,)),
+            ("counter", np.int32, (1,)), ("empty", np.float32, (0, 4)),
+            ("field", np.float32, (3, 17, 19)), ("scalar", np.float64, ())]
+
+
+def test_layout_is_aligned_disjoint_and_sized():
+    spec, total = serving._layout(_items())
+    ends = []
+    for name, dt, shape in _items():
+        off, sdt, sshape, nb = spec[name]
+        assert off % serving._ALIGN == 0, name
+        assert sdt == np.dtype(dt) and sshape == tuple(shape)
+        assert nb == int(np.prod(shape, dtype=np.int64)) * np.dtype(dt).itemsize
+        ends.append((off, off + nb))
+    ends.sort()
+    for (a0, a1), (b0, _b1) in zip(ends, ends[1:]):
+        assert a1 <= b0
+    assert total >= ends[-1][1] and total % serving._ALIGN == 0
+    # an empty request still gets a non-empty arena
+    assert serving._layout([])[1] == serving._ALIGN
+
+
+def test_device_and_host_views_agree_and_do_not_alias():
+    spec, total = serving._layout(_items())
+    buf = torch.zeros(total, dtype=torch.uint8)
+    arr = buf.numpy()                       # the same memory, seen from numpy
+    rng = np.random.default_rng(0)
+    for name, dt, shape in _items():
+        v = serving._view(buf, spec[name])
+        assert tuple(v.shape) == tuple(shape)
+        vals = rng.integers(0, 100, size=shape).astype(dt)
+        v.copy_(torch.from_numpy(np.array(vals)))  # keeps 0-d shapes
+    # every buffer still holds its own values (no view overlaps another)
+    rng = np.random.default_rng(0)
+    for name, dt, shape in _items():
+        vals = rng.integers(0, 100, size=shape).astype(dt)
+        assert np.array_equal(serving._host_view(arr, spec[name]), vals), name
+        assert np.array_equal(serving._view(buf, spec[name]).numpy(), vals), name
+
+
+def test_fit_step_packing_is_aligned_and_disjoint():
+    items = [("I", (7,)), ("x", (7, 3)), ("r", (7, 6)), ("data", (5, 11, 13)), ("loss", ())]
+    spec, total = engine._pack(items)
+    buf = torch.zeros(total, dtype=torch.float64)
+    for k, (name, shape) in enumerate(items):
+        off, sshape = spec[name]
+        assert off % 64 == 0 and tuple(sshape) == tuple(shape)
+        engine._packed_view(buf, spec[name]).fill_(k + 1)
+    for k, (name, shape) in enumerate(items):
+        assert bool((engine._packed_view(buf, spec[name]) == k + 1).all()), name
+
+
+def test_memory_estimate_grows_with_the_problem():
+    reqs = workloads.config3_requests(n=40, seed=5)
+    est = [(serving.GaussFitServer.estimate_bytes(r), r) for r in reqs]
+    assert all(b > 0 for b, _ in est)
+    # the estimate covers at least the request's fit fields and data (float32)
+    for b, r in est:
+        assert b >= 3 * 4 * r.size_hint[1]
+    # more cells, same atoms: a larger estimate
+    r = reqs[0]
+    small = serving.GaussFitServer.estimate_bytes(r)
+    n, cells = r.size_hint
+    r.size_hint = (n, 4 * cells)
+    try:
+        assert serving.GaussFitServer.estimate_bytes(r) > small
+    finally:
+        r.size_hint = (n, cells)
+
+
+def test_served_stream_is_seeded_and_within_its_ranges():
+    a = workloads.config3_requests(n=64, seed=9)
+    b = workloads.config3_requests(n=64, seed=9)
+    c = workloads.config3_requests(n=64, seed=10)
+    arr = [r.arrival for r in a]
+    assert arr == sorted(arr) and arr[0] > 0
+    assert arr == [r.arrival for r in b]
+    assert arr != [r.arrival for r in c]
+    dims = []
+    for ra, rb in zip(a, b):
+        n, cells = ra.size_hint
+        assert (n, cells) == rb.size_hint
+        for xa, xb in zip(ra.init, rb.init):
+            assert np.array_equal(xa, xb)
+        dim = len(ra.init[1][0])
+        dims.append(dim)
+        assert 16 <= n <= 4096
+        A = len(ra.orientations)
+        assert 30 <= A <= 180
+        D = len(ra.detector[0])
+        assert 64 <= D <= 512
+        assert cells == A * D ** (dim - 1)
+        assert ra.fit == "l2" and ra.max_iter == 100
+    assert set(dims) == {2, 3}
