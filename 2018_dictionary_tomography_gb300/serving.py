@@ -387,9 +387,10 @@ class _Slot:
         """Parameters, loss and iteration count from the pinned copies (call
         after the completion event: no stream sync, so other requests
         queued on the same stream are not waited for)."""
-        c = int(self.h_counter[0])
+        c = min(int(self.h_counter[0]), self.req.max_iter)
+        acc = self.h_acc.numpy()[:min(c, self.h_acc.numel())]
         return {"theta": self.h_theta.numpy().copy(), "loss": float(self.h_loss[0]),
-                "iterations": min(c, self.req.max_iter)}
+                "iterations": c, "rejected": int((acc == 0).sum())}
 
 
 _warmed = set()

@@ -742,6 +742,10 @@ def run_serving(args):
             "served_admission_host_s": admit_cmp,
             "served_admission_phases_s": phases_cmp,
             "served_device_loops": loops_cmp,
+            # trials rejected by the device-side accept; the next iteration
+            # of the device loop skips its derivatives (atoms unchanged)
+            "served_trials": int(sum(v["iterations"] for v in served_cmp.values())),
+            "served_rejected_trials": int(sum(v.get("rejected", 0) for v in served_cmp.values())),
             "served_latency_p99_s": pct([v["latency"] for v in served_cmp.values()], 99),
             "plain_latency_p99_s": pct([v["latency"] for v in plain.values()], 99),
         },
