@@ -9,7 +9,11 @@
 // on one stream) into the body of a WHILE node; gr_fit_loop_end appends
 // gr_fit_loop_stop_kernel, which reads the loss history that the accept
 // kernel writes and decides on the device whether to run another iteration.
-// A whole fit is then one graph launch with no host round trip.
+// A whole fit is then one graph launch with no host round trip.  Inside the
+// iteration, gr_fit_loop_gate_begin / _end put the derivative evaluation into
+// the body of an IF node that a gate kernel opens only after an accepted
+// trial (or on the first iteration): a rejected trial leaves the atoms and
+// so their derivatives unchanged.
 //
 // Termination does not depend on the fit: the stop kernel counts the body's
 // executions in its own guard word (cleared by a memset node ahead of the
