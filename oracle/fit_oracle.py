@@ -94,8 +94,23 @@ def newton(I, x, r, geom, data, max_iter, kind="l2", bg=0.0, tol=1e-4, min_iter=
     return (I, x, r), E[:jj], F[:jj]
 
 
+def _reference_block_grad(df, t, b, D, pr):
+    """Block gradient as GD_lib.linesearch_block forms it (GD_lib.py:138-151):
+    the slice is chosen by loop position t (df[0], df[1:1+D], df[1+D:]), the
+    null regulariser's gradient of block b (shape (1,), (1,D) or (1,pr),
+    regularisation.py null.grad) is added with numpy broadcasting, and the
+    step is taken along grad[0]."""
+    g = df[0] if t == 0 else (df[1:1 + D] if t == 1 else df[1 + D:])
+    shape = {"I": (1,), "x": (1, D), "r": (1, pr)}[b]
+    g = g + np.zeros(shape)
+    return g, g[0]
+
+
 def gd_block(I, x, r, geom, data, max_iter, kind="l2", bg=0.0, dim_str="xrI", tol=1e-4,
-             min_iter=1):
+             min_iter=1, slicing="block"):
+    """slicing="block": each block steps along its own gradient (the corrected
+    rule); slicing="reference": the reference's position-sliced gradient
+    (_reference_block_grad), for pinning against the reference's own loop."""
     I = np.array(I, dtype=np.float64)
     x = np.array(x, dtype=np.float64)
     r = np.array(r, dtype=np.float64).reshape(I.size, -1)
@@ -119,11 +134,14 @@ def gd_block(I, x, r, geom, data, max_iter, kind="l2", bg=0.0, dim_str="xrI", to
                 for t, b in enumerate(blocks):
                     al, be = _fields(kind, R, data, bg)
                     _, df, _dd = go.atom_derivs("field", I[j], x[j], r[j], geom, al, 1, beta=be)
-                    grad = df[sl[b]]
+                    if slicing == "reference":
+                        grad, step = _reference_block_grad(df, t, b, D, r.shape[1])
+                    else:
+                        grad = step = df[sl[b]]
                     cur = {"I": np.array([I[j]]), "x": x[j].copy(), "r": r[j].copy()}
                     old = cur[b].copy()
-                    h[t][j] = min(h[t][j], 1 / max(np.linalg.norm(grad), eps))
-                    T = old - h[t][j] * grad
+                    h[t][j] = min(h[t][j], 1 / max(np.sqrt((grad * grad).sum()), eps))
+                    T = old - h[t][j] * step
                     new = dict(cur)
                     new[b] = T
                     R_old = go.radproj(I[j:j + 1], x[j:j + 1], r[j:j + 1], geom)
