@@ -20,8 +20,8 @@ namespace gr {
 
 constexpr int kMaxK = 2;                          // detector dimensions
 constexpr float kNegThirtyLog2e = -43.28085122666891f;  // -30 / ln 2
-constexpr int kFrameStride2D = 8;   // T(2) w0(2) wt0(2) pad(2)
-constexpr int kFrameStride3D = 16;  // T(3) w0(3) w1(3) wt0(3) wt1(3) pad(1)
+constexpr int kFrameStride2D = 8;   // T(2) w0(2) wt0(2) wl0(2)
+constexpr int kFrameStride3D = 24;  // T(3) w0(3) w1(3) wt0(3) wt1(3) wl0(3) wl1(3) pad(3)
 
 // Error codes shared with the C ABI.
 enum Status : int {
@@ -120,7 +120,9 @@ template <int K>
 struct Frame {
   float T[K + 1];
   float w[K][K + 1];
-  float wt[K][K + 1];  // rows 0..K-1 of B^{-1}
+  float wt[K][K + 1];  // rows 0..K-1 of B^{-1} (rounded to FP32)
+  const float *wl;     // their rounding residues (B^{-1} rows = wt + wl), read
+                       // from the record only when a pair is set up
 };
 
 template <int K>
@@ -138,6 +140,7 @@ __device__ __forceinline__ void load_frame(const float *frames, int a,
   for (int k = 0; k < K; ++k)
 #pragma unroll
     for (int i = 0; i < D; ++i) f.wt[k][i] = p[D * (1 + K + k) + i];
+  f.wl = p + D * (1 + 2 * K);
 }
 
 // Upper-triangular r as a dense (K+1)x(K+1) matrix.
@@ -261,7 +264,17 @@ __device__ __forceinline__ bool pair_setup(const Atoms &at, int j,
 #pragma unroll
   for (int a = 0; a < D; ++a) xv[a] = at.x[(size_t)D * j + a];
 #pragma unroll
-  for (int k = 0; k < K; ++k) dot2<D>(f.wt[k], xv, p.qh[k], p.ql[k]);
+  // q* = (B^{-1} x)[k] with B^{-1} carried as wt + wl: a dual row rounded to
+  // FP32 alone moves the centre by up to ~4e-8, which for the sharpest atoms
+  // (r ~ 50) is a 2e-5 relative change of the basis at half its peak
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float hi, lo;
+    dot2<D>(f.wt[k], xv, hi, lo);
+#pragma unroll
+    for (int a = 0; a < D; ++a) lo = fmaf(__ldg(f.wl + k * D + a), xv[a], lo);
+    two_sum(hi, lo, p.qh[k], p.ql[k]);
+  }
 
   // support box of m <= 1: |d_i| <= sqrt((G^{-1})_ii)
   float hw[K];

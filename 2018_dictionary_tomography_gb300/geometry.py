@@ -61,7 +61,9 @@ def uniform_grid(coords, name="detector"):
 
 
 def frame_records(orientations, ortho, n_det_axes):
-    """Frame records (FP32) and kdet from reference-layout arrays.
+    """Frame records (FP32) and kdet from reference-layout arrays: T, the
+    detector axes, and the first kdet rows of inverse([w0 (w1) T]) as an FP32
+    pair (rounded rows, then their residues), 8 (2D) or 24 (3D) floats.
 
     orientations (A, 2|3); ortho tuple of (A, 2|3); n_det_axes 1 or 2.
     2D: T, w0 of length 2, one detector axis.  2.5D (reference
@@ -78,7 +80,7 @@ def frame_records(orientations, ortho, n_det_axes):
         B = np.stack([w[0], T], axis=2)               # (A, 2, 2) columns w0, T
         cols = [w[0], T]
     elif dT == 2 and n_det_axes == 2:
-        kdet, stride = 2, 16
+        kdet, stride = 2, 24
         z = np.zeros((A, 1))
         T3 = np.concatenate([T, z], axis=1)
         w03 = np.concatenate([w[0], z], axis=1)
@@ -86,7 +88,7 @@ def frame_records(orientations, ortho, n_det_axes):
         cols = [w03, w13, T3]
         B = np.stack(cols[:2] + [T3], axis=2)
     elif dT == 3 and n_det_axes == 2 and len(w) >= 2:
-        kdet, stride = 2, 16
+        kdet, stride = 2, 24
         cols = [w[0], w[1], T]
         B = np.stack(cols, axis=2)
     else:
@@ -101,8 +103,13 @@ def frame_records(orientations, ortho, n_det_axes):
     rec[:, 0:D] = cols[-1]
     for k in range(kdet):
         rec[:, D * (1 + k):D * (2 + k)] = cols[k]
+    # dual rows as an FP32 pair hi + lo (the kernels form the projection
+    # centre B^{-1} x from both)
+    hi = Binv.astype(np.float32).astype(np.float64)
+    lo = Binv - hi
     for k in range(kdet):
-        rec[:, D * (1 + kdet + k):D * (2 + kdet + k)] = Binv[:, k, :]
+        rec[:, D * (1 + kdet + k):D * (2 + kdet + k)] = hi[:, k, :]
+        rec[:, D * (1 + 2 * kdet + k):D * (2 + 2 * kdet + k)] = lo[:, k, :]
     return rec.astype(np.float32), kdet
 
 

@@ -1,17 +1,22 @@
 """Benchmark of the Gaussian-atom Radon hot path on GB300.
 
-Default workload (config 1): 2D anisotropic atoms, 512 atoms, 180 angles,
-256 detector cells, KL fit on Poisson counts (peak 1e4 photons).  One step is
-one Newton iteration's derivative work for every atom at once: the fused KL
-forward projection (sinogram, weight fields, loss) followed by the per-atom
-gradient and Hessian.
+Default workload (config 4, the largest single-GPU configuration): 8192
+anisotropic 3D atoms projected at 20 000 orientations uniform on SO(3) onto
+128 x 128 images, L2 fit at SNR 0.1.  One step is one gradient evaluation of
+the fit: the fused forward projection (sinogram, residual field, loss)
+followed by the per-atom gradient of every atom, accumulated over all images.
+The other workloads: config 1 (2D anisotropic KL Newton, 512 atoms, 180 x 256;
+gradient and Hessian per step), config 2 (3D tilt series, 4096 atoms,
+121 x 256 x 256), config 3 (the served request stream).
 
 Metric: atom-pixel fwd+grad evaluations per second, counting the useful
 (in-support, m <= 1) atom-cell pairs; each such pair is evaluated once by the
-forward and once by the derivative pass of a step.
+forward and once by the derivative pass of a step.  The default run adds the
+served stream's fits/s and p50/p99 latency against the plain single-problem
+loop (config 3, run in a child process) as the line's "served" object.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload config1|config2|config4]
+                  [--workload config1|config2|config3|config4] [--no-served]
 
 Multi-GPU (torchrun): replicas only -- every rank fits its own problem, no
 collective on the data path; value sums the ranks' work over the slowest
@@ -40,11 +45,13 @@ UNIT = "evals/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config1",
+    ap.add_argument("--workload", default="config4",
                     choices=["config1", "config2", "config3", "config4"])
+    ap.add_argument("--no-served", action="store_true",
+                    help="skip the served-stream sub-run of the default line")
     ap.add_argument("--requests", type=int, default=512,
                     help="config3: requests in the served Poisson stream")
     ap.add_argument("--compare", type=int, default=48,
@@ -372,10 +379,12 @@ def run_ours(args):
         "gradient_evaluations_per_s": ws * 1e3 / ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (FP64 reductions)", "data": "synthetic (seeded; reference datasets absent)",
-        "config": {"workload": W.name, "atoms": N, "detector": list(geom.shape),
-                   "fit": fit, "order": order, "in_support_pairs_per_pass": S,
-                   "dense_pairs_per_pass": dense, "l2": "flushed between steps (256 MB write)",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "config": bench_config(W),
+        "workload_detail": {"atoms": N, "detector": list(geom.shape), "fit": fit,
+                            "order": order, "in_support_pairs_per_pass": S,
+                            "dense_pairs_per_pass": dense,
+                            "l2_between_steps": "flushed (256 MB write)",
+                            "parallelism": "replicas" if ws > 1 else "single GPU"},
         "dense_equiv_evals_per_s": dense * args.steps * ws / (total_ms * 1e-3),
         "ms_per_step_eager": eager_ms,
         "timing": "CUDA events around graph replays of the step (eager per-call and per-kernel "
@@ -390,14 +399,86 @@ def run_ours(args):
         "roofline": roofline, "roofline_hbm": roofline_hbm, "roofline_issue": roofline_issue,
         "clocks": clocks,
     }
+    if rank == 0:
+        out["e2e_dropin"] = dropin_e2e(W, S, dev)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(W, args.cpu_seconds)
         out["parity_vs_fp64_oracle"] = oracle_parity(W, engine, geometry, dev, order)
+    if rank == 0 and ws == 1 and args.workload == "config4" and not args.no_served:
+        out["served"] = served_subrun()
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
+
+
+def bench_config(W):
+    """The line's config: the workload, and how L2 is kept from serving the
+    inputs between steps (the same for both arms)."""
+    data_bytes = int(np.prod(W.shape)) * 4
+    l2 = ("inputs larger than L2 (%.2f GB data sinogram per step)" % (data_bytes / 1e9)
+          if data_bytes > 129e6 else "L2 flushed between steps (256 MB write)")
+    return {"workload": W.name, "l2": l2}
+
+
+def dropin_e2e(W, S, dev, steps=3):
+    """Forward + gradient through the reference-facing API with host numpy
+    arrays: GaussTomo.__call__ (RadProj into a host sinogram) and
+    GaussTomo.derivs(atoms, R - data, order=1), whose per-atom gradient
+    <dR_j, R - data> is the gradient of 1/2 |R - data|^2 (the calls the
+    reference's fitting code makes, GaussDictCode/atomFuncs.py:115-144).  Every
+    step uploads the atoms and the residual sinogram and downloads the
+    sinogram, the values and the gradients; the residual is formed on the host
+    as the reference does.  Wall-clock time per step."""
+    import torch
+    sp = importlib.import_module(PKG + ".spaces")
+    af = importlib.import_module(PKG + ".atomFuncs")
+    I0, x0, r0 = (np.asarray(v, dtype=np.float32) for v in W.init)
+    dim = x0.shape[1]
+    S_atoms = sp.AtomSpace(dim, isotropic=r0.shape[1] == 1)
+    P = sp.ProjSpace(orientations=W.orientations, ortho=W.ortho, detector=W.detector)
+    Radon = af.GaussTomo(S_atoms, None, P)
+    atoms = S_atoms.element(x0, r0, I0)
+    data = np.asarray(W.data, dtype=np.float32)
+
+    def step():
+        R = Radon(atoms)
+        t1 = time.perf_counter()
+        C = R.data - data
+        t2 = time.perf_counter()
+        f, df = Radon.derivs(atoms, C, order=1)
+        return df, t2 - t1
+    step()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    host_sub = 0.0
+    for _ in range(steps):
+        _df, hs = step()
+        host_sub += hs
+    secs = (time.perf_counter() - t0) / steps
+    cells = int(np.prod(P.shape))
+    return {"value": S / secs, "unit": UNIT, "ms_per_step": secs * 1e3,
+            "host_residual_ms_per_step": host_sub * 1e3 / steps,
+            "h2d_bytes_per_step": cells * 4 + I0.nbytes + x0.nbytes + r0.nbytes,
+            "d2h_bytes_per_step": cells * 4 + len(I0) * (1 + 1 + x0.shape[1] + r0.shape[1]) * 8,
+            "api": "atomFuncs.GaussTomo: __call__ + derivs(order=1) with host numpy arrays "
+                   "(the reference's operator API), wall clock"}
+
+
+def served_subrun(timeout=900):
+    """The served request stream (config 3) in a child process: fits/s, p50/p99
+    latency, and served against the plain single-problem loop."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--workload", "config3"]
+    try:
+        res = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout)
+    except subprocess.TimeoutExpired:
+        return {"error": "served sub-run exceeded %d s" % timeout}
+    lines = [l for l in res.stdout.splitlines() if l.startswith("{")]
+    if res.returncode != 0 or not lines:
+        return {"error": "served sub-run failed (rc %d): %s"
+                % (res.returncode, (res.stderr or "").strip().splitlines()[-1:])}
+    return json.loads(lines[-1])
 
 
 def profiled_instructions(workload, kernel):
@@ -531,17 +612,20 @@ def oracle_parity(W, engine, geometry, dev, order, max_dense=6e7):
         sel_j = np.sort(rng.choice(n, n_j, replace=False))
         sel_a = np.sort(rng.choice(A, n_a, replace=False))
         sample = "seeded sample of %d atoms x %d angles" % (n_j, n_a)
-    T = np.asarray(W.orientations)[sel_a]
-    ortho = tuple(np.asarray(o)[sel_a] for o in W.ortho)
+    # the engine reads float32 geometry: the oracle gets the same rounded values
+    f32 = lambda a: np.asarray(a, dtype=np.float32).astype(np.float64)
+    T = f32(W.orientations)[sel_a]
+    ortho = tuple(f32(o)[sel_a] for o in W.ortho)
+    det = tuple(f32(d) for d in W.detector)
     data = np.asarray(W.data)[sel_a].astype(np.float32)
     Is, xs, rs = I[sel_j], x[sel_j], r.reshape(n, -1)[sel_j]
-    geom = geometry.DeviceGeometry(T, ortho, W.detector, dev)
+    geom = geometry.DeviceGeometry(T, ortho, det, dev)
     atoms = engine.DeviceAtoms(Is, xs, rs, dev)
     data_d = torch.from_numpy(data).to(dev).contiguous()
     fw = engine.fit_forward(atoms, geom, data_d, W.fit, W.background, want_R=True)
     bc = 1.0 if W.fit == "l2" else 0.0
     _f, gg, HH = engine.atom_derivs(atoms, geom, "field", fw["alpha"], fw["beta"], bc, order)
-    sub = type("Sub", (), dict(orientations=T, ortho=ortho, detector=W.detector))
+    sub = type("Sub", (), dict(orientations=T, ortho=ortho, detector=det))
     og = oracle_geometry(sub)
     d64 = data.astype(np.float64)
     Ro = go.radproj(Is, xs, rs, og)
@@ -616,14 +700,19 @@ def run_reference(args):
     from oracle import gauss_oracle as go
 
     def project(I, x, r, T, w, det):
+        # the data sinogram of the workload, projected on the host cores
+        # (each atom visits only its shadow box per angle: same values as the
+        # dense projection, in a time the 20 000-image workload allows)
         g = (go.Geometry(2, T, w[0], det[0]) if len(det) == 1 else
              go.Geometry(25 if T.shape[1] == 2 else 3, T, w[0], det[0],
                          None if T.shape[1] == 2 else w[1], det[1]))
-        return go.radproj(I, x, r, g, dtype=np.float32).astype(np.float64)
+        return go.radproj_boxed(I, x, r, g, dtype=np.float32).astype(np.float64)
 
     gen = {"config1": wl.config1, "config2": wl.config2, "config4": wl.config4}[args.workload]
-    kw = {"n_orient": 64} if args.workload == "config4" else {}
+    kw = {"n_orient": args.n_orient} if (args.workload == "config4" and args.n_orient) else {}
+    t_gen = time.perf_counter()
     W = gen(project=project, **kw)
+    t_gen = time.perf_counter() - t_gen
     threads = os.cpu_count() or 1
     per_step = max(0.05, min(2.0, 120.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
@@ -640,7 +729,8 @@ def run_reference(args):
         "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": W.name},
+        "config": bench_config(W),
+        "workload_generation_s": t_gen,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "per step: sampled atoms, dense FP32 forward + per-atom "
                                    "derivatives over the full sinogram (the reference's "

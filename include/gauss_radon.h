@@ -59,11 +59,13 @@ typedef struct {
 
 /*
  * Projection geometry in device memory.  frames holds one record per angle:
- *   kdet = 1 (2D):  T(2) w0(2) wt0(2) pad(2)                 -> 8 floats
- *   kdet = 2 (3D):  T(3) w0(3) w1(3) wt0(3) wt1(3) pad(1)    -> 16 floats
+ *   kdet = 1 (2D):  T(2) w0(2) wt0(2) wl0(2)                          -> 8 floats
+ *   kdet = 2 (3D):  T(3) w0(3) w1(3) wt0(3) wt1(3) wl0(3) wl1(3) pad(3) -> 24 floats
  * T is the ray direction (ProjSpace.orientations), w0/w1 the detector axes
  * (ProjSpace.ortho), wt0/wt1 the first kdet rows of inverse([w0 w1 T])
- * (equal to w0/w1 for orthonormal frames).  The 2.5D single-axis tilt of the
+ * rounded to float (equal to w0/w1 for orthonormal frames) and wl0/wl1 the
+ * rounding residues (row - wt, in float), from which the kernels form each
+ * atom's projection centre to ~1e-14.  The 2.5D single-axis tilt of the
  * reference (NewtonBases.py:685-688) is the 3D case with T = (T0, T1, 0),
  * w0 = (w00, w01, 0), w1 = (0, 0, 1).
  * det[k] are the detector cell centres (ProjSpace.detector), uniformly spaced

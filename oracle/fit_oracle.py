@@ -6,7 +6,9 @@ GD_lib._step (GD_lib.py:492-536).  GD: GD_lib.linesearch_block
 slicing by loop position and use of grad[0] are treated as defects, see the
 product's solvers module).  Derivatives come from the fidelity in use: L2
 (the reference's L2derivs_RadProj) or KL (weight fields 1 - f/g, f/g^2).
-Every projection is the dense oracle projection; sizes must stay small.
+Projections and per-atom derivatives visit each atom's shadow box per angle
+(go.radproj_boxed, go.atom_derivs(boxed=True)): the same sums as the dense
+evaluation, cheap enough for the benchmark configurations.
 """
 import numpy as np
 
@@ -56,7 +58,7 @@ def newton(I, x, r, geom, data, max_iter, kind="l2", bg=0.0, tol=1e-4, min_iter=
     F = np.zeros_like(E)
     h = [1.0] * n
     eps = 1e-4
-    R = go.radproj(I, x, r, geom)
+    R = go.radproj_boxed(I, x, r, geom)
     F[0] = E[0] = _loss(kind, R, data, bg)
     np.random.seed(1)
     jj = 1
@@ -66,12 +68,12 @@ def newton(I, x, r, geom, data, max_iter, kind="l2", bg=0.0, tol=1e-4, min_iter=
             for _ in range(max_iter[1]):
                 BREAK[1] = True
                 al, be = _fields(kind, R, data, bg)
-                _, df, ddf = go.atom_derivs("field", I[j], x[j], r[j], geom, al, 2, beta=be)
+                _, df, ddf = go.atom_derivs("field", I[j], x[j], r[j], geom, al, 2, beta=be, boxed=True)
                 ddf = ddf + np.eye(df.size) / h[j]
                 dx = np.linalg.solve(ddf, -df)
                 I1, x1, r1 = _step_params(I[j], x[j], r[j], dx, dim, iso)
-                R_old = go.radproj(I[j:j + 1], x[j:j + 1], r[j:j + 1], geom)
-                R_new = go.radproj(np.array([I1]), x1.reshape(1, -1), r1.reshape(1, -1), geom)
+                R_old = go.radproj_boxed(I[j:j + 1], x[j:j + 1], r[j:j + 1], geom)
+                R_new = go.radproj_boxed(np.array([I1]), x1.reshape(1, -1), r1.reshape(1, -1), geom)
                 Rt = R + R_new - R_old
                 F[jj] = E[jj] = _loss(kind, Rt, data, bg)
                 if E[jj] > E[jj - 1]:
@@ -122,7 +124,7 @@ def gd_block(I, x, r, geom, data, max_iter, kind="l2", bg=0.0, dim_str="xrI", to
     h = [[1e-2] * n for _ in blocks]
     eps = 1e-8
     sl = {"I": slice(0, 1), "x": slice(1, 1 + D), "r": slice(1 + D, None)}
-    R = go.radproj(I, x, r, geom)
+    R = go.radproj_boxed(I, x, r, geom)
     F[0] = E[0] = _loss(kind, R, data, bg)
     np.random.seed(1)
     jj = 1
@@ -133,7 +135,8 @@ def gd_block(I, x, r, geom, data, max_iter, kind="l2", bg=0.0, dim_str="xrI", to
                 BREAK[1] = True
                 for t, b in enumerate(blocks):
                     al, be = _fields(kind, R, data, bg)
-                    _, df, _dd = go.atom_derivs("field", I[j], x[j], r[j], geom, al, 1, beta=be)
+                    _, df, _dd = go.atom_derivs("field", I[j], x[j], r[j], geom, al, 1, beta=be,
+                                                    boxed=True)
                     if slicing == "reference":
                         grad, step = _reference_block_grad(df, t, b, D, r.shape[1])
                     else:
@@ -144,8 +147,8 @@ def gd_block(I, x, r, geom, data, max_iter, kind="l2", bg=0.0, dim_str="xrI", to
                     T = old - h[t][j] * step
                     new = dict(cur)
                     new[b] = T
-                    R_old = go.radproj(I[j:j + 1], x[j:j + 1], r[j:j + 1], geom)
-                    R_new = go.radproj(new["I"], new["x"].reshape(1, -1),
+                    R_old = go.radproj_boxed(I[j:j + 1], x[j:j + 1], r[j:j + 1], geom)
+                    R_new = go.radproj_boxed(new["I"], new["x"].reshape(1, -1),
                                        new["r"].reshape(1, -1), geom)
                     Rt = R + R_new - R_old
                     F[jj] = E[jj] = _loss(kind, Rt, data, bg)
@@ -175,7 +178,7 @@ def newton_batched(I, x, r, geom, data, iters, kind="l2", bg=0.0, lam0=1.0, lam_
     r = np.array(r, dtype=np.float64).reshape(I.size, -1)
     dim = geom.dim
     iso = r.shape[1] == 1
-    R = go.radproj(I, x, r, geom)
+    R = go.radproj_boxed(I, x, r, geom)
     loss = _loss(kind, R, data, bg)
     losses = [loss]
     lam = lam0
@@ -188,7 +191,7 @@ def newton_batched(I, x, r, geom, data, iters, kind="l2", bg=0.0, lam0=1.0, lam_
             for j in range(I.size):
                 d = np.linalg.solve(H[j] + lam * np.eye(H.shape[1]), -g[j])
                 In[j], xn[j], rn[j] = _step_params(I[j], x[j], r[j], d, dim, iso)
-            Rn = go.radproj(In, xn, rn, geom)
+            Rn = go.radproj_boxed(In, xn, rn, geom)
             new = _loss(kind, Rn, data, bg)
             if new <= loss:
                 I, x, r, R, loss = In, xn, rn, Rn, new

@@ -34,6 +34,8 @@ def lib():
         _lib = ctypes.CDLL(path)
         for sfx in ("_f64", "_f32"):
             getattr(_lib, "or_radproj" + sfx).restype = ctypes.c_int
+            getattr(_lib, "or_radproj_boxed" + sfx).restype = ctypes.c_int
+            getattr(_lib, "or_atom_derivs_boxed" + sfx).restype = ctypes.c_int
             getattr(_lib, "or_atom_derivs" + sfx).restype = ctypes.c_int
             getattr(_lib, "or_point_derivs" + sfx).restype = ctypes.c_int
             getattr(_lib, "or_volproj" + sfx).restype = ctypes.c_int
@@ -166,8 +168,25 @@ def radproj(I, x, r, geom, dtype=np.float64, nthreads=None):
     return out
 
 
+def radproj_boxed(I, x, r, geom, dtype=np.float64, nthreads=None):
+    """radproj visiting only each atom's shadow box per angle (same result:
+    every cell outside the boxes is exactly zero in the dense sum)."""
+    dim = geom.dim
+    g = geom.cast(dtype)
+    I = np.ascontiguousarray(I, dtype=dtype).reshape(-1)
+    x = np.ascontiguousarray(x, dtype=dtype).reshape(-1, dim)
+    r = np.ascontiguousarray(to_aniso(r, dim), dtype=dtype)
+    out = np.empty(geom.shape, dtype=dtype)
+    fn = lib().or_radproj_boxed_f64 if dtype == np.float64 else lib().or_radproj_boxed_f32
+    D1 = 1 if dim == 2 else g.p1.size
+    rc = fn(g.gm, I.size, _p(I), _p(x), _p(r), g.A, _p(g.T), _p(g.w0), _p(g.w1),
+            g.p0.size, _p(g.p0), D1, _p(g.p1), _p(out), _nthreads(nthreads))
+    assert rc == 0
+    return out
+
+
 def atom_derivs(kind, I, x, r, geom, C, order=2, dtype=np.float64, nthreads=None,
-                beta=None):
+                beta=None, boxed=False):
     """Single-atom derivatives summed over all cells.
 
     kind "l2": of 1/2|R(atom) - C|^2;  kind "ip": of <R(atom), C>;
@@ -190,9 +209,12 @@ def atom_derivs(kind, I, x, r, geom, C, order=2, dtype=np.float64, nthreads=None
     f = np.zeros(1)
     Df = np.zeros(P)
     DDf = np.zeros(P * P)
-    fn = lib().or_atom_derivs_f64 if dtype == np.float64 else lib().or_atom_derivs_f32
-    D1 = 1 if dim == 2 else g.p1.size
     code = {"l2": 0, "ip": 1, "field": 2}[kind]
+    if boxed and code == 0:
+        raise ValueError("boxed evaluation covers the 'ip' and 'field' kinds")
+    name = "or_atom_derivs_boxed" if boxed else "or_atom_derivs"
+    fn = getattr(lib(), name + ("_f64" if dtype == np.float64 else "_f32"))
+    D1 = 1 if dim == 2 else g.p1.size
     rc = fn(code, g.gm, _p(I), _p(x), _p(ra), g.A, _p(g.T),
             _p(g.w0), _p(g.w1), g.p0.size, _p(g.p0), D1, _p(g.p1), _p(C), _p(B),
             int(order), _p(f), _p(Df), _p(DDf), _nthreads(nthreads))

@@ -316,6 +316,101 @@ int FN(or_radproj)(int gm, int N, const REAL *I, const REAL *x, const REAL *r,
 }
 
 /*
+ * The same projection, visiting per (angle, atom) only the detector cells
+ * whose coordinates fall inside the atom's shadow box.  The basis support
+ * |r(z - x)| <= 1 is an ellipsoid; a cell's ray meets it exactly when the
+ * cell's m <= 1 (m is the minimum of |r(z - x)|^2 along the ray), and the
+ * ray's coordinate on a detector axis u (orthonormal to T) is u.z, so every
+ * in-support cell lies within |u.x - p| <= |r^{-T} u| on each axis.  The box
+ * is padded by one cell; Rf's own m <= 1 test still decides every visited
+ * cell, and atoms are added in index order per cell, so the result equals
+ * or_radproj's (cells outside every box receive exact zeros).  Used to build
+ * the large benchmark workloads on the host.
+ */
+static void FN(cell_range)(const REAL *p, int n, double c, double h, int *lo, int *hi)
+{
+    int a = 0, b = n;                        /* first index with p >= c - h */
+    while (a < b) {
+        int m = (a + b) / 2;
+        if ((double)p[m] < c - h) a = m + 1; else b = m;
+    }
+    int l = a - 1;
+    a = 0; b = n;                            /* first index with p > c + h */
+    while (a < b) {
+        int m = (a + b) / 2;
+        if ((double)p[m] <= c + h) a = m + 1; else b = m;
+    }
+    int u = a;
+    *lo = l < 0 ? 0 : l;
+    *hi = u > n - 1 ? n - 1 : u;
+}
+
+/* Cell index box [lo, hi] (per detector axis) of one atom's shadow at angle
+ * a; returns 1 when the box is empty. */
+static int FN(shadow_box)(int gm, int dim, int a, const REAL *w0, const REAL *w1,
+                          const REAL *xj, const REAL *rj, int D0, const REAL *p0,
+                          int D1, const REAL *p1, int *lo, int *hi)
+{
+    double u[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    if (gm == 2) {
+        u[0][0] = w0[2 * a]; u[0][1] = w0[2 * a + 1];
+    } else if (gm == 3) {
+        for (int i = 0; i < 3; i++) { u[0][i] = w0[3 * a + i]; u[1][i] = w1[3 * a + i]; }
+    } else {
+        u[0][0] = w0[2 * a]; u[0][1] = w0[2 * a + 1]; u[1][2] = 1;
+    }
+    REAL M[3][3];
+    FN(rmat)(dim, rj, M);
+    lo[1] = hi[1] = 0;
+    for (int c = 0; c < (dim == 2 ? 1 : 2); c++) {
+        /* v = M^{-T} u_c: forward substitution, M^T lower triangular */
+        double v[3], h2 = 0, ctr = 0;
+        for (int i = 0; i < dim; i++) {
+            double s = u[c][i];
+            for (int k = 0; k < i; k++) s -= (double)M[k][i] * v[k];
+            v[i] = s / (double)M[i][i];
+            h2 += v[i] * v[i];
+            ctr += u[c][i] * (double)xj[i];
+        }
+        double h = sqrt(h2) * (1 + 1e-6) + 1e-9;
+        const REAL *pc = c == 0 ? p0 : p1;
+        const int nc = c == 0 ? D0 : D1;
+        FN(cell_range)(pc, nc, ctr, h, &lo[c], &hi[c]);
+        if (!(h == h) || h > 1e30) { lo[c] = 0; hi[c] = nc - 1; }
+        if (lo[c] > hi[c]) return 1;
+    }
+    return 0;
+}
+
+int FN(or_radproj_boxed)(int gm, int N, const REAL *I, const REAL *x, const REAL *r,
+                         int A, const REAL *T, const REAL *w0, const REAL *w1, int D0,
+                         const REAL *p0, int D1, const REAL *p1, REAL *R, int nthreads)
+{
+    int dim, lenT;
+    if (FN(geom)(gm, &dim, &lenT)) return -1;
+    const int Pr = dim == 2 ? 3 : 6;
+    if (dim == 2) D1 = 1;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int a = 0; a < A; a++) {
+        REAL *Ra = R + (size_t)a * D0 * D1;
+        for (size_t c = 0; c < (size_t)D0 * D1; c++) Ra[c] = 0;
+        REAL y[3] = {0, 0, 0};
+        for (int j = 0; j < N; j++) {
+            const REAL *xj = x + dim * j, *rj = r + Pr * j;
+            int lo[2], hi[2];
+            if (FN(shadow_box)(gm, dim, a, w0, w1, xj, rj, D0, p0, D1, p1, lo, hi)) continue;
+            for (int k0 = lo[0]; k0 <= hi[0]; k0++)
+                for (int k1 = lo[1]; k1 <= hi[1]; k1++) {
+                    FN(tovec)(gm, a, w0, w1, p0[k0], dim == 2 ? 0 : p1[k1], y);
+                    Ra[(size_t)k0 * D1 + k1] += FN(Rf)(dim, lenT, I[j], xj, rj, y,
+                                                       T + lenT * a);
+                }
+        }
+    }
+    return 0;
+}
+
+/*
  * Single-atom derivatives of a data fit, summed over every detector cell:
  *   kind 0 (L2):   f = 1/2 sum (R-C)^2, Df = sum (R-C) dR,
  *                  DDf = sum dR dR^T + (R-C) ddR
@@ -386,6 +481,64 @@ int FN(or_atom_derivs)(int kind, int gm, const REAL *I, const REAL *x,
         for (int i = 0; i < stride; i++) tot[i] += part[(size_t)a * stride + i];
     free(part);
     *f = kind == 0 ? 0.5 * tot[0] : tot[0];
+    for (int i = 0; i < P; i++) Df[i] = tot[1 + i];
+    for (int i = 0; i < P * P; i++) DDf[i] = order > 1 ? tot[1 + P + i] : 0.0;
+    return 0;
+}
+
+/*
+ * or_atom_derivs for kinds 1 (inner product) and 2 (weight fields) visiting
+ * per angle only the atom's shadow box (or_radproj_boxed): every cell
+ * outside it contributes exact zeros to those sums, and the box is walked in
+ * the dense order, so the results are those of or_atom_derivs.  Kind 0 (whose
+ * value also sums C^2 off the support) is not offered.
+ */
+int FN(or_atom_derivs_boxed)(int kind, int gm, const REAL *I, const REAL *x,
+                             const REAL *r, int A, const REAL *T, const REAL *w0,
+                             const REAL *w1, int D0, const REAL *p0, int D1,
+                             const REAL *p1, const REAL *C, const REAL *Bf, int order,
+                             double *f, double *Df, double *DDf, int nthreads)
+{
+    int dim, lenT;
+    if (kind != 1 && kind != 2) return -1;
+    if (FN(geom)(gm, &dim, &lenT)) return -1;
+    const int Pr = dim == 2 ? 3 : 6, P = 1 + dim + Pr;
+    if (dim == 2) D1 = 1;
+    const int stride = 1 + P + P * P;
+    double *part = (double *)calloc((size_t)A * stride, sizeof(double));
+    if (!part) return -2;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+    for (int a = 0; a < A; a++) {
+        double *acc = part + (size_t)a * stride;
+        int lo[2], hi[2];
+        if (FN(shadow_box)(gm, dim, a, w0, w1, x, r, D0, p0, D1, p1, lo, hi)) continue;
+        REAL y[3] = {0, 0, 0}, Rv, dR[10], ddR[100];
+        for (int k0 = lo[0]; k0 <= hi[0]; k0++)
+            for (int k1 = lo[1]; k1 <= hi[1]; k1++) {
+                FN(tovec)(gm, a, w0, w1, p0[k0], dim == 2 ? 0 : p1[k1], y);
+                FN(dRf)(dim, lenT, I[0], x, r, y, T + lenT * a, &Rv, dR, ddR, order);
+                REAL c = C[((size_t)a * D0 + k0) * D1 + k1];
+                acc[0] += (double)Rv * c;
+                for (int i = 0; i < P; i++) acc[1 + i] += (double)c * dR[i];
+                if (order > 1) {
+                    if (kind == 1) {
+                        for (int i = 0; i < P * P; i++) acc[1 + P + i] += (double)c * ddR[i];
+                    } else {
+                        double be = Bf[((size_t)a * D0 + k0) * D1 + k1];
+                        for (int i = 0; i < P; i++)
+                            for (int j = 0; j < P; j++)
+                                acc[1 + P + i * P + j] += be * dR[i] * dR[j] +
+                                                          (double)c * ddR[i * P + j];
+                    }
+                }
+            }
+    }
+    double tot[1 + 10 + 100];
+    for (int i = 0; i < stride; i++) tot[i] = 0;
+    for (int a = 0; a < A; a++)
+        for (int i = 0; i < stride; i++) tot[i] += part[(size_t)a * stride + i];
+    free(part);
+    *f = tot[0];
     for (int i = 0; i < P; i++) Df[i] = tot[1 + i];
     for (int i = 0; i < P * P; i++) DDf[i] = order > 1 ? tot[1 + P + i] : 0.0;
     return 0;

@@ -1,0 +1,162 @@
+"""Parity at the benchmark configurations' own sizes (not toy shapes).
+
+* config 1 in full (512 anisotropic 2D atoms, 180 x 256, KL fit): sinogram,
+  loss, gradient and Hessian of every atom against the FP64 oracle;
+* config 2 (4096 atoms, 121 x 256 x 256 tilt series) and config 4 (8192
+  atoms, 20 000 orientations of 128 x 128) on seeded samples of atoms and
+  angles, Hessians included;
+* the fitting loops at their configured lengths: GD_linesearch_block on
+  config 0 (64 isotropic atoms, 200 sweeps, L2) against the oracle's GD
+  (GD_lib.py:82-178), and Newton_linesearch on config 1 (512 atoms, 30
+  sweeps, KL) against the oracle's Newton loop (NewtonGaussian.py:18-109).
+
+Bars: FP32 path within 1e-5 of the FP64 oracle (arrays normwise; gradients
+and Hessians per parameter entry, scaled by that entry's largest |oracle|
+over the atoms); fits reach the same final loss within 1e-4 relative after
+the same number of steps.  Inputs are float32-rounded for both sides.
+"""
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import fit_oracle
+from oracle import gauss_oracle as go
+from problems import entry_relerr, relerr
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+PKG = "2018_dictionary_tomography_gb300"
+TOL = 1e-5
+
+
+def f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
+def _oracle_geom(T, ortho, det):
+    T = np.asarray(T)
+    if len(det) == 1:
+        return go.Geometry(2, T, ortho[0], det[0])
+    if T.shape[1] == 2:
+        return go.Geometry(25, T, ortho[0], det[0], None, det[1])
+    return go.Geometry(3, T, ortho[0], det[0], ortho[1], det[1])
+
+
+def _parity(W, order, n_atoms=None, n_angles=None, seed=7):
+    """GPU fit fields and derivatives against the oracle on (a sample of) W."""
+    engine = importlib.import_module(PKG + ".engine")
+    geometry = importlib.import_module(PKG + ".geometry")
+    I, x, r = (f32(v) for v in W.init)
+    n, A = len(I), len(W.orientations)
+    rng = np.random.default_rng(seed)
+    sj = np.arange(n) if n_atoms is None else np.sort(rng.choice(n, n_atoms, replace=False))
+    sa = np.arange(A) if n_angles is None else np.sort(rng.choice(A, n_angles, replace=False))
+    T = f32(W.orientations)[sa]
+    ortho = tuple(f32(o)[sa] for o in W.ortho)
+    det = tuple(f32(d) for d in W.detector)
+    data = f32(np.asarray(W.data)[sa])
+    Is, xs, rs = I[sj], x[sj], r.reshape(n, -1)[sj]
+    dev = torch.device("cuda")
+    geom = geometry.DeviceGeometry(T, ortho, det, dev)
+    atoms = engine.DeviceAtoms(Is, xs, rs, dev)
+    fw = engine.fit_forward(atoms, geom, torch.from_numpy(data).float().to(dev), W.fit,
+                            W.background, want_R=True)
+    bc = 1.0 if W.fit == "l2" else 0.0
+    _f, g, H = engine.atom_derivs(atoms, geom, "field", fw["alpha"], fw["beta"], bc, order)
+    og = _oracle_geom(T, ortho, det)
+    Ro = go.radproj_boxed(Is, xs, rs, og)
+    if W.fit == "kl":
+        lo = go.kl_value(data, Ro, W.background)
+        al, be = go.kl_fields(data, Ro, W.background)
+    else:
+        lo = go.l2_value(Ro, data)
+        al, be = Ro - data, np.ones(og.shape)
+    Go, Ho = [], []
+    for j in range(len(Is)):
+        _, gj, hj = go.atom_derivs("field", Is[j], xs[j], rs[j], og, al, order, beta=be,
+                                   boxed=True)
+        Go.append(gj)
+        Ho.append(hj)
+    err = {"sinogram": relerr(fw["R"].cpu().numpy(), Ro),
+           "loss": abs(float(fw["loss"].item()) - lo) / abs(lo),
+           "gradient": entry_relerr(g.cpu().numpy(), np.array(Go))}
+    if order > 1:
+        err["hessian"] = entry_relerr(H.cpu().numpy(), np.array(Ho))
+    return err
+
+
+@pytest.fixture(scope="module")
+def wl(cuda_ready):
+    return importlib.import_module(PKG + ".workloads")
+
+
+def test_config1_full_problem(wl):
+    err = _parity(wl.config1(), 2)
+    print("config1", err)
+    assert all(v < TOL for v in err.values()), err
+
+
+def test_config2_sampled_with_hessian(wl):
+    err = _parity(wl.config2(), 2, n_atoms=48, n_angles=24)
+    print("config2", err)
+    assert all(v < TOL for v in err.values()), err
+
+
+def test_config4_sampled_with_hessian(wl):
+    err = _parity(wl.config4(), 2, n_atoms=48, n_angles=96)
+    print("config4", err)
+    assert all(v < TOL for v in err.values()), err
+
+
+def _fit_spaces(W, iso):
+    sp = importlib.import_module(PKG + ".spaces")
+    af = importlib.import_module(PKG + ".atomFuncs")
+    dim = len(W.detector) + 1
+    S = sp.AtomSpace(dim, isotropic=iso)
+    P = sp.ProjSpace(orientations=f32(W.orientations), ortho=tuple(f32(o) for o in W.ortho),
+                     detector=tuple(f32(d) for d in W.detector))
+    return S, P, af.GaussTomo(S, None, P)
+
+
+def test_gd_block_config0_200_sweeps(wl):
+    """Config 0 as the reference runs it: 64 isotropic atoms, 200 block-GD
+    sweeps over (x, r, I), L2 (the oracle follows the corrected block rule)."""
+    fid = importlib.import_module(PKG + ".fidelity")
+    regm = importlib.import_module(PKG + ".regularisation")
+    solvers = importlib.import_module(PKG + ".solvers")
+    W = wl.config0()
+    I0, x0, r0 = (f32(v) for v in W.init)
+    data = f32(W.data)
+    S, P, Radon = _fit_spaces(W, True)
+    recon = S.element(x0, r0, I0)
+    _, E, _F = solvers.GD_linesearch_block(recon, P.element(data), [200, 1],
+                                          fid.l2_squared_loss(2), regm.null(2), Radon)
+    og = _oracle_geom(P.orientations, P.ortho, P.detector)
+    _, Eo, _Fo = fit_oracle.gd_block(I0, x0, r0, og, data, [200, 1])
+    print("config0 GD: %d steps, loss %.6e -> %.6e (oracle %.6e)" % (E.size, E[0], E[-1], Eo[-1]))
+    assert E.size == Eo.size
+    assert abs(E[-1] - Eo[-1]) <= 1e-4 * abs(Eo[-1])
+    assert Eo[-1] < 0.5 * Eo[0]
+
+
+def test_newton_config1_30_sweeps_kl(wl):
+    """Config 1 as specified: 512 anisotropic atoms, KL on Poisson counts,
+    30 sweeps of per-atom damped Newton steps."""
+    fid = importlib.import_module(PKG + ".fidelity")
+    regm = importlib.import_module(PKG + ".regularisation")
+    solvers = importlib.import_module(PKG + ".solvers")
+    W = wl.config1()
+    I0, x0, r0 = (f32(v) for v in W.init)
+    data = f32(W.data)
+    S, P, Radon = _fit_spaces(W, False)
+    recon = S.element(x0, r0, I0)
+    _, E, _F = solvers.Newton_linesearch(recon, P.element(data), [30, 1],
+                                        fid.KL_loss(2, W.background), regm.null(2), Radon)
+    og = _oracle_geom(P.orientations, P.ortho, P.detector)
+    _, Eo, _Fo = fit_oracle.newton(I0, x0, r0, og, data, [30, 1], "kl", W.background)
+    print("config1 Newton: %d steps, loss %.8e -> %.8e (oracle %d steps, %.8e)"
+          % (E.size, E[0], E[-1], Eo.size, Eo[-1]))
+    assert E.size == Eo.size
+    assert abs(E[-1] - Eo[-1]) <= 1e-4 * abs(Eo[-1])
+    assert Eo[-1] < Eo[0]

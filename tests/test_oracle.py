@@ -107,3 +107,21 @@ def test_oracle_thread_count_invariance():
     b = go.all_atom_derivs("ip", I, x, r, g, C, 2, nthreads=4)
     for u, v in zip(a, b):
         assert np.array_equal(u, v)
+
+
+@pytest.mark.parametrize("kind,dim,args", [("2d", 2, (30, 96)), ("2p5d", 3, (9, 40, 36)),
+                                           ("3d", 3, (9, 40, 44))])
+def test_boxed_evaluation_equals_dense(kind, dim, args):
+    """The shadow-box projection and per-atom derivatives visit only the
+    cells an atom can reach and give the dense results (projection bitwise)."""
+    g = make_geometry(kind, *args)
+    I, x, r = make_atoms(dim, 30, 3)
+    assert np.array_equal(go.radproj(I, x, r, g), go.radproj_boxed(I, x, r, g))
+    C = np.random.default_rng(5).normal(size=g.shape)
+    B = np.random.default_rng(6).uniform(0.5, 2, size=g.shape)
+    for j in range(0, 30, 7):
+        for k, beta in (("ip", None), ("field", B)):
+            a = go.atom_derivs(k, I[j], x[j], r[j], g, C, 2, beta=beta)
+            b = go.atom_derivs(k, I[j], x[j], r[j], g, C, 2, beta=beta, boxed=True)
+            assert abs(a[0] - b[0]) <= 1e-13 * max(abs(a[0]), 1e-300)
+            assert relerr(b[1], a[1]) < 1e-13 and relerr(b[2], a[2]) < 1e-13

@@ -65,10 +65,20 @@ def test_frame_records_dual_rows():
     w0 = rng.normal(size=(5, 3))
     w1 = rng.normal(size=(5, 3))
     rec, kdet = geo.frame_records(T, (w0, w1), 2)
-    assert kdet == 2 and rec.shape == (5, 16)
+    assert kdet == 2 and rec.shape == (5, 24)
     B = np.stack([w0, w1, T], 2).astype(np.float32).astype(np.float64)
     inv = np.linalg.inv(B)
     assert np.allclose(rec[:, 9:12], inv[:, 0, :], rtol=1e-5, atol=1e-5)
+    # hi + lo carries the FP64 dual rows to ~1e-14 (the kernels' centre B^-1 x)
+    for k in range(2):
+        full = rec[:, 9 + 3 * k:12 + 3 * k].astype(np.float64) + rec[:, 15 + 3 * k:18 + 3 * k]
+        assert np.abs(full - inv[:, k, :]).max() <= 1e-13 * np.abs(inv).max()
+    rec2, kdet2 = geo.frame_records(T[:, :2], (w0[:, :2],), 1)
+    B2 = np.stack([w0[:, :2], T[:, :2]], 2).astype(np.float32).astype(np.float64)
+    inv2 = np.linalg.inv(B2)
+    assert kdet2 == 1 and rec2.shape == (5, 8)
+    full2 = rec2[:, 4:6].astype(np.float64) + rec2[:, 6:8]
+    assert np.abs(full2 - inv2[:, 0, :]).max() <= 1e-13 * np.abs(inv2).max()
     with pytest.raises(ValueError):
         geo.uniform_grid([0.0, 1.0, 3.0])
     with pytest.raises(ValueError):
