@@ -46,7 +46,10 @@ EXPORTS = ("gr_version", "gr_preload", "gr_status_string", "gr_workspace_bytes",
            "gr_fit_loop_begin", "gr_fit_loop_end", "gr_fit_loop_gate_begin",
            "gr_fit_loop_gate_end", "gr_fit_loop_instantiate",
            "gr_fit_loop_launch", "gr_fit_loop_destroy", "gr_regulariser",
-           "gr_sino_moments", "gr_accept_fields", "gr_newton_accept_fields")
+           "gr_sino_moments", "gr_accept_fields", "gr_newton_accept_fields",
+           "gr_plan_create", "gr_plan_destroy", "gr_plan_set", "gr_plan_get",
+           "gr_plan_workspace_bytes", "gr_radproj_plan", "gr_fit_forward_plan",
+           "gr_atom_derivs_plan")
 
 _lock = threading.Lock()
 _lib = None
@@ -164,6 +167,22 @@ def load(build_if_missing=True):
                                              ctypes.POINTER(ctypes.c_int)]
         lib.gr_launch_count.restype = ctypes.c_ulonglong
         lib.gr_launch_count.argtypes = []
+        lib.gr_plan_create.restype = ctypes.c_int
+        lib.gr_plan_create.argtypes = [ctypes.c_int, P(GrAtoms), P(GrGeometry), ctypes.POINTER(vp)]
+        lib.gr_plan_destroy.restype = ctypes.c_int
+        lib.gr_plan_destroy.argtypes = [vp]
+        lib.gr_plan_set.restype = ctypes.c_int
+        lib.gr_plan_set.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+        lib.gr_plan_get.restype = ctypes.c_int
+        lib.gr_plan_get.argtypes = [vp, ctypes.c_int]
+        lib.gr_plan_workspace_bytes.restype = ctypes.c_size_t
+        lib.gr_plan_workspace_bytes.argtypes = [vp, ctypes.c_int, P(GrAtoms), P(GrGeometry)]
+        lib.gr_radproj_plan.restype = ctypes.c_int
+        lib.gr_radproj_plan.argtypes = [vp] + lib.gr_radproj.argtypes
+        lib.gr_fit_forward_plan.restype = ctypes.c_int
+        lib.gr_fit_forward_plan.argtypes = [vp] + lib.gr_fit_forward.argtypes
+        lib.gr_atom_derivs_plan.restype = ctypes.c_int
+        lib.gr_atom_derivs_plan.argtypes = [vp] + lib.gr_atom_derivs.argtypes
         _lib = lib
         return lib
 

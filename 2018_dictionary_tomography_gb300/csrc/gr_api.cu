@@ -1,4 +1,6 @@
 // C ABI of the Gaussian-atom Radon engine (declared in include/gauss_radon.h).
+#include <new>
+
 #include "gr_kernels.cuh"
 #include "gauss_radon.h"
 
@@ -64,22 +66,28 @@ const char *gr_status_string(int status) {
   }
 }
 
-size_t gr_workspace_bytes(int op, const gr_atoms *atoms, const gr_geometry *geom) {
+static size_t workspace_bytes_impl(int op, const gr_atoms *atoms, const gr_geometry *geom,
+                                   const Tuning &t) {
   Atoms at;
   Geom g;
   int st;
   if (!to_internal(atoms, geom, at, g, &st)) return 0;
   const int D1 = g.K == 2 ? g.ax[1].n : 1;
   if (op == GR_OP_PROJECT)
-    return project_workspace_bytes(g.K, at.n, g.n_angles, g.ax[0].n, D1);
+    return project_workspace_bytes(g.K, at.n, g.n_angles, g.ax[0].n, D1, t);
   if (op == GR_OP_DERIVS_1 || op == GR_OP_DERIVS_2)
-    return derivs_workspace_bytes(g.K, at.n, g.n_angles, op == GR_OP_DERIVS_1 ? 1 : 2);
+    return derivs_workspace_bytes(g.K, at.n, g.n_angles, op == GR_OP_DERIVS_1 ? 1 : 2, t);
   if (op == GR_OP_ATOM_STEP) return align_up((size_t)g.n_angles * sizeof(double));
   return 0;
 }
 
+size_t gr_workspace_bytes(int op, const gr_atoms *atoms, const gr_geometry *geom) {
+  return workspace_bytes_impl(op, atoms, geom, g_tuning);
+}
+
 static int radproj_impl(const gr_atoms *atoms, const gr_geometry *geom, float *R,
-                        void *workspace, size_t workspace_bytes, void *stream, int psf) {
+                        void *workspace, size_t workspace_bytes, void *stream, int psf,
+                        const Tuning &t = g_tuning) {
   Atoms at;
   Geom g;
   int st;
@@ -90,7 +98,7 @@ static int radproj_impl(const gr_atoms *atoms, const gr_geometry *geom, float *R
   o.epilogue = kEpiNone;
   o.psf = psf;
   return launch_project(at, g, o, nullptr, workspace, workspace_bytes,
-                        static_cast<cudaStream_t>(stream));
+                        static_cast<cudaStream_t>(stream), t);
 }
 
 int gr_radproj(const gr_atoms *atoms, const gr_geometry *geom, float *R,
@@ -106,7 +114,8 @@ int gr_psf_radproj(const gr_atoms *atoms, const gr_geometry *geom, float *R,
 static int fit_forward_impl(const gr_atoms *atoms, const gr_geometry *geom, int fit,
                             const float *data, float background, float *R, float *alpha,
                             float *beta, double *loss, void *workspace,
-                            size_t workspace_bytes, void *stream, int psf) {
+                            size_t workspace_bytes, void *stream, int psf,
+                            const Tuning &t = g_tuning) {
   Atoms at;
   Geom g;
   int st;
@@ -124,7 +133,7 @@ static int fit_forward_impl(const gr_atoms *atoms, const gr_geometry *geom, int 
   o.beta = beta;
   o.psf = psf;
   return launch_project(at, g, o, loss, workspace, workspace_bytes,
-                        static_cast<cudaStream_t>(stream));
+                        static_cast<cudaStream_t>(stream), t);
 }
 
 int gr_fit_forward(const gr_atoms *atoms, const gr_geometry *geom, int fit,
@@ -146,7 +155,8 @@ int gr_psf_fit_forward(const gr_atoms *atoms, const gr_geometry *geom, int fit,
 static int atom_derivs_impl(const gr_atoms *atoms, const gr_geometry *geom, int mode,
                             const float *field, const float *beta_field, float beta_const,
                             int order, double *f, double *g_out, double *H, void *workspace,
-                            size_t workspace_bytes, void *stream, int psf) {
+                            size_t workspace_bytes, void *stream, int psf,
+                            const Tuning &t = g_tuning) {
   Atoms at;
   Geom g;
   int st;
@@ -164,7 +174,7 @@ static int atom_derivs_impl(const gr_atoms *atoms, const gr_geometry *geom, int 
   in.psf = psf;
   DerivOut out{f, g_out, H};
   return launch_derivs(at, g, in, out, workspace, workspace_bytes,
-                       static_cast<cudaStream_t>(stream));
+                       static_cast<cudaStream_t>(stream), t);
 }
 
 int gr_atom_derivs(const gr_atoms *atoms, const gr_geometry *geom, int mode,
@@ -333,8 +343,76 @@ int gr_kernel_timer_read(int which, double *total_ms, int *launches) {
   return gr::timer_read(which, total_ms, launches);
 }
 
-int gr_set_tuning(int key, int value) { return set_tuning(key, value); }
+int gr_set_tuning(int key, int value) { return tuning_set(g_tuning, key, value); }
 
-int gr_get_tuning(int key) { return get_tuning(key); }
+int gr_get_tuning(int key) { return tuning_get(g_tuning, key); }
+
+// ---- plans: a schedule (Tuning) owned by the caller ------------------------
+struct gr_plan {
+  gr::Tuning t;
+  int op;
+  int kdet, n_atoms, n_angles, n_det[2];
+};
+
+int gr_plan_create(int op, const gr_atoms *atoms, const gr_geometry *geom, gr_plan **plan) {
+  if (!plan) return GR_ERR_ARG;
+  *plan = nullptr;
+  if (op != GR_OP_PROJECT && op != GR_OP_DERIVS_1 && op != GR_OP_DERIVS_2) return GR_ERR_ARG;
+  Atoms at;
+  Geom g;
+  int st;
+  if (!to_internal(atoms, geom, at, g, &st)) return st;
+  gr_plan *p = new (std::nothrow) gr_plan;
+  if (!p) return GR_ERR_ARG;
+  p->t = g_tuning;
+  p->op = op;
+  p->kdet = g.K;
+  p->n_atoms = at.n;
+  p->n_angles = g.n_angles;
+  p->n_det[0] = g.ax[0].n;
+  p->n_det[1] = g.K == 2 ? g.ax[1].n : 1;
+  *plan = p;
+  return GR_OK;
+}
+
+int gr_plan_destroy(gr_plan *plan) {
+  delete plan;
+  return GR_OK;
+}
+
+int gr_plan_set(gr_plan *plan, int key, int value) {
+  return plan ? tuning_set(plan->t, key, value) : GR_ERR_ARG;
+}
+
+int gr_plan_get(const gr_plan *plan, int key) { return plan ? tuning_get(plan->t, key) : -1; }
+
+size_t gr_plan_workspace_bytes(const gr_plan *plan, int op, const gr_atoms *atoms,
+                               const gr_geometry *geom) {
+  return plan ? workspace_bytes_impl(op, atoms, geom, plan->t) : 0;
+}
+
+int gr_radproj_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                    float *R, void *workspace, size_t workspace_bytes, void *stream) {
+  if (!plan) return GR_ERR_ARG;
+  return radproj_impl(atoms, geom, R, workspace, workspace_bytes, stream, 0, plan->t);
+}
+
+int gr_fit_forward_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                        int fit, const float *data, float background, float *R, float *alpha,
+                        float *beta, double *loss, void *workspace, size_t workspace_bytes,
+                        void *stream) {
+  if (!plan) return GR_ERR_ARG;
+  return fit_forward_impl(atoms, geom, fit, data, background, R, alpha, beta, loss, workspace,
+                          workspace_bytes, stream, 0, plan->t);
+}
+
+int gr_atom_derivs_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                        int mode, const float *field, const float *beta_field,
+                        float beta_const, int order, double *f, double *g, double *H,
+                        void *workspace, size_t workspace_bytes, void *stream) {
+  if (!plan) return GR_ERR_ARG;
+  return atom_derivs_impl(atoms, geom, mode, field, beta_field, beta_const, order, f, g, H,
+                          workspace, workspace_bytes, stream, 0, plan->t);
+}
 
 }  // extern "C"

@@ -45,55 +45,60 @@ inline int next_pow2(int v) {
 }
 
 constexpr int kRowChunk = 8;
+// cells per chunk of a 3D box row, and resident blocks per SM asked of the
+// gradient (order 1) kernels; compile-time, for sweeps
+#ifndef GR_ROW_CHUNK_3D
+#define GR_ROW_CHUNK_3D 8
+#endif
+#ifndef GR_GRAD_MIN_BLOCKS
+#define GR_GRAD_MIN_BLOCKS 5
+#endif
+constexpr int kRowChunk3 = GR_ROW_CHUNK_3D;
 
-// Work split of the derivative kernels (tunable through gr_set_tuning):
-// about g_deriv_target_warps warps in total, each angle chunk holding at
-// least g_deriv_min_angles angles per lane group.
-int g_deriv_target_warps = 131072;
-int g_deriv_min_angles = 1;
-// Atoms per warp (power of two up to 32; 0 = automatic): with fewer atoms per
-// warp the lanes of a warp take different angles of one atom, whose support
-// boxes are of similar size, so fewer lanes idle.  Automatic: one atom per
-// warp for Hessians and for long angle series, else four (so each lane still
-// has a few angles to amortise the warp's closing reduction).
-int g_deriv_atoms_per_warp = 0;
-// Problems with few (atom, angle) pairs split each pair's cells over rs
-// lanes (rows of a 3D box, chunks of kRowChunk cells of a 2D one), rs the
-// largest power of two up to 8 with pairs * rs <= g_deriv_split_lanes; the
-// lanes' moment sums are combined before one of them does the chain-rule
-// assembly.  A pair's cell walk is otherwise one lane's serial loop, which
-// sets the kernel time when there are too few pairs to fill the GPU and
-// their boxes are large.  0: never split.
-int g_deriv_split_lanes = 65536;
-// Take as many angle chunks as give every lane at most one angle (the ONE
-// kernel variant: fewer registers, no spills) whenever the chunk partials
-// then fit in this many MB; 0: keep the target-warps split.  On 8192 atoms x
-// 20000 orientations the one-angle split (625 chunks, 225 MB of partials)
-// runs the gradient kernel in 23.6 ms against 25.7 ms for 16 chunks.
-int g_deriv_one_mb = 1024;
-
-inline DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order, bool split = true) {
+// Work split of the derivative kernels (Tuning, gr_set_tuning / gr_plan_set):
+// about deriv_target_warps warps in total, each angle chunk holding at least
+// deriv_min_angles angles per lane group.
+// deriv_atoms_per_warp (power of two up to 32; 0 = automatic): with fewer
+// atoms per warp the lanes of a warp take different angles of one atom, whose
+// support boxes are of similar size, so fewer lanes idle.  Automatic: one
+// atom per warp for Hessians and for long angle series, else four (so each
+// lane still has a few angles to amortise the warp's closing reduction).
+// deriv_split_lanes: problems with few (atom, angle) pairs split each pair's
+// cells over rs lanes (rows of a 3D box, chunks of kRowChunk cells of a 2D
+// one), rs the largest power of two up to 8 with pairs * rs <=
+// deriv_split_lanes; the lanes' moment sums are combined before one of them
+// does the chain-rule assembly.  A pair's cell walk is otherwise one lane's
+// serial loop, which sets the kernel time when there are too few pairs to
+// fill the GPU and their boxes are large.  0: never split.
+// deriv_one_mb: take as many angle chunks as give every lane at most one
+// angle (the ONE kernel variant: fewer registers, no spills) whenever the
+// chunk partials then fit in this many MB; 0: keep the target-warps split.
+// On 8192 atoms x 20000 orientations the one-angle split (625 chunks, 225 MB
+// of partials) runs the gradient kernel in 23.6 ms against 25.7 ms for 16
+// chunks.
+inline DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order, const Tuning &t,
+                          bool split = true) {
   DerivCfg c;
   c.ag = next_pow2(n_atoms < 1 ? 1 : n_atoms);
-  const int ag_cap = g_deriv_atoms_per_warp > 0 ? g_deriv_atoms_per_warp
+  const int ag_cap = t.deriv_atoms_per_warp > 0 ? t.deriv_atoms_per_warp
                      : (order > 1 || n_angles >= 1024) ? 1 : 4;
   if (c.ag > ag_cap) c.ag = ag_cap;
   c.sg = 32 / c.ag;
   const long long pairs = (long long)(n_atoms < 1 ? 1 : n_atoms) * (n_angles < 1 ? 1 : n_angles);
   c.rs = 1;
-  while (split && g_deriv_split_lanes > 0 && c.rs < 8 && c.rs < c.sg &&
-         pairs * c.rs * 2 <= (long long)g_deriv_split_lanes)
+  while (split && t.deriv_split_lanes > 0 && c.rs < 8 && c.rs < c.sg &&
+         pairs * c.rs * 2 <= (long long)t.deriv_split_lanes)
     c.rs <<= 1;
   const int warps_atoms = (n_atoms + c.ag - 1) / c.ag;
-  int nch = (g_deriv_target_warps + warps_atoms - 1) / warps_atoms;
-  const int per = (c.sg / c.rs) * (g_deriv_min_angles < 1 ? 1 : g_deriv_min_angles);
+  int nch = (t.deriv_target_warps + warps_atoms - 1) / warps_atoms;
+  const int per = (c.sg / c.rs) * (t.deriv_min_angles < 1 ? 1 : t.deriv_min_angles);
   const int max_ch = (n_angles + per - 1) / per;
   if (nch > max_ch) nch = max_ch;
   const int P0 = 1 + (K + 1) + (K == 1 ? 3 : 6);
   const size_t qn0 = 1 + P0 + (order > 1 ? P0 * (P0 + 1) / 2 : 0);
-  if (g_deriv_one_mb > 0 && g_deriv_min_angles == 1 && nch < max_ch &&
+  if (t.deriv_one_mb > 0 && t.deriv_min_angles == 1 && nch < max_ch &&
       (size_t)max_ch * qn0 * (size_t)(n_atoms < 1 ? 1 : n_atoms) * sizeof(float) <=
-          ((size_t)g_deriv_one_mb << 20))
+          ((size_t)t.deriv_one_mb << 20))
     nch = max_ch;
   if (nch < 1) nch = 1;
   c.ch = (n_angles + nch - 1) / nch;
@@ -205,20 +210,20 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
         const float rlo = ceilf(rc - rh), rhi = floorf(rc + rh);
         const int c_lo = (int)fminf(fmaxf(rlo, (float)p.lo[1]), (float)p.hi[1] + 1.f);
         const int c_hi = (int)fmaxf(fminf(rhi, (float)p.hi[1]), (float)p.lo[1] - 1.f);
-        // the row is walked in chunks of kRowChunk cells whose field values
+        // the row is walked in chunks of kRowChunk3 cells whose field values
         // and coordinates are loaded together first, so the loads overlap
         // instead of each cell waiting for its own
-        for (int kb = c_lo; kb <= c_hi; kb += kRowChunk) {
-          float cv[kRowChunk], pv[kRowChunk], bv[GN ? kRowChunk : 1];
+        for (int kb = c_lo; kb <= c_hi; kb += kRowChunk3) {
+          float cv[kRowChunk3], pv[kRowChunk3], bv[GN ? kRowChunk3 : 1];
 #pragma unroll
-          for (int i = 0; i < kRowChunk; ++i) {
+          for (int i = 0; i < kRowChunk3; ++i) {
             const int k1 = min(kb + i, c_hi);
             cv[i] = __ldg(field + rbase + k1);
             pv[i] = __ldg(g.ax[1].coords + k1);
             if (GN) bv[i] = bfield ? __ldg(bfield + rbase + k1) : in.beta_const;
           }
 #pragma unroll
-          for (int i = 0; i < kRowChunk; ++i) {
+          for (int i = 0; i < kRowChunk3; ++i) {
             if (kb + i > c_hi) break;
             const float d1 = (pv[i] - p.qh[1]) - p.ql[1];
             const float m = fmaf(d1, fmaf(p.G[2], d1, u), t0);
@@ -269,7 +274,7 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
 // the Hessian kernel from 255 to 168 registers (3 resident blocks per SM
 // instead of 2).
 template <int K, int ORDER, bool ONE>
-__global__ void __launch_bounds__(128, ORDER == 1 ? 5 : (ONE ? 3 : 1))
+__global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS : (ONE ? 3 : 1))
     gr_deriv_kernel(Atoms at, Geom g, DerivIn in, DerivCfg cfg, float *part) {
   constexpr int D = K + 1;
   constexpr int PR = n_rparam<K>();
@@ -695,47 +700,49 @@ int launch_sum_squares(const float *C, size_t n, double *out, void *ws,
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
-int set_tuning(int key, int value) {
+Tuning g_tuning;
+
+int tuning_set(Tuning &t, int key, int value) {
   if (key == 0 && value >= 32 && value <= (1 << 26)) {
-    g_deriv_target_warps = value;
+    t.deriv_target_warps = value;
     return kOk;
   }
   if (key == 1 && value >= 1 && value <= 65536) {
-    g_deriv_min_angles = value;
+    t.deriv_min_angles = value;
     return kOk;
   }
   if (key == 2 && (value == 0 || (value >= 1 && value <= 32 && (value & (value - 1)) == 0))) {
-    g_deriv_atoms_per_warp = value;
+    t.deriv_atoms_per_warp = value;
     return kOk;
   }
   if (key == 3 && value >= 1 && value <= 2) {
-    g_proj_form = value;
+    t.proj_form = value;
     return kOk;
   }
   if (key == 4 && value >= 0) {
-    g_proj_split_cells = value;
+    t.proj_split_cells = value;
     return kOk;
   }
   if (key == 6 && value >= 0) {
-    g_deriv_split_lanes = value;
+    t.deriv_split_lanes = value;
     return kOk;
   }
   if (key == 7 && value >= 0) {
-    g_deriv_one_mb = value;
+    t.deriv_one_mb = value;
     return kOk;
   }
   return kErrArg;
 }
 
-int get_tuning(int key) {
-  return key == 0 ? g_deriv_target_warps : key == 1 ? g_deriv_min_angles
-         : key == 2 ? g_deriv_atoms_per_warp : key == 3 ? g_proj_form
-         : key == 4 ? g_proj_split_cells
-         : key == 6 ? g_deriv_split_lanes : key == 7 ? g_deriv_one_mb : -1;
+int tuning_get(const Tuning &t, int key) {
+  return key == 0 ? t.deriv_target_warps : key == 1 ? t.deriv_min_angles
+         : key == 2 ? t.deriv_atoms_per_warp : key == 3 ? t.proj_form
+         : key == 4 ? t.proj_split_cells
+         : key == 6 ? t.deriv_split_lanes : key == 7 ? t.deriv_one_mb : -1;
 }
 
-size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order) {
-  DerivCfg c = deriv_cfg(K, n_atoms, n_angles, order);
+size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order, const Tuning &t) {
+  DerivCfg c = deriv_cfg(K, n_atoms, n_angles, order, t);
   size_t b = align_up((size_t)c.nchunks * c.qn * (size_t)n_atoms * sizeof(float));
   b += align_up(kSumSqBlocks * sizeof(double)) + align_up(sizeof(double));
   return b;
@@ -743,14 +750,14 @@ size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order) {
 
 int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
                   const DerivOut &out, void *ws, size_t ws_bytes,
-                  cudaStream_t stream) {
+                  cudaStream_t stream, const Tuning &t) {
   const int K = g.K;
   if (at.n <= 0) return kOk;
   if (in.order < 1 || in.order > 2) return kErrArg;
   // the pixel-integrated kernel walks whole pairs per lane (no cell split);
   // its chunking never needs more workspace than the split one
-  DerivCfg c = deriv_cfg(K, at.n, g.n_angles, in.order, !in.psf);
-  if (ws == nullptr || ws_bytes < derivs_workspace_bytes(K, at.n, g.n_angles, in.order))
+  DerivCfg c = deriv_cfg(K, at.n, g.n_angles, in.order, t, !in.psf);
+  if (ws == nullptr || ws_bytes < derivs_workspace_bytes(K, at.n, g.n_angles, in.order, t))
     return kErrWorkspace;
   char *wp = static_cast<char *>(ws);
   float *part = reinterpret_cast<float *>(wp);

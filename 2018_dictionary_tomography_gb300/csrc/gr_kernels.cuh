@@ -64,18 +64,35 @@ struct DerivOut {
 
 inline size_t align_up(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// Work-split and tiling schedule of the projection and derivative launches
+// (keys of gr_set_tuning / gr_plan_set).  g_tuning is the process-wide
+// default; a gr_plan carries its own copy, so launches on different streams
+// can run different schedules at once.
+struct Tuning {
+  int deriv_target_warps = 131072;  // key 0
+  int deriv_min_angles = 1;         // key 1
+  int deriv_atoms_per_warp = 0;     // key 2 (0: automatic)
+  int proj_form = 1;                // key 3 (1: 16 x 32 tiles, 2: 32 x 32)
+  int proj_split_cells = 4 << 20;   // key 4
+  int deriv_split_lanes = 65536;    // key 6
+  int deriv_one_mb = 1024;          // key 7
+};
+extern Tuning g_tuning;
+int tuning_set(Tuning &t, int key, int value);
+int tuning_get(const Tuning &t, int key);
+
 TileCfg make_tiles(int K, int D0, int D1, int rows);
-extern int g_proj_form;
-extern int g_proj_split_cells;
-size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1);
+size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1,
+                               const Tuning &t = g_tuning);
 int launch_project(const Atoms &at, const Geom &g, const ProjOut &o,
                    double *loss_out, void *ws, size_t ws_bytes,
-                   cudaStream_t stream);
+                   cudaStream_t stream, const Tuning &t = g_tuning);
 
-size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order);
+size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order,
+                              const Tuning &t = g_tuning);
 int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
                   const DerivOut &out, void *ws, size_t ws_bytes,
-                  cudaStream_t stream);
+                  cudaStream_t stream, const Tuning &t = g_tuning);
 
 int launch_sum_squares(const float *C, size_t n, double *out, void *ws,
                        size_t ws_bytes, cudaStream_t stream);
@@ -117,8 +134,6 @@ int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
 int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y,
                    float *u, int psf, float s, cudaStream_t stream);
 
-int set_tuning(int key, int value);
-int get_tuning(int key);
 
 // host-side count of kernels launched by this library
 void note_launches(int n);

@@ -21,6 +21,13 @@
 // names a host-side stand-in).  The first call on each device therefore looks
 // the address up with cudaGetSymbolAddress, with that device current, and
 // caches it; make that first call before any stream capture on the device.
+// The address belongs to the module loaded in one CUDA context: the cache is
+// keyed by the context's process-unique id (cuCtxGetId), so a call made
+// under another context of the device (a context the caller created, or the
+// primary context re-created after cudaDeviceReset) looks the address up
+// again instead of reusing one that is no longer valid.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "gauss_radon.h"
@@ -34,23 +41,72 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_noalloc_mutex;
-void *g_noalloc_ptr[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (looked up once
-// per device).  Returns nullptr on failure.
+// Driver entry points, found through the runtime (the library links only
+// the CUDA runtime, so that it loads on machines without a driver).
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+bool driver_entry_points() {
+  if (g_ctx_get_current && g_ctx_get_id) return true;
+  void *a = nullptr, *b = nullptr;
+  cudaDriverEntryPointQueryResult qa, qb;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) !=
+          cudaSuccess ||
+      cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) !=
+          cudaSuccess ||
+      qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b) {
+    cudaGetLastError();
+    return false;
+  }
+  g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(a);
+  g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(b);
+  return true;
+}
+
+struct ScratchAddr {
+  unsigned long long ctx_id;  // 0: not looked up yet
+  void *ptr;
+};
+ScratchAddr g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch in the current context of the current
+// device (looked up once per device and context).  Returns nullptr on failure.
 void *noalloc_scratch_for_current_device() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (g_noalloc_ptr[dev] == nullptr) {
-    void *ptr = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!driver_entry_points()) return nullptr;
+  }
+  void *ptr = nullptr;
+  CUcontext ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return nullptr;
+  if (ctx == nullptr) {
+    // no context current on this thread yet: the runtime makes the device's
+    // primary context current on its first call, this lookup
     if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || ptr == nullptr) {
       cudaGetLastError();  // reset the runtime's last-error slot left by the failure
       return nullptr;
     }
-    g_noalloc_ptr[dev] = ptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return nullptr;
   }
-  return g_noalloc_ptr[dev];
+  unsigned long long id = 0;
+  if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS || id == 0) return nullptr;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  ScratchAddr &c = g_noalloc_addr[dev];
+  if (c.ctx_id != id || c.ptr == nullptr) {
+    if (ptr == nullptr &&
+        (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || ptr == nullptr)) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    c.ctx_id = id;
+    c.ptr = ptr;
+  }
+  return c.ptr;
 }
 
 }  // namespace

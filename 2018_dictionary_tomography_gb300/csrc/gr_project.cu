@@ -740,11 +740,9 @@ __global__ void __launch_bounds__(kLossThreads)
   if (threadIdx.x == 0) out[0] = sh[0];
 }
 
-// Tiling of the point-sampled 3D projection (gr_set_tuning key 3):
+// Tiling of the point-sampled 3D projection (Tuning::proj_form, key 3):
 // 1: 16-row tiles (more resident warps), 2: 32-row tiles (fewer atoms cut
 // by tile edges).
-int g_proj_form = 1;
-
 static int proj_rows(int form) { return form == 2 ? kTileDim0 : 16; }
 
 // Loss partials of up to this many items are summed by the projection's
@@ -752,9 +750,9 @@ static int proj_rows(int form) { return form == 2 ? kTileDim0 : 16; }
 // above it the 1024-thread gr_loss_finalize_kernel does it.
 constexpr size_t kFusedLossItems = 8192;
 
-// 3D problems of fewer detector cells (all angles) than this split every
-// tile's atoms over a block's warps (gr_set_tuning key 4; 0: never).
-int g_proj_split_cells = 4 << 20;
+// 3D problems of fewer detector cells (all angles) than
+// Tuning::proj_split_cells (key 4; 0: never) split every tile's atoms over a
+// block's warps.
 
 template <int ROWS, int S, int NW>
 static void launch_project3d(size_t items, const Atoms &at, const Geom &g, const TileCfg &tc,
@@ -800,9 +798,10 @@ TileCfg make_tiles(int K, int D0, int D1, int rows) {
   return tc;
 }
 
-size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1) {
+size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1,
+                               const Tuning &t) {
   // sized for the smaller of the point-sampled and pixel-integrated tilings
-  const int rows = proj_rows(g_proj_form) < kTileDim0 ? proj_rows(g_proj_form) : kTileDim0;
+  const int rows = proj_rows(t.proj_form) < kTileDim0 ? proj_rows(t.proj_form) : kTileDim0;
   TileCfg tc = make_tiles(K, D0, D1, rows);
   const size_t W = (size_t)(n_atoms + 31) / 32;
   const size_t items = (size_t)n_angles * tc.ntiles;
@@ -817,14 +816,14 @@ size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1)
 
 int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
                    double *loss_out, void *ws, size_t ws_bytes,
-                   cudaStream_t stream) {
+                   cudaStream_t stream, const Tuning &t) {
   const int K = g.K;
   const int D0 = g.ax[0].n, D1 = K == 1 ? 1 : g.ax[1].n;
-  const int form = g_proj_form;
+  const int form = t.proj_form;
   TileCfg tc = make_tiles(K, D0, D1, (K == 2 && !o_in.psf) ? proj_rows(form) : kTileDim0);
   const int W = (at.n + 31) / 32;
   const size_t items = (size_t)g.n_angles * tc.ntiles;
-  const size_t need = project_workspace_bytes(K, at.n, g.n_angles, D0, D1);
+  const size_t need = project_workspace_bytes(K, at.n, g.n_angles, D0, D1, t);
   if (ws_bytes < need || (ws == nullptr && need > 0)) return kErrWorkspace;
   char *wp = static_cast<char *>(ws);
   int *next_item = reinterpret_cast<int *>(wp);
@@ -878,8 +877,8 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   } else {
     // the split is chosen from the problem's size alone (not from the
     // tiling), so both tilings keep giving the same cell sums
-    const bool split = g_proj_split_cells > 0 && W >= kProjWarps &&
-                       (size_t)g.n_angles * D0 * D1 < (size_t)g_proj_split_cells;
+    const bool split = t.proj_split_cells > 0 && W >= kProjWarps &&
+                       (size_t)g.n_angles * D0 * D1 < (size_t)t.proj_split_cells;
     fused_loss = loss_out != nullptr && items <= kFusedLossItems;
     double *lo = fused_loss ? loss_out : nullptr;
     if (form == 2) {

@@ -31,19 +31,26 @@ struct UpdateArgs {
   double *part;       // per-angle loss-change partials
 };
 
-__device__ __forceinline__ float kl_cell(float f, float g) {
-  if (!(f > 0.f)) return g;
-  const float e = (f - g) / g;
-  float h;
-  if (fabsf(e) < 0.125f) {
-    const float e2 = e * e;
-    h = e2 * (0.5f + e * (-1.f / 6.f + e * (1.f / 12.f + e * (-1.f / 20.f +
-             e * (1.f / 30.f + e * (-1.f / 42.f + e * (1.f / 56.f)))))));
+// Change of the cell's KL term f log(f/g) - f + g when g = g0 (model +
+// background) moves by d: d - f log1p(d/g0), written as
+//   d (g0 - f)/g0 + f (t - log1p t),  t = d / g0,
+// so that neither the new model value g0 + d (which would round d to the
+// spacing of g0) nor a difference of two nearly equal terms is formed.
+__device__ __forceinline__ double kl_cell_change(float f, float g0, float d) {
+  if (!(f > 0.f)) return (double)d;
+  const float t = d / g0;
+  double phi;
+  if (fabsf(t) < 0.0625f) {
+    // t - log1p(t) = t^2/2 - t^3/3 + t^4/4 - ...  (|t| < 1/16: 8 terms)
+    const double td = (double)t;
+    double s2 = 1.0 / 9.0;
+#pragma unroll
+    for (int k = 8; k >= 2; --k) s2 = fma(s2, -td, 1.0 / (double)k);
+    phi = td * td * s2;
   } else {
-    const float u = f / g;
-    h = u * logf(u) - u + 1.f;
+    phi = (double)t - log1p((double)t);
   }
-  return g * h;
+  return (double)d * (double)((g0 - f) / g0) + (double)f * phi;
 }
 
 template <int K>
@@ -110,7 +117,7 @@ __global__ void __launch_bounds__(128)
           u.alpha[gi] = 1.f - fo * ig;
           if (u.beta) u.beta[gi] = fo * ig * ig;
         } else {
-          acc += (double)kl_cell(fo, Rv + d + u.bg) - (double)kl_cell(fo, Rv + u.bg);
+          acc += kl_cell_change(fo, Rv + u.bg, d);
         }
       }
     }

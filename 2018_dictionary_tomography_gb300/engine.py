@@ -132,13 +132,72 @@ def _check_dims(atoms, geom):
             raise ValueError("anisotropic r must have %d entries per atom" % want)
 
 
-def _ws_for(op, atoms, geom):
-    lib = _lib.load()
-    n = lib.gr_workspace_bytes(op, ctypes.byref(atoms.struct), ctypes.byref(geom.struct))
+class Plan:
+    """A launch schedule (work split and tiling) owned by the caller: the
+    C ABI's gr_plan.  Engine calls given ``plan=`` run under it instead of
+    the process-wide values of gr_set_tuning, so fits on concurrent streams
+    can each use the schedule tuned for their shape class.  Created from the
+    current process-wide values; ``set``/``get`` take the GR_TUNE_* keys."""
+
+    def __init__(self, op, atoms, geom):
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(lib.gr_plan_create(int(op), ctypes.byref(atoms.struct),
+                                      ctypes.byref(geom.struct), ctypes.byref(h)),
+                   "gr_plan_create")
+        self._h = h
+        self.op = int(op)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set(self, key, value):
+        _lib.check(_lib.load().gr_plan_set(self._h, int(key), int(value)), "gr_plan_set")
+        return self
+
+    def get(self, key):
+        return int(_lib.load().gr_plan_get(self._h, int(key)))
+
+    def workspace_bytes(self, op, atoms, geom):
+        return int(_lib.load().gr_plan_workspace_bytes(self._h, int(op),
+                                                       ctypes.byref(atoms.struct),
+                                                       ctypes.byref(geom.struct)))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().gr_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ws_for(op, atoms, geom, plan=None):
+    if plan is not None:
+        n = plan.workspace_bytes(op, atoms, geom)
+    else:
+        n = _lib.load().gr_workspace_bytes(op, ctypes.byref(atoms.struct),
+                                           ctypes.byref(geom.struct))
     return workspace(n, geom.device), n
 
 
-def radproj(atoms, geom, out=None, psf=False):
+def _fn(name, psf, plan):
+    """The entry point for a call: psf variant, or the plan-taking variant
+    (bound to the plan's handle)."""
+    lib = _lib.load()
+    if plan is None:
+        return getattr(lib, ("gr_psf_" + name) if psf else ("gr_" + name))
+    if psf:
+        raise ValueError("plans cover the point-sampled operator")
+    f = getattr(lib, "gr_%s_plan" % name)
+    return lambda *a: f(plan.handle, *a)
+
+
+def radproj(atoms, geom, out=None, psf=False, plan=None):
     """Forward projection R (A, D0[, D1]) float32 on the device; psf=True
     gives the pixel-integrated (single-particle) projection."""
     _check_dims(atoms, geom)
@@ -146,8 +205,8 @@ def radproj(atoms, geom, out=None, psf=False):
         out = torch.empty(geom.shape, dtype=torch.float32, device=geom.device)
     if tuple(out.shape) != tuple(geom.shape) or out.dtype != torch.float32 or not out.is_contiguous():
         raise ValueError("output must be a contiguous float32 tensor of shape %s" % (geom.shape,))
-    ws, n = _ws_for(_lib.GR_OP_PROJECT, atoms, geom)
-    fn = _lib.load().gr_psf_radproj if psf else _lib.load().gr_radproj
+    ws, n = _ws_for(_lib.GR_OP_PROJECT, atoms, geom, plan)
+    fn = _fn("radproj", psf, plan)
     st = fn(ctypes.byref(atoms.struct), ctypes.byref(geom.struct),
             out.data_ptr(), ws.data_ptr(), n, _stream_handle(geom.device))
     _lib.check(st, "gr_radproj")
@@ -155,7 +214,7 @@ def radproj(atoms, geom, out=None, psf=False):
 
 
 def fit_forward(atoms, geom, data, fit="l2", background=0.0, want_R=False,
-                want_fields=True, psf=False):
+                want_fields=True, psf=False, plan=None):
     """Projection fused with an L2 or KL fit.
 
     Returns dict with 'loss' (0-d float64 device tensor), 'alpha', 'beta'
@@ -172,9 +231,9 @@ def fit_forward(atoms, geom, data, fit="l2", background=0.0, want_R=False,
     alpha = torch.empty(geom.shape, dtype=torch.float32, device=dev) if want_fields else None
     beta = (torch.empty(geom.shape, dtype=torch.float32, device=dev)
             if (want_fields and fit == "kl") else None)
-    ws, n = _ws_for(_lib.GR_OP_PROJECT, atoms, geom)
+    ws, n = _ws_for(_lib.GR_OP_PROJECT, atoms, geom, plan)
     p = lambda t: None if t is None else t.data_ptr()
-    fn = _lib.load().gr_psf_fit_forward if psf else _lib.load().gr_fit_forward
+    fn = _fn("fit_forward", psf, plan)
     st = fn(
         ctypes.byref(atoms.struct), ctypes.byref(geom.struct), code, data.data_ptr(),
         float(background), p(R), p(alpha), p(beta), out["loss"].data_ptr(),
@@ -189,7 +248,7 @@ MODES = {"field": _lib.GR_MODE_FIELD, "l2_atom": _lib.GR_MODE_L2_ATOM,
 
 
 def atom_derivs(atoms, geom, mode, field, beta_field=None, beta_const=1.0, order=2,
-                psf=False):
+                psf=False, plan=None):
     """Per-atom value (N,), gradient (N, P) and Hessian (N, P, P), float64.
 
     mode 'inner' (field = C): derivatives of <R_j, C>;
@@ -212,8 +271,8 @@ def atom_derivs(atoms, geom, mode, field, beta_field=None, beta_const=1.0, order
     if N == 0:
         return f, g, H
     op = _lib.GR_OP_DERIVS_1 if order == 1 else _lib.GR_OP_DERIVS_2
-    ws, n = _ws_for(op, atoms, geom)
-    fn = _lib.load().gr_psf_atom_derivs if psf else _lib.load().gr_atom_derivs
+    ws, n = _ws_for(op, atoms, geom, plan)
+    fn = _fn("atom_derivs", psf, plan)
     st = fn(
         ctypes.byref(atoms.struct), ctypes.byref(geom.struct), MODES[mode],
         field.data_ptr(), None if beta_field is None else beta_field.data_ptr(),
@@ -331,7 +390,9 @@ def preload(device=None):
         _lib.check(_lib.load().gr_preload(), "gr_preload")
 
 
-def workspace_bytes(op, atoms, geom):
+def workspace_bytes(op, atoms, geom, plan=None):
+    if plan is not None:
+        return plan.workspace_bytes(op, atoms, geom)
     return int(_lib.load().gr_workspace_bytes(op, ctypes.byref(atoms.struct),
                                               ctypes.byref(geom.struct)))
 
@@ -340,9 +401,10 @@ def _ptr(t):
     return None if t is None else t.data_ptr()
 
 
-def fit_forward_into(atoms, geom, data, fit, background, R, alpha, beta, loss, ws, psf=False):
+def fit_forward_into(atoms, geom, data, fit, background, R, alpha, beta, loss, ws, psf=False,
+                     plan=None):
     code = {"l2": _lib.GR_FIT_L2, "kl": _lib.GR_FIT_KL}[fit]
-    fn = _lib.load().gr_psf_fit_forward if psf else _lib.load().gr_fit_forward
+    fn = _fn("fit_forward", psf, plan)
     st = fn(
         ctypes.byref(atoms.struct), ctypes.byref(geom.struct), code, data.data_ptr(),
         float(background), _ptr(R), _ptr(alpha), _ptr(beta), _ptr(loss), ws.data_ptr(),
@@ -351,8 +413,8 @@ def fit_forward_into(atoms, geom, data, fit, background, R, alpha, beta, loss, w
 
 
 def atom_derivs_into(atoms, geom, mode, field, beta_field, beta_const, order, f, g, H, ws,
-                     psf=False):
-    fn = _lib.load().gr_psf_atom_derivs if psf else _lib.load().gr_atom_derivs
+                     psf=False, plan=None):
+    fn = _fn("atom_derivs", psf, plan)
     st = fn(
         ctypes.byref(atoms.struct), ctypes.byref(geom.struct), MODES[mode], field.data_ptr(),
         _ptr(beta_field), float(beta_const), int(order), f.data_ptr(), g.data_ptr(), _ptr(H),

@@ -95,6 +95,58 @@ class FitRequest:
         self.size_hint = (n, cells)
 
 
+def validate_request(req):
+    """Host-side checks of a request before it may queue: consistent shapes
+    (orientations (A, d) with ortho/detector for a 2D, 2.5D or 3D geometry;
+    atoms I (N,), x (N, dim), r (N, 1 | 3 | 6)), at least one atom and one
+    angle, finite parameters and payload, a known fit with a positive KL
+    background, max_iter >= 1 and tol >= 0.  Raises ValueError naming the
+    first problem found."""
+    T = np.asarray(req.orientations, dtype=np.float64)
+    if T.ndim != 2 or T.shape[0] < 1 or T.shape[1] not in (2, 3):
+        raise ValueError("request %s: orientations must be (A, 2|3) with A >= 1" % req.id)
+    A, dT = T.shape
+    det = [np.asarray(d, dtype=np.float64).reshape(-1) for d in req.detector]
+    if len(det) not in (1, 2) or any(d.size < 1 for d in det):
+        raise ValueError("request %s: one or two non-empty detector coordinate vectors" % req.id)
+    if dT == 3 and len(det) != 2:
+        raise ValueError("request %s: 3D orientations need two detector axes" % req.id)
+    ortho = [np.asarray(o, dtype=np.float64) for o in req.ortho]
+    n_axes = len(det) if dT == 3 else 1
+    if len(ortho) < n_axes or any(o.shape != (A, dT) for o in ortho[:n_axes]):
+        raise ValueError("request %s: ortho must hold %d arrays of shape (%d, %d)"
+                         % (req.id, n_axes, A, dT))
+    dim = 3 if (dT == 3 or len(det) == 2) else 2
+    I, x, r = (np.asarray(v, dtype=np.float64) for v in req.init)
+    n = I.size
+    if n < 1:
+        raise ValueError("request %s: no atoms" % req.id)
+    if x.size != n * dim:
+        raise ValueError("request %s: x must be (%d, %d)" % (req.id, n, dim))
+    pr = r.size // n if r.size % n == 0 else -1
+    if pr not in (1, 3 if dim == 2 else 6):
+        raise ValueError("request %s: r must be (%d, 1) or (%d, %d)"
+                         % (req.id, n, n, 3 if dim == 2 else 6))
+    for name, v in (("I", I), ("x", x), ("r", r), ("orientations", T)):
+        if not np.all(np.isfinite(v)):
+            raise ValueError("request %s: %s holds NaN or Inf" % (req.id, name))
+    if req.fit not in ("l2", "kl"):
+        raise ValueError("request %s: fit must be 'l2' or 'kl'" % req.id)
+    if req.fit == "kl" and not req.background > 0:
+        raise ValueError("request %s: the KL fit needs a positive background" % req.id)
+    if int(req.max_iter) < 1 or not req.tol >= 0:
+        raise ValueError("request %s: max_iter >= 1 and tol >= 0" % req.id)
+    if req.data_host is not None:
+        d = req.data_host
+        shape = (A,) + tuple(v.size for v in det)
+        if tuple(d.shape) != shape and d.numel() != int(np.prod(shape)):
+            raise ValueError("request %s: data must have shape %s" % (req.id, shape))
+        if not bool(torch.isfinite(d).all()):
+            raise ValueError("request %s: data holds NaN or Inf" % req.id)
+    elif req.make_data is None:
+        raise ValueError("request %s: no data (data_host or make_data)" % req.id)
+
+
 _ALIGN = 256
 _TORCH_DTYPE = {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64,
                 np.dtype(np.int32): torch.int32, np.dtype(np.uint8): torch.uint8}
@@ -158,8 +210,11 @@ class _Slot:
     """Device state of one admitted request."""
 
     def __init__(self, req, stream, device, use_graph=True, iters_per_launch=4,
-                 device_loop=True, setup_stream=None):
+                 device_loop=True, setup_stream=None, plans=(None, None)):
         self.req = req
+        # launch schedules of this request's shape class (engine.Plan, or
+        # None for the process-wide one): projection, derivatives
+        self.plan_p, self.plan_d = plans
         self.stream = stream
         self.dev = device
         self.k = iters_per_launch
@@ -218,8 +273,10 @@ class _Slot:
         self.hist, self.hist_acc, self.counter = v("hist"), v("acc"), v("counter")
         shape = self.geom.shape
         kl = req.fit == "kl"
-        ws_p = max(256, engine.workspace_bytes(_lib.GR_OP_PROJECT, self.cur, self.geom))
-        ws_d = max(256, engine.workspace_bytes(_lib.GR_OP_DERIVS_2, self.cur, self.geom))
+        ws_p = max(256, engine.workspace_bytes(_lib.GR_OP_PROJECT, self.cur, self.geom,
+                                               self.plan_p))
+        ws_d = max(256, engine.workspace_bytes(_lib.GR_OP_DERIVS_2, self.cur, self.geom,
+                                               self.plan_d))
         wl, n_work = _layout([("data", np.float32, shape), ("alpha", np.float32, shape),
                               ("alpha_t", np.float32, shape)] +
                              ([("beta", np.float32, shape), ("beta_t", np.float32, shape)]
@@ -244,11 +301,12 @@ class _Slot:
         self.res_layout, n_res = _layout([("hist", np.float64, (L,)), ("acc", np.int32, (L,)),
                                           ("counter", np.int32, (1,)),
                                           ("theta", np.float64, (n, P)),
-                                          ("loss", np.float64, (1,))])
+                                          ("loss", np.float64, (1,)),
+                                          ("loss0", np.float64, (1,))])
         self.results = _pinned_take(n_res)
         r = lambda name: _view(self.results, self.res_layout[name])
         self.h_hist, self.h_acc, self.h_counter = r("hist"), r("acc"), r("counter")
-        self.h_theta, self.h_loss = r("theta"), r("loss")
+        self.h_theta, self.h_loss, self.h_loss0 = r("theta"), r("loss"), r("loss0")
         t_bufs = time.perf_counter()
         if setup is not stream:
             ready = torch.cuda.Event()
@@ -308,10 +366,13 @@ class _Slot:
         self.staging = self.results = None
 
     def prologue(self):
-        """Fit fields and loss of the starting atoms (once per fit)."""
+        """Fit fields and loss of the starting atoms (once per fit); the
+        starting loss is also copied out (the fit's initial loss)."""
         r = self.req
         engine.fit_forward_into(self.cur, self.geom, self.data, r.fit, r.background, None,
-                                self.alpha, self.beta, self.loss_cur, self.ws_p)
+                                self.alpha, self.beta, self.loss_cur, self.ws_p,
+                                plan=self.plan_p)
+        self.h_loss0.copy_(self.loss_cur.reshape(1), non_blocking=True)
 
     def iterate(self, loop=None):
         """One damped-Newton iteration.  The current atoms' fields are always
@@ -323,11 +384,12 @@ class _Slot:
         beta_c = 1.0 if r.fit == "l2" else 0.0
         with (loop.unless_rejected() if loop is not None else contextlib.nullcontext()):
             engine.atom_derivs_into(self.cur, self.geom, "field", self.alpha, self.beta, beta_c,
-                                    2, self.f, self.g, self.H, self.ws_d)
+                                    2, self.f, self.g, self.H, self.ws_d, plan=self.plan_d)
         engine.newton_solve_into(self.dim, self.iso, self.g, self.H, self.lam, self.theta,
                                  self.theta_trial, self.step, self.trial, self.dev)
         engine.fit_forward_into(self.trial, self.geom, self.data, r.fit, r.background, None,
-                                self.alpha_t, self.beta_t, self.loss_trial, self.ws_p)
+                                self.alpha_t, self.beta_t, self.loss_trial, self.ws_p,
+                                plan=self.plan_p)
         engine.newton_accept_into(self.dim, self.iso, self.loss_cur, self.loss_trial,
                                   self.theta, self.theta_trial, self.lam, 1e-4, 1e4,
                                   self.cur, self.trial, self.hist, self.hist_acc,
@@ -389,8 +451,12 @@ class _Slot:
         queued on the same stream are not waited for)."""
         c = min(int(self.h_counter[0]), self.req.max_iter)
         acc = self.h_acc.numpy()[:min(c, self.h_acc.numel())]
+        accepted = int((acc != 0).sum())
         return {"theta": self.h_theta.numpy().copy(), "loss": float(self.h_loss[0]),
-                "iterations": c, "rejected": int((acc == 0).sum())}
+                "loss0": float(self.h_loss0[0]), "iterations": c,
+                "rejected": int((acc == 0).sum()), "accepted": accepted,
+                # a fit that accepted no step returns its starting atoms
+                "status": "ok" if accepted > 0 else "no_progress"}
 
 
 _warmed = set()
@@ -429,7 +495,7 @@ class GaussFitServer:
 
     def __init__(self, device=None, max_slots=32, n_streams=16, hbm_budget=None,
                  hbm_reserve=4 << 30, use_graphs=True, iters_per_launch=4, device_loop=True,
-                 largest_first=True, exclusive_streams=True):
+                 largest_first=True, exclusive_streams=True, tuned=False):
         self.dev = torch.device(device or "cuda")
         engine._require_cuda(self.dev)
         self.max_slots = max_slots
@@ -455,6 +521,14 @@ class GaussFitServer:
         # destroying an executable graph waits for the whole device to idle,
         # which would stall the host loop behind every fit in flight.
         self._retired_loops = []
+        # launches of each request run under the plans tuned for its shape
+        # class (tune_classes), when there are any
+        self.tuned = tuned
+        self._hold_admission = False
+        self.admission_retries = 0   # admissions that failed and were retried
+        self.cancelled = set()       # ids of requests cancelled while in flight
+        self.errors = {}             # id -> reason, for requests that could not run
+        self._admit_fault = None     # test hook: called before a slot is built
         _warm_engine(self.dev)
 
     @staticmethod
@@ -472,9 +546,36 @@ class GaussFitServer:
         return int(1.3 * (sino + bitmap + deriv + per_atom)) + (8 << 20)
 
     def submit(self, req):
+        """Queue a request.  Malformed requests are refused here
+        (ValueError, see validate_request) and never reach the device."""
+        validate_request(req)
         self.pending.append(req)
 
+    def cancel(self, rid):
+        """Cancel a request.  A queued one leaves the queue; one in flight
+        runs to the end of its device work (nothing is killed on the
+        device), after which its result is discarded and its memory freed.
+        The request's result is then {"status": "cancelled"}.  Returns
+        False if the request is unknown or already finished."""
+        for req in list(self.pending):
+            if req.id == rid:
+                self.pending.remove(req)
+                self.results[rid] = {"status": "cancelled", "arrival": req.arrival}
+                return True
+        if any(slot.req.id == rid for slot in self.active):
+            self.cancelled.add(rid)
+            return True
+        return False
+
+    def _plans(self, req):
+        if not self.tuned:
+            return None, None
+        from . import tuning
+        return tuning.plans_for_request(req)
+
     def _admit(self, now):
+        if self._hold_admission:
+            return                      # retry only after a fit has finished
         if self.largest_first and len(self.pending) > 1:
             # among the requests that have arrived, the largest go first, so
             # the longest fits start early (arrival order otherwise kept)
@@ -497,12 +598,37 @@ class GaussFitServer:
                                       % (req.id, need, self.budget))
                 break
             self.pending.popleft()
+            ta = time.perf_counter()
+            try:
+                if self._admit_fault is not None:
+                    self._admit_fault(req)
+                slot = _Slot(req, self.streams[si], self.dev, self.use_graphs, self.k,
+                             self.device_loop, self.setup_stream, self._plans(req))
+            except _lib.EngineError as e:
+                # the engine refused the request's set-up: it cannot run
+                self.admit_seconds += time.perf_counter() - ta
+                self.errors[req.id] = "%s: %s" % (type(e).__name__, e)
+                self.results[req.id] = {"status": "error", "error": self.errors[req.id],
+                                        "arrival": req.arrival}
+                continue
+            except torch.cuda.OutOfMemoryError as e:
+                # the device could not take the request now: whatever the
+                # slot had allocated is garbage once this frame ends.  With
+                # fits in flight it waits (at the head of the queue) until
+                # one finishes; with none it can never fit.
+                self.admit_seconds += time.perf_counter() - ta
+                if not self.active:
+                    self.errors[req.id] = "%s: %s" % (type(e).__name__, e)
+                    self.results[req.id] = {"status": "error", "error": self.errors[req.id],
+                                            "arrival": req.arrival}
+                    continue
+                self.pending.appendleft(req)
+                self.admission_retries += 1
+                self._hold_admission = True
+                break
             self.stream_busy[si] += 1
             if self.active:
                 self.admitted_while_busy += 1
-            ta = time.perf_counter()
-            slot = _Slot(req, self.streams[si], self.dev, self.use_graphs, self.k,
-                         self.device_loop, self.setup_stream)
             self.admit_seconds += time.perf_counter() - ta
             phases = dict(slot.phase_seconds)
             if slot.loop is not None:
@@ -530,13 +656,17 @@ class GaussFitServer:
                 if not slot.event.query():
                     continue
                 progressed = True
-                if slot.done():
+                if slot.done() or slot.req.id in self.cancelled:
                     res = slot.result()
+                    if slot.req.id in self.cancelled:
+                        self.cancelled.discard(slot.req.id)
+                        res = {"status": "cancelled"}
                     res["arrival"] = slot.req.arrival
                     res["finish"] = time.perf_counter() - t0
                     res["latency"] = res["finish"] - slot.req.arrival
                     self.results[slot.req.id] = res
                     self.active.remove(slot)
+                    self._hold_admission = False
                     self.in_use -= slot.need
                     self.stream_busy[slot.stream_index] -= 1
                     if slot.loop is not None:
@@ -569,10 +699,14 @@ class GaussFitServer:
             self._retired_loops = []
 
 
-def serve_plain(requests, device=None, t0=None):
+def serve_plain(requests, device=None, t0=None, lean=False):
     """Baseline: the same fits one at a time with the eager host-driven loop
-    (no graphs, no overlap); a request starts at max(arrival, previous end)."""
-    from . import solvers
+    (no graphs, no overlap); a request starts at max(arrival, previous end).
+    lean=False keeps the reference loop's structure (NewtonGaussian.py:57-60
+    evaluates the derivatives on every inner iteration, and the current
+    atoms are projected anew each iteration); lean=True does only the work
+    the served loop does (one projection per iteration, no derivatives after
+    a rejected trial).  Both give the same fits."""
     dev = torch.device(device or "cuda")
     t0 = time.perf_counter() if t0 is None else t0
     out = {}
@@ -584,16 +718,16 @@ def serve_plain(requests, device=None, t0=None):
         geom = DeviceGeometry(req.orientations, req.ortho, req.detector, dev)
         data = req.device_data(geom, dev, stream)
         atoms = engine.DeviceAtoms(*req.init, dev)
-        losses = []
-        cur, losses = _plain_fit(atoms, geom, data, req)
+        cur, losses, accepted = _plain_fit(atoms, geom, data, req, lean)
         torch.cuda.synchronize(dev)
         fin = time.perf_counter() - t0
-        out[req.id] = {"loss": losses[-1], "iterations": len(losses) - 1,
+        out[req.id] = {"loss": losses[-1], "loss0": losses[0], "iterations": len(losses) - 1,
+                       "accepted": accepted, "status": "ok" if accepted else "no_progress",
                        "arrival": req.arrival, "finish": fin, "latency": fin - req.arrival}
     return out
 
 
-def _plain_fit(atoms, geom, data, req):
+def _plain_fit(atoms, geom, data, req, lean=False):
     """Eager damped Newton with the same accept rule and stopping test."""
     from . import solvers
     dim, iso = atoms.dim, atoms.iso
@@ -604,25 +738,36 @@ def _plain_fit(atoms, geom, data, req):
     cur = atoms
     losses = []
     rejects = 0
+    accepted = 0
+    fw = engine.fit_forward(cur, geom, data, fit, bg)
+    loss = float(fw["loss"].item())
+    g = H = None
     for it in range(req.max_iter):
-        fw = engine.fit_forward(cur, geom, data, fit, bg)
-        loss = float(fw["loss"].item())
+        if not lean and it > 0:
+            fw = engine.fit_forward(cur, geom, data, fit, bg)
+            loss = float(fw["loss"].item())
         if not losses:
             losses.append(loss)
-        _f, g, H = engine.atom_derivs(cur, geom, "field", fw["alpha"], fw["beta"], beta_c, 2)
+        if g is None or not lean or rejects == 0:
+            _f, g, H = engine.atom_derivs(cur, geom, "field", fw["alpha"], fw["beta"], beta_c, 2)
         th, _s, _fl = engine.newton_solve(dim, iso, g.contiguous(), H.contiguous(), lam, theta)
         trial = solvers.atoms_of(th, dim, geom.device)
-        new = float(engine.fit_forward(trial, geom, data, fit, bg, want_fields=False)["loss"].item())
+        fwt = engine.fit_forward(trial, geom, data, fit, bg, want_fields=lean)
+        new = float(fwt["loss"].item())
         if new <= loss:
             theta, cur = th, trial
+            if lean:
+                fw = fwt
             lam = torch.clamp(lam / 2, 1e-4, 1e4)
             losses.append(new)
             rejects = 0
-            if abs(loss - new) <= req.tol * max(abs(loss), 1e-300):
+            accepted += 1
+            prev, loss = loss, new
+            if abs(prev - new) <= req.tol * max(abs(prev), 1e-300):
                 break
         else:
             lam = torch.clamp(lam * 10, 1e-4, 1e4)
             rejects += 1
             if rejects >= MAX_BACKTRACK:
                 break
-    return cur, losses
+    return cur, losses, accepted

@@ -4,9 +4,11 @@ The derivative launch splits (atoms x angle chunks) into about
 ``GR_TUNE_DERIV_WARPS`` warps with at least ``GR_TUNE_DERIV_MIN_ANGLES`` angles
 per lane group and ``GR_TUNE_DERIV_ATOMS_PER_WARP`` atoms per warp; the best split depends on the atom count, angle count,
 support sizes and derivative order.  ``autotune_derivs`` times candidate
-splits on the actual problem with CUDA events and keeps the fastest; results
-are cached per shape class (detector dims, log2 atom count, log2 angle count,
-order, pixel-integrated or not) and reapplied by ``apply_for``.
+splits on the actual problem with CUDA events and keeps the fastest as an
+``engine.Plan`` (the C ABI's gr_plan) cached per shape class (detector dims,
+log2 atom count, log2 angle count, order, pixel-integrated or not):
+``plan_for`` returns it, and launches given that plan run the tuned split
+while other streams keep theirs; the process-wide values are not touched.
 Results do not depend on the split beyond FP rounding of the chunk sums.
 """
 import math
@@ -77,38 +79,121 @@ def shape_key(atoms, geom, order, psf=False):
 
 def autotune_derivs(atoms, geom, field, beta_field=None, beta_const=1.0, order=1,
                     psf=False, reps=5, candidates=None):
-    """Time every candidate split on this problem; apply and return the best
-    (target_warps, min_angles, atoms_per_warp, ms)."""
+    """Time every candidate split on this problem under a plan of its own;
+    cache the best plan for the problem's shape class and return
+    (target_warps, min_angles, atoms_per_warp, ms).  The process-wide
+    schedule is left as it was."""
     key = shape_key(atoms, geom, order, psf)
     cands = candidates or [(w, m, g) for w in WARPS for m in MIN_ANGLES
                            for g in ATOMS_PER_WARP]
-    saved = get_split()
+    op = _lib.GR_OP_DERIVS_1 if order == 1 else _lib.GR_OP_DERIVS_2
+    plan = engine.Plan(op, atoms, geom)
     best = None
     for cand in cands:
         w, m = cand[0], cand[1]
-        g = cand[2] if len(cand) > 2 else saved[2]
-        set_split(w, m, g)
-        engine.atom_derivs(atoms, geom, "field", field, beta_field, beta_const, order, psf=psf)
+        g = cand[2] if len(cand) > 2 else plan.get(2)
+        plan.set(0, w).set(1, m).set(2, g)
+        run = lambda: engine.atom_derivs(atoms, geom, "field", field, beta_field, beta_const,
+                                         order, psf=psf, plan=None if psf else plan)
+        if psf:
+            # the pixel-integrated kernels run under the process-wide values
+            saved = get_split()
+            set_split(w, m, g)
+        run()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
         for _ in range(reps):
-            engine.atom_derivs(atoms, geom, "field", field, beta_field, beta_const, order, psf=psf)
+            run()
         b.record()
         torch.cuda.synchronize()
+        if psf:
+            set_split(*saved)
         ms = a.elapsed_time(b) / reps
         if best is None or ms < best[3]:
             best = (w, m, g, ms)
     if best is None:
-        set_split(*saved)
         return None
-    _cache[key] = best[:3]
-    set_split(*best[:3])
+    plan.set(0, best[0]).set(1, best[1]).set(2, best[2])
+    _cache[key] = plan
     return best
 
 
+def plan_for(atoms, geom, order, psf=False):
+    """The tuned plan of this shape class, or None (then the process-wide
+    schedule applies)."""
+    return _cache.get(shape_key(atoms, geom, order, psf))
+
+
 def apply_for(atoms, geom, order, psf=False):
-    """Apply the cached split for this shape class, if any; returns it."""
-    v = _cache.get(shape_key(atoms, geom, order, psf))
-    if v is not None:
-        set_split(*v)
-    return v
+    """The cached split (target_warps, min_angles, atoms_per_warp) of this
+    shape class, or None; use ``plan_for`` to run under it."""
+    p = plan_for(atoms, geom, order, psf)
+    return None if p is None else (p.get(0), p.get(1), p.get(2))
+
+
+# ---------------------------------------------------------------------------
+# serving: plans per shape class of fitting requests
+# ---------------------------------------------------------------------------
+_req_plans = {}
+# small candidate sets: a server tunes each new class once, on its first
+# request, and the fits of the class then run under the winners
+DERIV_CANDIDATES = ((131072, 1, 1), (32768, 1, 1), (8192, 1, 1), (131072, 2, 1),
+                    (32768, 4, 1))
+PROJ_CANDIDATES = ((1, 4 << 20), (1, 0), (2, 4 << 20), (2, 0))
+
+
+def request_key(req, order=2):
+    """Shape class of a fitting request (as shape_key)."""
+    n = len(req.init[0])
+    return (len(req.detector), int(math.log2(max(1, n))),
+            int(math.log2(max(1, len(req.orientations)))), int(order), False)
+
+
+def plans_for_request(req, order=2):
+    """(projection plan, derivative plan) of the request's class, or
+    (None, None) when the class has not been tuned."""
+    return _req_plans.get(request_key(req, order), (None, None))
+
+
+def tune_request_classes(requests, device, reps=3, order=2):
+    """Tune each shape class among ``requests`` once, on its first request:
+    the projection's tiling and block split and the derivative split, each
+    timed under a plan of its own.  Returns the number of classes tuned."""
+    from .geometry import DeviceGeometry
+    done = 0
+    for req in requests:
+        key = request_key(req, order)
+        if key in _req_plans:
+            continue
+        geom = DeviceGeometry(req.orientations, req.ortho, req.detector, device)
+        atoms = engine.DeviceAtoms(*req.init, device)
+        stream = torch.cuda.current_stream(device)
+        data = req.device_data(geom, device, stream)
+        pp = engine.Plan(_lib.GR_OP_PROJECT, atoms, geom)
+        best_p = None
+        for form, split in PROJ_CANDIDATES:
+            pp.set(3, form).set(4, split)
+            ms = _time(lambda: engine.fit_forward(atoms, geom, data, req.fit, req.background,
+                                                  plan=pp), reps)
+            if best_p is None or ms < best_p[2]:
+                best_p = (form, split, ms)
+        pp.set(3, best_p[0]).set(4, best_p[1])
+        fw = engine.fit_forward(atoms, geom, data, req.fit, req.background, plan=pp)
+        autotune_derivs(atoms, geom, fw["alpha"], fw["beta"],
+                        1.0 if req.fit == "l2" else 0.0, order=order, reps=reps,
+                        candidates=DERIV_CANDIDATES)
+        _req_plans[key] = (pp, plan_for(atoms, geom, order))
+        done += 1
+    torch.cuda.synchronize(device)
+    return done
+
+
+def _time(fn, reps):
+    fn()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps

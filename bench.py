@@ -54,8 +54,8 @@ def parse():
                     help="skip the served-stream sub-run of the default line")
     ap.add_argument("--requests", type=int, default=512,
                     help="config3: requests in the served Poisson stream")
-    ap.add_argument("--compare", type=int, default=48,
-                    help="config3: requests fitted by both the server and the plain loop")
+    ap.add_argument("--compare", type=int, default=512,
+                    help="config3: requests fitted by both the server and the plain loops")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -753,6 +753,7 @@ def run_serving(args):
     dev = torch.device("cuda", local)
     importlib.import_module("__graft_entry__").build()
     serving = importlib.import_module(PKG + ".serving")
+    tuning = importlib.import_module(PKG + ".tuning")
     wl = importlib.import_module(PKG + ".workloads")
 
     def pct(v, q):
@@ -775,15 +776,21 @@ def run_serving(args):
     cmp_reqs = wl.materialize_data(wl.config3_requests(n=args.compare, seed=3), dev)
     for r in cmp_reqs:
         r.arrival = 0.0
+    # every shape class of the stream is tuned once (the server would do so
+    # on the first request of a class): projection and derivative schedules
+    # held in plans per class
+    t_tune = time.perf_counter()
+    n_classes = tuning.tune_request_classes(cmp_reqs, dev)
+    t_tune = time.perf_counter() - t_tune
     # one untimed pass of the same mix first: the first graph instantiations
     # made while the GPU is loaded grow the driver's pools (about 1 ms each,
     # once per process), which a running server has long paid
-    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31)
+    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31, tuned=True)
     for r in cmp_reqs:
         srv.submit(r)
     srv.run()
     t0 = time.perf_counter()
-    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31)
+    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31, tuned=True)
     for r in cmp_reqs:
         srv.submit(r)
     served_cmp = srv.run(t0=t0)
@@ -791,20 +798,30 @@ def run_serving(args):
     admit_cmp = srv.admit_seconds
     phases_cmp = dict(srv.admit_phases)
     loops_cmp = srv.device_loops
-    plain_reqs = wl.config3_requests(n=args.compare, seed=3)
-    for r, c in zip(plain_reqs, cmp_reqs):
-        r.arrival = 0.0
-        r.data_host = c.data_host
-    t0 = time.perf_counter()
-    plain = serving.serve_plain(plain_reqs, dev, t0=t0)
-    t_plain = time.perf_counter() - t0
+
+    def plain_run(lean):
+        reqs = wl.config3_requests(n=args.compare, seed=3)
+        for r, c in zip(reqs, cmp_reqs):
+            r.arrival = 0.0
+            r.data_host = c.data_host
+        t0 = time.perf_counter()
+        res = serving.serve_plain(reqs, dev, t0=t0, lean=lean)
+        return res, time.perf_counter() - t0
+    plain, t_plain = plain_run(False)
+    lean, t_lean = plain_run(True)
 
     # (2) the Poisson stream (200 requests/s)
-    stream_reqs = wl.materialize_data(wl.config3_requests(n=args.requests, seed=3), dev)
+    # the stream's requests are the comparison's (same seed): reuse their data
+    stream_reqs = wl.config3_requests(n=args.requests, seed=3)
+    if args.requests <= args.compare:
+        for r, c in zip(stream_reqs, cmp_reqs):
+            r.data_host = c.data_host
+    else:
+        wl.materialize_data(stream_reqs, dev)
     sampler = ClockSampler(local)
     sampler.start()
     t0 = time.perf_counter()
-    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31)
+    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31, tuned=True)
     for r in stream_reqs:
         srv.submit(r)
     res = srv.run(t0=t0)
@@ -813,8 +830,20 @@ def run_serving(args):
     lat = [v["latency"] for v in res.values()]
     its = [v["iterations"] for v in res.values()]
     fits_s = len(res) / makespan
+
+    def progress(results):
+        """fits that accepted at least one step, and those that accepted none
+        (they return their starting atoms)"""
+        ok = [v for v in results.values() if v.get("accepted", 0) > 0]
+        return len(ok), len(results) - len(ok)
+    ok_cmp, none_cmp = progress(served_cmp)
+    ok_plain, _ = progress(plain)
+    ok_stream, none_stream = progress(res)
+    gain = [v["loss"] / v["loss0"] for v in served_cmp.values()
+            if v.get("loss0") and v.get("accepted", 0) > 0]
     out = {
         "metric": "served fits/s (config 3 stream)", "value": fits_s, "unit": "fits/s",
+        "fits_with_progress": ok_stream, "fits_without_progress": none_stream,
         "n_gpus": ws, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (FP64 reductions and Newton solves)",
         "data": "synthetic (seeded per request)",
@@ -826,9 +855,19 @@ def run_serving(args):
         "makespan_s": makespan,
         "saturation_compare": {
             "requests": args.compare,
-            "served_fits_s": args.compare / t_served,
-            "plain_fits_s": args.compare / t_plain,
+            # fits/s count only fits that accepted at least one step; the
+            # others (same in every arm: the same rule) are reported apart
+            "fits_with_progress": ok_cmp, "fits_without_progress": none_cmp,
+            "served_fits_s": ok_cmp / t_served,
+            "plain_fits_s": ok_plain / t_plain,
+            "plain_lean_fits_s": ok_plain / t_lean,
             "speedup": t_plain / t_served,
+            "speedup_vs_lean_plain": t_lean / t_served,
+            "plain": "host-driven eager loop, reference structure (re-projects the current "
+                     "atoms and evaluates derivatives every iteration)",
+            "plain_lean": "host-driven eager loop doing only the served loop's work",
+            "final_over_initial_loss_median": float(np.median(gain)) if gain else None,
+            "shape_classes_tuned": n_classes, "tuning_s": t_tune,
             "served_admission_host_s": admit_cmp,
             "served_admission_phases_s": phases_cmp,
             "served_device_loops": loops_cmp,
@@ -836,8 +875,10 @@ def run_serving(args):
             # of the device loop skips its derivatives (atoms unchanged)
             "served_trials": int(sum(v["iterations"] for v in served_cmp.values())),
             "served_rejected_trials": int(sum(v.get("rejected", 0) for v in served_cmp.values())),
+            "served_latency_p50_s": pct([v["latency"] for v in served_cmp.values()], 50),
             "served_latency_p99_s": pct([v["latency"] for v in served_cmp.values()], 99),
             "plain_latency_p99_s": pct([v["latency"] for v in plain.values()], 99),
+            "plain_lean_latency_p99_s": pct([v["latency"] for v in lean.values()], 99),
         },
         "clocks": clocks,
     }

@@ -311,6 +311,45 @@ int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);
 
 /*
+ * Plans: a schedule of the same knobs held by the caller instead of the
+ * process-wide one, so that concurrent streams (a serving process fitting
+ * problems of different shapes at once) each run the split and tiling tuned
+ * for their shape class.  No reference counterpart: the reference's kernel
+ * modules derive their launch configuration from each call's sizes
+ * (NewtonBases2D.py:302-316) and keep no schedule.
+ *   gr_plan_create: a plan for op (GR_OP_PROJECT, GR_OP_DERIVS_1/2) on
+ *     problems shaped like atoms/geom (only their sizes are read), holding a
+ *     copy of the current process-wide values; GR_ERR_ARG / GR_ERR_SHAPE as
+ *     gr_workspace_bytes' argument checks.
+ *   gr_plan_set / gr_plan_get: as gr_set_tuning / gr_get_tuning on the plan.
+ *   gr_plan_workspace_bytes: gr_workspace_bytes under the plan's schedule.
+ *   gr_radproj_plan, gr_fit_forward_plan, gr_atom_derivs_plan: gr_radproj,
+ *     gr_fit_forward and gr_atom_derivs under the plan's schedule (any
+ *     problem size; the workspace must hold gr_plan_workspace_bytes of it).
+ * Results do not depend on the schedule beyond the FP rounding stated for
+ * gr_set_tuning.  A plan may be used by several streams at once; destroy it
+ * only when no launch made with it is still to be enqueued (launches
+ * already enqueued hold their own copy of the schedule).
+ */
+typedef struct gr_plan gr_plan;
+int gr_plan_create(int op, const gr_atoms *atoms, const gr_geometry *geom, gr_plan **plan);
+int gr_plan_destroy(gr_plan *plan);
+int gr_plan_set(gr_plan *plan, int key, int value);
+int gr_plan_get(const gr_plan *plan, int key);
+size_t gr_plan_workspace_bytes(const gr_plan *plan, int op, const gr_atoms *atoms,
+                               const gr_geometry *geom);
+int gr_radproj_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                    float *R, void *workspace, size_t workspace_bytes, void *stream);
+int gr_fit_forward_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                        int fit, const float *data, float background, float *R, float *alpha,
+                        float *beta, double *loss, void *workspace, size_t workspace_bytes,
+                        void *stream);
+int gr_atom_derivs_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                        int mode, const float *field, const float *beta_field,
+                        float beta_const, int order, double *f, double *g, double *H,
+                        void *workspace, size_t workspace_bytes, void *stream);
+
+/*
  * Per-angle detector moments of a sinogram, for the moment-matching initial
  * guess of a new atom.  Replaces the reference's MOM0 / MOM1 / MOM2
  * (KL_GaussRadon.py:227-253, :347-368), CPU loops inside its guess
@@ -450,7 +489,11 @@ int gr_kernel_timer_read(int which, double *total_ms, int *launches);
  * Problems whose projection workspace (gr_workspace_bytes(GR_OP_PROJECT, ..))
  * exceeds 4 MiB are rejected with GR_ERR_TOO_LARGE.  The call allocates
  * nothing.  The first call on a device looks up the scratch address on that
- * device (make it before any stream capture there).  All calls share the
+ * device (make it before any stream capture there); the address is kept per
+ * CUDA context, so a call under another context of the device (one the
+ * caller created, or the primary context re-created after cudaDeviceReset)
+ * looks it up again, and the first call under that context should also come
+ * before any capture.  All calls share the
  * scratch: calls whose GPU work overlaps in time race and must be serialised
  * by the caller.  Results equal gr_radproj's.
  */

@@ -97,3 +97,39 @@ def test_fit_loop_calls_reject_bad_arguments_without_gpu():
     assert lib.gr_fit_loop_launch(None, None) == err
     assert lib.gr_fit_loop_destroy(None) == lib_mod.GR_OK
     assert lib.gr_fit_loop_begin(None, None, None) == err
+
+
+def test_plan_create_set_get_without_gpu():
+    """gr_plan_*: a caller-owned schedule; argument checks and workspace sizes
+    run on the host (sizes only: no pointer is dereferenced)."""
+    lib_mod = importlib.import_module("2018_dictionary_tomography_gb300._lib")
+    lib = lib_mod.load()
+    at = lib_mod.GrAtoms()
+    at.n_atoms = 100
+    at.I = at.x = at.r = 16            # non-null stand-ins, never read
+    g = lib_mod.GrGeometry()
+    g.kdet, g.n_angles, g.frames = 2, 50, 16
+    for k in range(2):
+        g.n_det[k], g.det[k] = 64, 16
+        g.det_first[k], g.det_inv_step[k] = -1.0, 32.0
+    h = ctypes.c_void_p()
+    assert lib.gr_plan_create(9, ctypes.byref(at), ctypes.byref(g), ctypes.byref(h)) == -1
+    assert lib.gr_plan_create(2, ctypes.byref(at), ctypes.byref(g), ctypes.byref(h)) == 0
+    assert h.value
+    # a copy of the process-wide values, then independent of them
+    for key in (0, 1, 2, 3, 4, 6, 7):
+        assert lib.gr_plan_get(h, key) == lib.gr_get_tuning(key)
+    assert lib.gr_plan_set(h, 3, 2) == 0 and lib.gr_plan_get(h, 3) == 2
+    assert lib.gr_get_tuning(3) == 1
+    assert lib.gr_plan_set(h, 3, 5) == -1 and lib.gr_plan_set(h, 5, 1) == -1
+    assert lib.gr_plan_get(h, 5) == -1
+    # the workspace follows the plan's schedule (32-row tiles: fewer bitmaps)
+    ws_default = lib.gr_workspace_bytes(0, ctypes.byref(at), ctypes.byref(g))
+    ws_plan = lib.gr_plan_workspace_bytes(h, 0, ctypes.byref(at), ctypes.byref(g))
+    assert 0 < ws_plan < ws_default
+    # at least 4 angles per lane group: fewer angle chunks, smaller partials
+    assert lib.gr_plan_set(h, 1, 4) == 0 and lib.gr_plan_set(h, 7, 0) == 0
+    assert (lib.gr_plan_workspace_bytes(h, 2, ctypes.byref(at), ctypes.byref(g)) <
+            lib.gr_workspace_bytes(2, ctypes.byref(at), ctypes.byref(g)))
+    assert lib.gr_plan_destroy(h) == 0
+    assert lib.gr_radproj_plan(None, ctypes.byref(at), ctypes.byref(g), None, None, 0, None) == -1

@@ -4,6 +4,7 @@ seeded served-stream generator."""
 import importlib
 
 import numpy as np
+import pytest
 import torch
 
 PKG = "2018_dictionary_tomography_gb300"
@@ -107,3 +108,57 @@ def test_served_stream_is_seeded_and_within_its_ranges():
         assert cells == A * D ** (dim - 1)
         assert ra.fit == "l2" and ra.max_iter == 100
     assert set(dims) == {2, 3}
+
+
+def _valid_request():
+    wl = importlib.import_module(PKG + ".workloads")
+    return wl.config3_requests(n=1, seed=5, atoms=(8, 16), angles=(10, 12), det=(24, 32))[0]
+
+
+def test_malformed_requests_are_refused_before_the_device():
+    """validate_request (GaussFitServer.submit): shape mismatches, NaN
+    parameters or data, empty atom sets and bad fit settings raise ValueError
+    on the host."""
+    import copy
+
+    import torch
+    serving = importlib.import_module(PKG + ".serving")
+    req = _valid_request()
+    serving.validate_request(req)
+    cases = []
+    r = copy.copy(req)
+    I, x, rr = req.init
+    r.init = (I[:0], x[:0], rr[:0])
+    cases.append(("no atoms", r))
+    r = copy.copy(req)
+    r.init = (I, x[:, :1], rr)
+    cases.append(("x shape", r))
+    r = copy.copy(req)
+    x2 = np.array(x, dtype=np.float64)
+    x2[0, 0] = np.nan
+    r.init = (I, x2, rr)
+    cases.append(("nan atom", r))
+    r = copy.copy(req)
+    r.ortho = (np.asarray(req.ortho[0])[:-1],)
+    cases.append(("ortho length", r))
+    r = copy.copy(req)
+    r.orientations = np.zeros((0, 2))
+    cases.append(("no angles", r))
+    r = copy.copy(req)
+    r.fit, r.background = "kl", 0.0
+    cases.append(("kl background", r))
+    r = copy.copy(req)
+    r.max_iter = 0
+    cases.append(("max_iter", r))
+    r = copy.copy(req)
+    shape = (len(req.orientations),) + tuple(len(d) for d in req.detector)
+    bad = torch.zeros(shape)
+    bad[0].view(-1)[0] = float("inf")
+    r.data_host = bad
+    cases.append(("inf data", r))
+    r = copy.copy(req)
+    r.data_host = torch.zeros(3, 3)
+    cases.append(("data shape", r))
+    for what, rq in cases:
+        with pytest.raises(ValueError):
+            serving.validate_request(rq)

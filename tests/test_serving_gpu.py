@@ -138,3 +138,111 @@ def test_gated_derivatives_match_eager_loop_after_rejections(cuda_ready):
     assert np.array_equal(gated["theta"], eager["theta"])
     assert gated["loss"] == eager["loss"]
     s.loop.close()
+
+
+def test_lean_plain_loop_gives_the_same_fits(cuda_ready):
+    """The plain loop without the reference structure's repeated work (no
+    re-projection of the current atoms, no derivatives after a rejection)
+    takes exactly the same steps."""
+    ref = serving.serve_plain(_requests(n=4))
+    lean = serving.serve_plain(_requests(n=4), lean=True)
+    for k in ref:
+        assert ref[k]["iterations"] == lean[k]["iterations"]
+        assert ref[k]["loss"] == lean[k]["loss"]
+        assert ref[k]["accepted"] == lean[k]["accepted"]
+
+
+def test_admission_failure_waits_for_memory_then_runs(cuda_ready):
+    """An allocation failure at admission (injected on the host: the hook
+    raises the allocator's out-of-memory error once) puts the request back at
+    the head of the queue; it is admitted again once a fit has finished and
+    its result equals the undisturbed one.  With nothing in flight, a request
+    that cannot be allocated ends with an error result and the server goes
+    on."""
+    reqs = _requests(n=4)
+    for r in reqs:
+        r.arrival = 0.0
+    clean_srv = serving.GaussFitServer(max_slots=4, n_streams=4)
+    for r in _requests(n=4):
+        r.arrival = 0.0
+        clean_srv.submit(r)
+    clean = clean_srv.run()
+    srv = serving.GaussFitServer(max_slots=4, n_streams=4)
+    fired = []
+
+    def fault(req):
+        if req.id == reqs[2].id and not fired:
+            fired.append(req.id)
+            raise torch.cuda.OutOfMemoryError("injected: no memory for this request now")
+    srv._admit_fault = fault
+    for r in reqs:
+        srv.submit(r)
+    res = srv.run()
+    assert fired and srv.admission_retries == 1
+    for k in clean:
+        assert res[k]["status"] == clean[k]["status"]
+        assert np.array_equal(res[k]["theta"], clean[k]["theta"])
+    # nothing in flight: the request cannot ever fit -> error, others still run
+    srv2 = serving.GaussFitServer(max_slots=1, n_streams=1)
+    reqs2 = _requests(n=2)
+
+    def always(req):
+        if req.id == reqs2[0].id:
+            raise torch.cuda.OutOfMemoryError("injected")
+    srv2._admit_fault = always
+    for r in reqs2:
+        r.arrival = 0.0
+        srv2.submit(r)
+    res2 = srv2.run()
+    assert res2[reqs2[0].id]["status"] == "error"
+    assert res2[reqs2[1].id]["status"] in ("ok", "no_progress")
+
+
+def test_cancel_queued_and_in_flight_requests(cuda_ready):
+    """cancel(): a queued request leaves the queue; one in flight finishes
+    its device work, then its result is discarded.  The others are not
+    affected."""
+    reqs = _requests(n=5)
+    for r in reqs:
+        r.arrival = 0.0
+    srv = serving.GaussFitServer(max_slots=2, n_streams=2)
+    for r in reqs:
+        srv.submit(r)
+    assert srv.cancel(reqs[4].id)             # still queued
+    srv._admit(0.0)                            # two fits now in flight
+    inflight = srv.active[0].req.id
+    assert srv.cancel(inflight)
+    assert not srv.cancel(12345)
+    res = srv.run()
+    assert res[reqs[4].id]["status"] == "cancelled"
+    assert res[inflight]["status"] == "cancelled"
+    clean_srv = serving.GaussFitServer(max_slots=2, n_streams=2)
+    for r in _requests(n=5):
+        r.arrival = 0.0
+        clean_srv.submit(r)
+    clean = clean_srv.run()
+    for k in res:
+        if res[k]["status"] != "cancelled":
+            assert np.array_equal(res[k]["theta"], clean[k]["theta"])
+    assert not srv.active and srv.in_use == 0
+
+
+def test_tuned_server_runs_each_class_under_its_plans(cuda_ready):
+    """tune_request_classes times candidate schedules per shape class under
+    plans; a tuned server's fits match the untuned ones (the schedule only
+    changes FP rounding of derivative chunk sums)."""
+    tuning = importlib.import_module(PKG + ".tuning")
+    reqs = _requests(n=4)
+    n = tuning.tune_request_classes(reqs, torch.device("cuda"), reps=1)
+    assert n >= 1
+    assert all(p is not None for p in tuning.plans_for_request(reqs[0]))
+    srv = serving.GaussFitServer(max_slots=4, n_streams=4, tuned=True)
+    base = serving.GaussFitServer(max_slots=4, n_streams=4)
+    for r, q in zip(reqs, _requests(n=4)):
+        r.arrival = q.arrival = 0.0
+        srv.submit(r)
+        base.submit(q)
+    a, b = srv.run(), base.run()
+    for k in a:
+        assert abs(a[k]["loss"] - b[k]["loss"]) <= 1e-4 * abs(b[k]["loss"])
+        assert a[k]["loss"] <= a[k]["loss0"]
