@@ -76,7 +76,8 @@ class FitRequest:
         return self.make_data(geom, device, stream)
 
     def __init__(self, rid, orientations, ortho, detector, init, make_data, fit="l2",
-                 background=0.0, max_iter=100, tol=1e-6, arrival=0.0, lam0=1.0):
+                 background=0.0, max_iter=100, tol=1e-6, arrival=0.0, lam0=1.0,
+                 lam_max=1e8):
         self.id = rid
         self.orientations = orientations
         self.ortho = ortho
@@ -89,6 +90,13 @@ class FitRequest:
         self.tol = tol
         self.arrival = arrival
         self.lam0 = lam0
+        # damping bounds of the all-atoms step: lam in [1e-4, lam_max].  The
+        # reference clamps its per-atom damping at 1e4 (NewtonGaussian.py:92);
+        # all atoms stepping at once need more: the steps of overlapping
+        # atoms add up, and with the ceiling at 1e4 the backtracking stalls
+        # there, repeating one rejected trial (on the 512-request stream 204
+        # fits ended without an accepted step; with 1e8 none)
+        self.lam_max = lam_max
         self.data_host = None       # optional payload (pinned host tensor)
         n = len(init[0])
         cells = len(orientations) * int(np.prod([len(d) for d in detector]))
@@ -391,7 +399,7 @@ class _Slot:
                                 self.alpha_t, self.beta_t, self.loss_trial, self.ws_p,
                                 plan=self.plan_p)
         engine.newton_accept_into(self.dim, self.iso, self.loss_cur, self.loss_trial,
-                                  self.theta, self.theta_trial, self.lam, 1e-4, 1e4,
+                                  self.theta, self.theta_trial, self.lam, 1e-4, r.lam_max,
                                   self.cur, self.trial, self.hist, self.hist_acc,
                                   self.counter, self.dev,
                                   fields=(self.alpha_t, self.alpha, self.beta_t, self.beta))
@@ -758,7 +766,7 @@ def _plain_fit(atoms, geom, data, req, lean=False):
             theta, cur = th, trial
             if lean:
                 fw = fwt
-            lam = torch.clamp(lam / 2, 1e-4, 1e4)
+            lam = torch.clamp(lam / 2, 1e-4, req.lam_max)
             losses.append(new)
             rejects = 0
             accepted += 1
@@ -766,7 +774,7 @@ def _plain_fit(atoms, geom, data, req, lean=False):
             if abs(prev - new) <= req.tol * max(abs(prev), 1e-300):
                 break
         else:
-            lam = torch.clamp(lam * 10, 1e-4, 1e4)
+            lam = torch.clamp(lam * 10, 1e-4, req.lam_max)
             rejects += 1
             if rejects >= MAX_BACKTRACK:
                 break

@@ -49,9 +49,11 @@ def test_concurrent_streams_with_different_plans(eng, cuda_ready):
             assert torch.equal(x, y)
     # the plans did not touch the process-wide schedule
     assert [lib.load().gr_get_tuning(k) for k in (0, 1, 2, 3, 4, 6, 7)] == saved
-    # and the projection is the same under either tiling (sums in atom order)
-    rd = _fit(eng, ga, aa, da, None, None, 2)
-    assert torch.equal(rd[0], alone_a[0])
+    # the tiling leaves the projection bitwise equal (cells sum their atoms in
+    # index order): plan b's 32 x 32 tiles against the default 16 x 32 ones,
+    # both with the block split of small problems
+    rd = _fit(eng, gb, ab, db, None, None, 2)
+    assert torch.equal(rd[0], alone_b[0])
 
 
 def test_autotuned_plan_per_shape_class(eng, cuda_ready):

@@ -168,10 +168,12 @@ def test_admission_failure_waits_for_memory_then_runs(cuda_ready):
         clean_srv.submit(r)
     clean = clean_srv.run()
     srv = serving.GaussFitServer(max_slots=4, n_streams=4)
-    fired = []
+    fired, calls = [], []
 
     def fault(req):
-        if req.id == reqs[2].id and not fired:
+        # the second admission: one fit is then in flight
+        calls.append(req.id)
+        if len(calls) == 2 and not fired:
             fired.append(req.id)
             raise torch.cuda.OutOfMemoryError("injected: no memory for this request now")
     srv._admit_fault = fault
