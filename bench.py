@@ -331,6 +331,7 @@ def run_ours(args):
         "frac": (S / (dom_ms * 1e-3)) / ex2_rate,
         "peak_source": "measured ex2.approx probe on this GPU (gr_probe_ex2)",
         "traffic": traffic,
+        "traffic_source": "not measured in this run: " + (profile_source("traffic.json") or "none"),
         "ms_per_launch": dom_ms,
         "units_per_launch": S,
         "unit_note": "one ex2 per in-support (atom, angle, cell) evaluation",
@@ -367,8 +368,9 @@ def run_ours(args):
             "peak_source": "%d SMs x 4 schedulers x 1 warp instruction per clock at the "
                            "median SM clock sampled in the timed region" % n_sm,
             "instructions_per_launch": instr,
-            "instructions_source": "ncu smsp__inst_executed.sum of the committed capture "
-                                   "(profiles/instructions.json)",
+            "instructions_source": "ncu smsp__inst_executed.sum of the committed capture, not "
+                                   "measured in this run: " + (profile_source("instructions.json")
+                                                               or "none"),
         }
 
     out = {
@@ -491,6 +493,15 @@ def profiled_instructions(workload, kernel):
         tab = json.load(f)
     v = tab.get(workload.split(":")[0], {}).get(kernel)
     return None if v is None else float(v)
+
+
+def profile_source(name):
+    """The note of a committed ncu table: which capture and kernels it holds."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f).get("_note")
 
 
 def profiled_traffic(workload, kernel):
