@@ -56,6 +56,10 @@ constexpr int kRowChunk = 8;
 #ifndef GR_GRAD_MIN_BLOCKS
 #define GR_GRAD_MIN_BLOCKS 8
 #endif
+// resident blocks per SM asked of the 2D Hessian kernel with one angle per lane
+#ifndef GR_HESS2D_MIN_BLOCKS
+#define GR_HESS2D_MIN_BLOCKS 3
+#endif
 constexpr int kRowChunk3 = GR_ROW_CHUNK_3D;
 
 // Work split of the derivative kernels (Tuning, gr_set_tuning / gr_plan_set):
@@ -277,7 +281,8 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
 // the Hessian kernel from 255 to 168 registers (3 resident blocks per SM
 // instead of 2).
 template <int K, int ORDER, bool ONE>
-__global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS : (ONE ? 3 : 1))
+__global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS
+                                           : (ONE ? (K == 1 ? GR_HESS2D_MIN_BLOCKS : 3) : 1))
     gr_deriv_kernel(Atoms at, Geom g, DerivIn in, DerivCfg cfg, float *part) {
   constexpr int D = K + 1;
   constexpr int PR = n_rparam<K>();

@@ -21,10 +21,13 @@
 
 namespace gr {
 
+// pairs (2D only, nullable): the pair's projection data as the 2D
+// projection stages it, two float4 per (angle, atom) at [a n + j], written
+// here once instead of being recomputed by every tile the atom touches
 template <int K>
 __global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
                                                      TileCfg tc, uint32_t *bitmap,
-                                                     int W) {
+                                                     int W, float4 *pairs) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int a = blockIdx.y;
   if (j >= at.n) return;
@@ -32,6 +35,13 @@ __global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
   load_frame<K>(g.frames, a, f);
   Pair<K> p;
   pair_setup<K>(at, j, f, g, p);
+  if constexpr (K == 1) {
+    if (pairs) {
+      float4 *rec = pairs + ((size_t)a * at.n + j) * 2;
+      rec[0] = make_float4(p.qh[0], p.ql[0], p.G[0], p.l2amp);
+      rec[1] = make_float4(__int_as_float(p.lo[0]), __int_as_float(p.hi[0]), p.sgn, 0.f);
+    }
+  }
   if (p.lo[0] > p.hi[0]) return;
   const uint32_t bit = 1u << (j & 31);
   const size_t base = (size_t)a * tc.ntiles;
@@ -353,7 +363,8 @@ __global__ void __launch_bounds__(kProjWarps * 32)
 template <bool KAHAN, int NW>
 __global__ void __launch_bounds__(NW * 32)
     gr_project1d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
-                        int W, ProjOut out, double *loss_out, int *done) {
+                        int W, ProjOut out, double *loss_out, int *done,
+                        const float4 *__restrict__ pairs) {
   constexpr int T = NW * 32;
   __shared__ float4 prm[T][2];
   __shared__ int list[T];
@@ -365,8 +376,7 @@ __global__ void __launch_bounds__(NW * 32)
   const int D0 = g.ax[0].n;
   const int cell = t * tc.t0 + lane;
   const float pc = cell < D0 ? g.ax[0].coords[cell] : 0.f;
-  Frame<1> f;
-  load_frame<1>(g.frames, a, f);
+  const float4 *apairs = pairs + (size_t)a * at.n * 2;
   float acc = 0.f, cmp = 0.f;
 
   const uint32_t *words = bitmap + (size_t)item * W;
@@ -402,12 +412,12 @@ __global__ void __launch_bounds__(NW * 32)
     __syncthreads();
     total = wsum[0];
     wb += ntake > 0 ? ntake : W;   // ntake = 0 only past the last word
-    // pair data of the listed atoms, one per thread
+    // pair data of the listed atoms (set up once per pair by the binning
+    // launch), one per thread
     if ((int)threadIdx.x < total) {
-      Pair<1> p;
-      pair_setup<1>(at, list[threadIdx.x], f, g, p);
-      prm[threadIdx.x][0] = make_float4(p.qh[0], p.ql[0], p.G[0], p.l2amp);
-      prm[threadIdx.x][1] = make_float4(__int_as_float(p.lo[0]), __int_as_float(p.hi[0]), p.sgn, 0.f);
+      const float4 *rec = apairs + (size_t)list[threadIdx.x] * 2;
+      prm[threadIdx.x][0] = __ldg(rec);
+      prm[threadIdx.x][1] = __ldg(rec + 1);
     }
     __syncthreads();
     // warp w: slice [w total / NW, (w + 1) total / NW) in list order
@@ -811,6 +821,8 @@ size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1,
   bytes += align_up(items * W * sizeof(uint32_t));
   bytes += align_up(items * sizeof(double));
   bytes += align_up(kLossMaxBlocks * sizeof(double));  // block sums of the loss finalize
+  if (K == 1)  // per-(angle, atom) pair records of the 2D projection
+    bytes += align_up((size_t)n_angles * (size_t)n_atoms * 2 * sizeof(float4));
   return bytes;
 }
 
@@ -831,6 +843,8 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   uint32_t *bitmap = reinterpret_cast<uint32_t *>(wp);
   wp += align_up(items * W * sizeof(uint32_t));
   double *loss_part = reinterpret_cast<double *>(wp);
+  wp += align_up(items * sizeof(double)) + align_up(kLossMaxBlocks * sizeof(double));
+  float4 *pairs = K == 1 ? reinterpret_cast<float4 *>(wp) : nullptr;
   // one clear covers the counters and the bitmap
   if (cudaMemsetAsync(ws, 0, align_up(2 * sizeof(int)) + items * W * sizeof(uint32_t), stream) !=
       cudaSuccess)
@@ -845,9 +859,9 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
       if (K == 1) gr_psf_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, psf_s);
       else gr_psf_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, psf_s);
     } else if (K == 1) {
-      gr_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W);
+      gr_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, pairs);
     } else {
-      gr_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W);
+      gr_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, nullptr);
     }
     note_launches(1);
   }
@@ -870,10 +884,10 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
     double *lo = fused_loss ? loss_out : nullptr;
     if (W >= 8)  // 8 warps share a tile's atoms from 8 bitmap words (256 atoms) up
       gr_project1d_kernel<true, 8><<<(unsigned)items, 8 * 32, 0, stream>>>(
-          at, g, tc, bitmap, W, o, lo, next_item + 1);
+          at, g, tc, bitmap, W, o, lo, next_item + 1, pairs);
     else
       gr_project1d_kernel<true, kProjWarps><<<(unsigned)items, kProjWarps * 32, 0, stream>>>(
-          at, g, tc, bitmap, W, o, lo, next_item + 1);
+          at, g, tc, bitmap, W, o, lo, next_item + 1, pairs);
   } else {
     // the split is chosen from the problem's size alone (not from the
     // tiling), so both tilings keep giving the same cell sums
