@@ -27,7 +27,9 @@ What is recorded (``tests/golden/reference_kernels.npz``):
   ``derivs_RadProj`` and ``VolProj`` (point_spread_functions.py:143-1523) in 2D
   and 3D;
 * ``NewtonGaussian.linesearch`` and ``GD_lib.linesearch_block`` runs on a small
-  2D anisotropic L2 problem: final atoms and the energy history.
+  2D anisotropic L2 problem: final atoms and the energy history;
+* ``KL_GaussRadon.doKL_ProjGDStep_iso`` (the moment-matching atom guess) on a
+  seeded 2D residual with t = 1 and t = 0.5.
 
 Needs the reference checkout (run from the repository root):
 
@@ -363,6 +365,51 @@ def fit_sets(mods, out):
             print("  gd %s: %d energies, %.1f s" % (blocks, E.size, time.time() - t0))
 
 
+class SinoS(Sino):
+    """A Sino with the ``.space`` (detector, ortho, orientations) that
+    KL_GaussRadon.doKL_ProjGDStep_iso reads from its residual."""
+
+    def __array_finalize__(self, obj):
+        self.space = getattr(obj, "space", None)
+
+
+def kl_set(mods, out, root):
+    """KL_GaussRadon.doKL_ProjGDStep_iso (KL_GaussRadon.py:57-132), the
+    reference's moment-matching atom guess, on a seeded single-atom residual,
+    2D anisotropic, with t = 1 and t = 0.5.  Isotropic atoms cannot run: the
+    reference's projection of them raises (NewtonBases2D.__to_aniso indexes
+    column 1 of an (N, 1) array)."""
+    spec = importlib.util.spec_from_file_location("ref_KL_GaussRadon",
+                                                  os.path.join(root, "KL_GaussRadon.py"))
+    kl = importlib.util.module_from_spec(spec)
+    sys.modules["ref_KL_GaussRadon"] = kl
+    spec.loader.exec_module(kl)
+    nb2, mgr = mods["NewtonBases2D"], mods["manager"]
+    rng = np.random.default_rng(23)
+    T, w, p = geom_2d(24, 48)
+    tomo = Tomo(nb2, T, w, p)
+    space = NS(detector=p, ortho=w, orientations=T)
+    # the data: one anisotropic atom and small noise (negative cells included)
+    I, x, r = atoms_2d(rng, 1, r_lo=2.5, r_hi=3.5, x_half=0.3)
+    data = f32grid(tomo(Atoms(2, False, I, x, r)).asarray() +
+                   rng.normal(0, 0.01, tomo.shape))
+    put(out, "kl", T=T, w0=w[0], p0=p[0], data=data)
+    n = 0
+    with mgr.myManager(device="cpu", fType="float64"):
+        for iso, t in ((False, 1.0), (False, 0.5)):
+            t0 = time.time()
+            # the atom passed in: its projection is added back to the residual
+            # (res = data - R(atom)), so the guess sees the data itself
+            a_in = Atoms(2, iso, [0.7], [[0.1, -0.2]], [[3.0]] if iso else [[3.0, 2.5, 0.4]])
+            res = (data - tomo(a_in).asarray()).view(SinoS)
+            res.space = space
+            got = kl.doKL_ProjGDStep_iso(res, a_in, t, tomo)
+            put(out, "kl%d" % n, iso=np.array(iso), t=np.array(t), I=got.I, x=got.x, r=got.r)
+            print("  KL guess iso=%s t=%.1f: %.1f s" % (iso, t, time.time() - t0))
+            n += 1
+    out["kl_n"] = np.array(n)
+
+
 def main(root):
     mods = load_reference(root)
     out = {}
@@ -391,6 +438,7 @@ def main(root):
     I, x, r = atoms_3d(rng, 3)
     volproj_set(mods, out, "vol3d", "NewtonBases", 3, I, x, r, 7)
     fit_sets(mods, out)
+    kl_set(mods, out, root)
     dst = os.path.join(HERE, "reference_kernels.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst, len(out), "arrays in %.0f s" % (time.time() - t0))

@@ -137,3 +137,37 @@ def test_gd_block_corrected_rule_departs_from_reference_slicing(z):
                                   z["fit_data"], list(z[key + "_max_iter"]), dim_str="xI")
     n = min(E.size, z[key + "_E"].size)
     assert rel(E[:n], z[key + "_E"][:n]) > 1e-8
+
+
+def _kl_geom(z):
+    return go.Geometry(2, z["kl_T"], z["kl_w0"], z["kl_p0"])
+
+
+def test_kl_guess_oracle_matches_reference(z):
+    """KL_GaussRadon.doKL_ProjGDStep_iso (KL_GaussRadon.py:57-132) run by the
+    reference: the oracle's restatement of its rule gives the same atom."""
+    from oracle import kl_init_oracle as ko
+    assert int(z["kl_n"]) >= 2
+    for i in range(int(z["kl_n"])):
+        g = lambda k: z["kl%d_%s" % (i, k)]
+        I, x, r = ko.reference_guess(z["kl_data"], _kl_geom(z), 2, bool(g("iso")), float(g("t")))
+        assert rel(I, g("I")[0]) <= TOL
+        assert rel(x, g("x")[0]) <= TOL
+        assert rel(r, g("r")[0]) <= TOL
+
+
+def test_kl_guess_departs_only_in_width_rule(z):
+    """Where the engine's guess departs from the reference's, on the t = 1
+    golden (the blend weight that makes the moments those of the data): the
+    centre and the spread S are the reference's; the widths follow the
+    kernels' basis, r = 1/(sqrt(60) S) instead of 1/S, with the 2D
+    off-diagonal 0 instead of the start value 10 the reference leaves; the
+    intensity, matched to the mass of R(atom), follows the widths."""
+    from oracle import kl_init_oracle as ko
+    i = [k for k in range(int(z["kl_n"])) if float(z["kl%d_t" % k]) == 1.0][0]
+    g = lambda k: z["kl%d_%s" % (i, k)]
+    I, x, r = ko.moment_fit(z["kl_data"], _kl_geom(z), 2, False, 1.0)
+    assert rel(x, g("x")[0]) <= TOL
+    assert rel(np.sqrt(60.0) * r[:2], g("r")[0][:2]) <= TOL
+    assert r[2] == 0.0 and g("r")[0][2] == 10.0
+    assert rel(I, g("I")[0]) > 0.5
