@@ -9,12 +9,13 @@ one damped-Newton iteration
   gr_atom_derivs(all atoms)      -> gradient and Hessian blocks
   gr_newton_solve                -> trial parameters (FP64 block solves)
   gr_fit_forward(trial atoms)    -> trial fit fields, trial loss
-  gr_newton_accept_fields        -> device-side accept/reject, damping update,
-                                    loss history; an accepted trial's fields
-                                    become current (one launch)
+  gr_newton_accept               -> device-side accept/reject, damping update,
+                                    loss history
 
 (one projection per iteration: the current atoms' fields come from the
-prologue's gr_fit_forward, an accepted trial, or stay after a rejection)
+prologue's gr_fit_forward or an accepted trial; the derivatives read them
+only right after one of those, while they are still in the trial buffers,
+so they are never copied)
 
 is captured once into the body of a device-resident loop (engine.FitLoop: a
 CUDA graph whose WHILE node repeats the iteration until a device-side stop
@@ -48,6 +49,7 @@ eager host-driven loop, one host sync per iteration.
 """
 import collections
 import contextlib
+import math
 import time
 
 import numpy as np
@@ -149,7 +151,10 @@ def validate_request(req):
         shape = (A,) + tuple(v.size for v in det)
         if tuple(d.shape) != shape and d.numel() != int(np.prod(shape)):
             raise ValueError("request %s: data must have shape %s" % (req.id, shape))
-        if not bool(torch.isfinite(d).all()):
+        # one summing pass (about 25x cheaper than an elementwise test): a
+        # NaN or Inf anywhere makes the sum NaN or Inf; only a finite sum
+        # that overflowed needs the elementwise test
+        if not math.isfinite(float(d.sum())) and not bool(torch.isfinite(d).all()):
             raise ValueError("request %s: data holds NaN or Inf" % req.id)
     elif req.make_data is None:
         raise ValueError("request %s: no data (data_host or make_data)" % req.id)
@@ -180,10 +185,24 @@ def _layout(items):
     return out, max(off, _ALIGN)
 
 
-def _view(buf, spec):
-    """Typed view of a uint8 torch buffer (device or host)."""
-    off, dt, shape, nb = spec
-    return buf[off:off + nb].view(_TORCH_DTYPE[dt]).view(shape)
+def _typed_views(buf):
+    """View maker for a uint8 torch buffer (device or host) whose size is a
+    multiple of 8 bytes: the buffer is reinterpreted once per element type,
+    and each (offset, dtype, shape) of a _layout becomes one strided view
+    of it (admission makes some thirty views per request)."""
+    typed = {}
+
+    def view(spec):
+        off, dt, shape, _nb = spec
+        t = typed.get(dt)
+        if t is None:
+            t = typed[dt] = buf.view(_TORCH_DTYPE[dt])
+        strides, k = [], 1
+        for v in reversed(shape):
+            strides.append(k)
+            k *= v
+        return t.as_strided(shape, tuple(reversed(strides)), off // dt.itemsize)
+    return view
 
 
 def _host_view(arr, spec):
@@ -269,7 +288,8 @@ class _Slot:
         self.arena_in = torch.empty(n_in, dtype=torch.uint8, device=device)
         with torch.cuda.stream(setup):
             self.arena_in.copy_(self.staging[:n_in], non_blocking=True)
-        v = lambda name: _view(self.arena_in, lay[name])
+        vin = _typed_views(self.arena_in)
+        v = lambda name: vin(lay[name])
         self.geom = DeviceGeometry.bound(rec, kdet, det_h, v("frames"),
                                          [v("det%d" % k) for k in range(kdet)], device)
         self.cur = engine.DeviceAtoms.wrap(v("I"), v("x"), v("r"))
@@ -293,7 +313,8 @@ class _Slot:
                               ("H", np.float64, (n, P, P)), ("step", np.float64, (n,)),
                               ("ws_p", np.uint8, (ws_p,)), ("ws_d", np.uint8, (ws_d,))])
         self.arena_work = torch.empty(n_work, dtype=torch.uint8, device=device)
-        w = lambda name: _view(self.arena_work, wl[name])
+        vwork = _typed_views(self.arena_work)
+        w = lambda name: vwork(wl[name])
         self.data = w("data")
         with torch.cuda.stream(setup):
             if req.data_host is not None:
@@ -312,7 +333,8 @@ class _Slot:
                                           ("loss", np.float64, (1,)),
                                           ("loss0", np.float64, (1,))])
         self.results = _pinned_take(n_res)
-        r = lambda name: _view(self.results, self.res_layout[name])
+        vres = _typed_views(self.results)
+        r = lambda name: vres(self.res_layout[name])
         self.h_hist, self.h_acc, self.h_counter = r("hist"), r("acc"), r("counter")
         self.h_theta, self.h_loss, self.h_loss0 = r("theta"), r("loss"), r("loss0")
         t_bufs = time.perf_counter()
@@ -373,13 +395,23 @@ class _Slot:
                 _pinned_give(b)
         self.staging = self.results = None
 
+    def _current_fields(self, device_loop):
+        """Where the current atoms' fit fields live.  In the device loop they
+        stay in the trial buffers: the derivatives, their only reader, run
+        only right after an accepted trial (or on the first iteration, after
+        the prologue), when the trial buffers hold exactly the current
+        atoms' fields, so an accepted trial's fields need no copy.  The
+        iteration replayed from the host recomputes the derivatives every
+        time and keeps a separate copy."""
+        return (self.alpha_t, self.beta_t) if device_loop else (self.alpha, self.beta)
+
     def prologue(self):
         """Fit fields and loss of the starting atoms (once per fit); the
         starting loss is also copied out (the fit's initial loss)."""
         r = self.req
+        alpha, beta = self._current_fields(self.loop is not None)
         engine.fit_forward_into(self.cur, self.geom, self.data, r.fit, r.background, None,
-                                self.alpha, self.beta, self.loss_cur, self.ws_p,
-                                plan=self.plan_p)
+                                alpha, beta, self.loss_cur, self.ws_p, plan=self.plan_p)
         self.h_loss0.copy_(self.loss_cur.reshape(1), non_blocking=True)
 
     def iterate(self, loop=None):
@@ -390,8 +422,9 @@ class _Slot:
         trial: the atoms did not move, so g and H still hold their values."""
         r = self.req
         beta_c = 1.0 if r.fit == "l2" else 0.0
+        alpha, beta = self._current_fields(loop is not None)
         with (loop.unless_rejected() if loop is not None else contextlib.nullcontext()):
-            engine.atom_derivs_into(self.cur, self.geom, "field", self.alpha, self.beta, beta_c,
+            engine.atom_derivs_into(self.cur, self.geom, "field", alpha, beta, beta_c,
                                     2, self.f, self.g, self.H, self.ws_d, plan=self.plan_d)
         engine.newton_solve_into(self.dim, self.iso, self.g, self.H, self.lam, self.theta,
                                  self.theta_trial, self.step, self.trial, self.dev)
@@ -402,7 +435,8 @@ class _Slot:
                                   self.theta, self.theta_trial, self.lam, 1e-4, r.lam_max,
                                   self.cur, self.trial, self.hist, self.hist_acc,
                                   self.counter, self.dev,
-                                  fields=(self.alpha_t, self.alpha, self.beta_t, self.beta))
+                                  fields=None if loop is not None else
+                                  (self.alpha_t, self.alpha, self.beta_t, self.beta))
 
     def _copy_back(self):
         self.h_counter.copy_(self.counter, non_blocking=True)
@@ -586,11 +620,22 @@ class GaussFitServer:
             return                      # retry only after a fit has finished
         if self.largest_first and len(self.pending) > 1:
             # among the requests that have arrived, the largest go first, so
-            # the longest fits start early (arrival order otherwise kept)
+            # the longest fits start early (arrival order otherwise kept);
+            # "both ends": largest and smallest alternately, so the small
+            # fits, whose time is mostly their host set-up and launch
+            # latency, run beside the large ones instead of after them
             arrived = [r for r in self.pending if r.arrival <= now]
             if len(arrived) > 1:
                 later = [r for r in self.pending if r.arrival > now]
                 arrived.sort(key=lambda r: -(r.size_hint[0] * r.size_hint[1]))
+                if self.largest_first == "both_ends":
+                    lo, hi, mixed = 0, len(arrived) - 1, []
+                    while lo <= hi:
+                        mixed.append(arrived[lo])
+                        if hi > lo:
+                            mixed.append(arrived[hi])
+                        lo, hi = lo + 1, hi - 1
+                    arrived = mixed
                 self.pending = collections.deque(arrived + later)
         while self.pending and len(self.active) < self.max_slots:
             req = self.pending[0]

@@ -41,8 +41,9 @@ def test_device_and_host_views_agree_and_do_not_alias():
     buf = torch.zeros(total, dtype=torch.uint8)
     arr = buf.numpy()                       # the same memory, seen from numpy
     rng = np.random.default_rng(0)
+    view = serving._typed_views(buf)
     for name, dt, shape in _items():
-        v = serving._view(buf, spec[name])
+        v = view(spec[name])
         assert tuple(v.shape) == tuple(shape)
         vals = rng.integers(0, 100, size=shape).astype(dt)
         v.copy_(torch.from_numpy(np.array(vals)))  # keeps 0-d shapes
@@ -51,7 +52,7 @@ def test_device_and_host_views_agree_and_do_not_alias():
     for name, dt, shape in _items():
         vals = rng.integers(0, 100, size=shape).astype(dt)
         assert np.array_equal(serving._host_view(arr, spec[name]), vals), name
-        assert np.array_equal(serving._view(buf, spec[name]).numpy(), vals), name
+        assert np.array_equal(view(spec[name]).numpy(), vals), name
 
 
 def test_fit_step_packing_is_aligned_and_disjoint():
