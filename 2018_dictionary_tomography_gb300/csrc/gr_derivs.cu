@@ -124,7 +124,8 @@ struct PairMoments {
   float X0, Y0;  // sum E*C and sum E^2 (per-atom L2 value)
 };
 
-template <int K, int DEG, bool GN>
+// CH: cells per chunk of the row walk (loaded together before any is used)
+template <int K, int DEG, bool GN, int CH>
 __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
                                              const DerivIn &in, int a, float I,
                                              PairMoments<K, DEG, GN> &mo, int phase = 0,
@@ -159,17 +160,17 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
     // values and coordinates are loaded together first (one cell per load
     // round trip would leave the lane waiting on every cell)
     const int c_hi = p.hi[0];
-    for (int kb = p.lo[0] + phase * kRowChunk; kb <= c_hi; kb += rs * kRowChunk) {
-      float cv[kRowChunk], pv[kRowChunk], bv[GN ? kRowChunk : 1];
+    for (int kb = p.lo[0] + phase * CH; kb <= c_hi; kb += rs * CH) {
+      float cv[CH], pv[CH], bv[GN ? CH : 1];
 #pragma unroll
-      for (int i = 0; i < kRowChunk; ++i) {
+      for (int i = 0; i < CH; ++i) {
         const int k0 = min(kb + i, c_hi);
         cv[i] = __ldg(field + abase + k0);
         pv[i] = __ldg(g.ax[0].coords + k0);
-        if (GN) bv[i] = bfield ? __ldg(bfield + abase + k0) : in.beta_const;
+        if (GN) bv[i] = bfield ? __ldg(bfield + abase + k0) : 0.f;
       }
 #pragma unroll
-      for (int i = 0; i < kRowChunk; ++i) {
+      for (int i = 0; i < CH; ++i) {
         if (kb + i > c_hi) break;
         const float d0 = (pv[i] - p.qh[0]) - p.ql[0];
         const float m = p.G[0] * d0 * d0;
@@ -177,19 +178,21 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
           const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
           const float c = cv[i];
           const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
-          float w = al * E;
+          // powers of d0, shared by both moment sets: one FMA per moment
+          float pw[NM];
+          pw[0] = 1.f;
 #pragma unroll
-          for (int q = 0; q < NM; ++q) {
-            mo.Ma[q] += w;
-            w *= d0;
-          }
+          for (int q = 1; q < NM; ++q) pw[q] = pw[q - 1] * d0;
+          const float w = al * E;
+          mo.Ma[0] += w;
+#pragma unroll
+          for (int q = 1; q < NM; ++q) mo.Ma[q] = fmaf(w, pw[q], mo.Ma[q]);
           if (GN) {
-            float wb = bv[i] * E * E;
+            // a constant beta scales the moments once per pair instead
+            const float wb = bfield ? bv[i] * (E * E) : E * E;
+            mo.Mb[0] += wb;
 #pragma unroll
-            for (int q = 0; q < NM; ++q) {
-              mo.Mb[q] += wb;
-              wb *= d0;
-            }
+            for (int q = 1; q < NM; ++q) mo.Mb[q] = fmaf(wb, pw[q], mo.Mb[q]);
           }
           if (in.mode == kModeL2Atom) {
             mo.X0 = fmaf(E, c, mo.X0);
@@ -217,20 +220,20 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
         const float rlo = ceilf(rc - rh), rhi = floorf(rc + rh);
         const int c_lo = (int)fminf(fmaxf(rlo, (float)p.lo[1]), (float)p.hi[1] + 1.f);
         const int c_hi = (int)fmaxf(fminf(rhi, (float)p.hi[1]), (float)p.lo[1] - 1.f);
-        // the row is walked in chunks of kRowChunk3 cells whose field values
-        // and coordinates are loaded together first, so the loads overlap
+        // the row is walked in chunks of CH cells whose field values and
+        // coordinates are loaded together first, so the loads overlap
         // instead of each cell waiting for its own
-        for (int kb = c_lo; kb <= c_hi; kb += kRowChunk3) {
-          float cv[kRowChunk3], pv[kRowChunk3], bv[GN ? kRowChunk3 : 1];
+        for (int kb = c_lo; kb <= c_hi; kb += CH) {
+          float cv[CH], pv[CH], bv[GN ? CH : 1];
 #pragma unroll
-          for (int i = 0; i < kRowChunk3; ++i) {
+          for (int i = 0; i < CH; ++i) {
             const int k1 = min(kb + i, c_hi);
             cv[i] = __ldg(field + rbase + k1);
             pv[i] = __ldg(g.ax[1].coords + k1);
-            if (GN) bv[i] = bfield ? __ldg(bfield + rbase + k1) : in.beta_const;
+            if (GN) bv[i] = bfield ? __ldg(bfield + rbase + k1) : 0.f;
           }
 #pragma unroll
-          for (int i = 0; i < kRowChunk3; ++i) {
+          for (int i = 0; i < CH; ++i) {
             if (kb + i > c_hi) break;
             const float d1 = (pv[i] - p.qh[1]) - p.ql[1];
             const float m = fmaf(d1, fmaf(p.G[2], d1, u), t0);
@@ -238,19 +241,19 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
               const float E = ex2_approx(fmaf(m, kNegThirtyLog2e, l2n));
               const float c = cv[i];
               const float al = (in.mode == kModeL2Atom) ? fmaf(I, E, -c) : c;
-              float w = al * E;
+              float pw[DEG + 1];
+              pw[0] = 1.f;
 #pragma unroll
-              for (int q = 0; q <= DEG; ++q) {
-                Sa[q] += w;
-                w *= d1;
-              }
+              for (int q = 1; q <= DEG; ++q) pw[q] = pw[q - 1] * d1;
+              const float w = al * E;
+              Sa[0] += w;
+#pragma unroll
+              for (int q = 1; q <= DEG; ++q) Sa[q] = fmaf(w, pw[q], Sa[q]);
               if (GN) {
-                float wb = bv[i] * E * E;
+                const float wb = bfield ? bv[i] * (E * E) : E * E;
+                Sb[0] += wb;
 #pragma unroll
-                for (int q = 0; q <= DEG; ++q) {
-                  Sb[q] += wb;
-                  wb *= d1;
-                }
+                for (int q = 1; q <= DEG; ++q) Sb[q] = fmaf(wb, pw[q], Sb[q]);
               }
               if (in.mode == kModeL2Atom) {
                 mo.X0 = fmaf(E, c, mo.X0);
@@ -272,6 +275,10 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
       }
     }
   }
+  if (GN && !bfield) {
+#pragma unroll
+    for (int q = 0; q < NM; ++q) mo.Mb[q] *= in.beta_const;
+  }
 }
 
 // ONE: the work split gives every lane at most one angle of its atom (every
@@ -280,7 +287,12 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
 // accumulators need not live across the whole pair computation, which cuts
 // the Hessian kernel from 255 to 168 registers (3 resident blocks per SM
 // instead of 2).
-template <int K, int ORDER, bool ONE>
+// WIDE (3D Hessians): rows walked in chunks of 8 cells instead of 4, which
+// keeps more field loads in flight when supports are many cells wide and
+// costs idle lanes on narrow ones (Tuning key 8; measured: 2936 atoms x 148
+// angles of 493^2 cells 460 -> 408 us, config 2's atoms 192 -> 200 us; 16
+// instead of 8 cells slowed every 2D Hessian measured, by up to 25 %)
+template <int K, int ORDER, bool ONE, bool WIDE = false>
 __global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS
                                            : (ONE ? (K == 1 ? GR_HESS2D_MIN_BLOCKS : 3) : 1))
     gr_deriv_kernel(Atoms at, Geom g, DerivIn in, DerivCfg cfg, float *part) {
@@ -324,7 +336,9 @@ __global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS
     Pair<K> p;
     pair_setup<K>(at, jj, fr, g, p);
     PairMoments<K, DEG, GN> mo;
-    pair_moments<K, DEG, GN>(p, g, in, a, I, mo, phase, cfg.rs);
+    static_assert(!WIDE || K == 2, "wide rows: 3D Hessians only");
+    constexpr int CH = K == 1 ? kRowChunk : (WIDE ? 2 * kRowChunk3 : kRowChunk3);
+    pair_moments<K, DEG, GN, CH>(p, g, in, a, I, mo, phase, cfg.rs);
     for (int o = 1; o < cfg.rs; o <<= 1) {
 #pragma unroll
       for (int q = 0; q < n_mom<K, DEG>(); ++q) {
@@ -739,6 +753,10 @@ int tuning_set(Tuning &t, int key, int value) {
     t.deriv_one_mb = value;
     return kOk;
   }
+  if (key == 8 && (value == 0 || value == 1)) {
+    t.deriv_wide_rows = value;
+    return kOk;
+  }
   return kErrArg;
 }
 
@@ -746,7 +764,8 @@ int tuning_get(const Tuning &t, int key) {
   return key == 0 ? t.deriv_target_warps : key == 1 ? t.deriv_min_angles
          : key == 2 ? t.deriv_atoms_per_warp : key == 3 ? t.proj_form
          : key == 4 ? t.proj_split_cells
-         : key == 6 ? t.deriv_split_lanes : key == 7 ? t.deriv_one_mb : -1;
+         : key == 6 ? t.deriv_split_lanes : key == 7 ? t.deriv_one_mb
+         : key == 8 ? t.deriv_wide_rows : -1;
 }
 
 size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order, const Tuning &t) {
@@ -797,6 +816,7 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
     // at most one angle per lane: a lane's angles a_lo + sub + k sg lie
     // below a_lo + ch
     const bool one = c.ch <= c.sg / c.rs;
+    const bool wide = t.deriv_wide_rows != 0;
     if (K == 1) {
       if (in.order == 1) {
         if (one) gr_deriv_kernel<1, 1, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
@@ -809,6 +829,9 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
       if (in.order == 1) {
         if (one) gr_deriv_kernel<2, 1, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
         else gr_deriv_kernel<2, 1, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+      } else if (wide) {
+        if (one) gr_deriv_kernel<2, 2, true, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+        else gr_deriv_kernel<2, 2, false, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
       } else {
         if (one) gr_deriv_kernel<2, 2, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
         else gr_deriv_kernel<2, 2, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
@@ -832,6 +855,8 @@ int preload_derivs() {
          preload_fn(gr_deriv_kernel<2, 1, false>) + preload_fn(gr_deriv_kernel<2, 2, false>) +
          preload_fn(gr_deriv_kernel<1, 1, true>) + preload_fn(gr_deriv_kernel<1, 2, true>) +
          preload_fn(gr_deriv_kernel<2, 1, true>) + preload_fn(gr_deriv_kernel<2, 2, true>) +
+         preload_fn(gr_deriv_kernel<2, 2, false, true>) +
+         preload_fn(gr_deriv_kernel<2, 2, true, true>) +
          preload_fn(gr_psf_deriv_kernel<1, 1>) + preload_fn(gr_psf_deriv_kernel<1, 2>) +
          preload_fn(gr_psf_deriv_kernel<2, 1>) + preload_fn(gr_psf_deriv_kernel<2, 2>) +
          preload_fn(gr_deriv_finalize_kernel<1>) + preload_fn(gr_deriv_finalize_kernel<2>) +

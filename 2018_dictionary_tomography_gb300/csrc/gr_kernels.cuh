@@ -76,6 +76,7 @@ struct Tuning {
   int proj_split_cells = 4 << 20;   // key 4
   int deriv_split_lanes = 65536;    // key 6
   int deriv_one_mb = 1024;          // key 7
+  int deriv_wide_rows = 0;          // key 8 (1: 3D Hessian rows in 8-cell chunks)
 };
 extern Tuning g_tuning;
 int tuning_set(Tuning &t, int key, int value);

@@ -290,7 +290,11 @@ unsigned long long gr_launch_count(void);
  * pairs x lanes <= value; default 65536; 0 = never).  GR_TUNE_DERIV_ONE_MB:
  * take enough angle chunks that every lane has at most one angle whenever the
  * chunk partials then fit in this many MB of workspace (default 1024; 0 =
- * keep GR_TUNE_DERIV_WARPS).  Set them before
+ * keep GR_TUNE_DERIV_WARPS).  GR_TUNE_DERIV_WIDE_ROWS: 1 walks the rows of
+ * the 3D Hessian (order 2) kernels in chunks of 8 cells instead of 4, which
+ * keeps more field loads in flight when supports are many cells wide and
+ * idles lanes when they are narrow (default 0; the serving tuner picks it
+ * per class of requests).  Set them before
  * gr_workspace_bytes and keep them fixed while launches that used the old
  * values are in flight.  Results do not depend on them beyond FP rounding of
  * the derivative chunk and lane sums and of a split tile's combined cell sums (the
@@ -305,7 +309,8 @@ enum {
   GR_TUNE_PROJ_TILING = 3,
   GR_TUNE_PROJ_SPLIT_CELLS = 4,
   GR_TUNE_DERIV_SPLIT_LANES = 6,
-  GR_TUNE_DERIV_ONE_MB = 7
+  GR_TUNE_DERIV_ONE_MB = 7,
+  GR_TUNE_DERIV_WIDE_ROWS = 8
 };
 int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);

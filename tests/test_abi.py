@@ -117,8 +117,12 @@ def test_plan_create_set_get_without_gpu():
     assert lib.gr_plan_create(2, ctypes.byref(at), ctypes.byref(g), ctypes.byref(h)) == 0
     assert h.value
     # a copy of the process-wide values, then independent of them
-    for key in (0, 1, 2, 3, 4, 6, 7):
+    for key in (0, 1, 2, 3, 4, 6, 7, 8):
         assert lib.gr_plan_get(h, key) == lib.gr_get_tuning(key)
+    # the wide-row Hessian walk is a switch (0 or 1)
+    assert lib.gr_plan_set(h, 8, 1) == 0 and lib.gr_plan_get(h, 8) == 1
+    assert lib.gr_plan_set(h, 8, 2) == -1 and lib.gr_get_tuning(8) == 0
+    assert lib.gr_plan_set(h, 8, 0) == 0
     assert lib.gr_plan_set(h, 3, 2) == 0 and lib.gr_plan_get(h, 3) == 2
     assert lib.gr_get_tuning(3) == 1
     assert lib.gr_plan_set(h, 3, 5) == -1 and lib.gr_plan_set(h, 5, 1) == -1

@@ -258,3 +258,28 @@ def test_projection_split_over_warps(eng, cuda_ready):
     lo = 0.5 * float(np.sum((Ro - d32) ** 2))
     for key, (_R, loss) in outs.items():
         assert abs(loss - lo) <= TOL * lo, key
+
+
+@pytest.mark.parametrize("case", ["2p5d", "3d"])
+def test_wide_row_hessian_walk_matches_oracle(eng, cuda_ready, case):
+    """The 3D Hessian kernel's wide-row variant (plan key 8: rows walked in
+    8-cell chunks) against the oracle, on atoms whose supports span 5-10
+    cells per row, and against the default walk (the cells of a row are
+    summed in the same order: equal up to contraction choices)."""
+    lib = __import__("importlib").import_module("2018_dictionary_tomography_gb300._lib")
+    c = CASES[case]
+    g = make_geometry(c["kind"], c["A"], c["D0"], c.get("D1"))
+    I, x, r = make_atoms(c["dim"], c["N"], 11, rdiag=(2.0, 4.0), roff=0.5)
+    rng = np.random.default_rng(12)
+    data = (go.radproj(I * 0.9, x + 0.01, r, g) + rng.normal(0, 0.01, g.shape))
+    data = data.astype(np.float32).astype(np.float64)
+    atoms, geom = engine_atoms(I, x, r), engine_geometry(g)
+    d = torch.from_numpy(data).float().cuda()
+    fw = eng.fit_forward(atoms, geom, d, "l2", 0.0)
+    plan = eng.Plan(lib.GR_OP_DERIVS_2, atoms, geom).set(8, 1)
+    _f, gw, Hw = eng.atom_derivs(atoms, geom, "field", fw["alpha"], None, 1.0, 2, plan=plan)
+    _f, gd, Hd = eng.atom_derivs(atoms, geom, "field", fw["alpha"], None, 1.0, 2)
+    _fo, go_, Ho = go.all_atom_derivs("l2fit", I, x, r, g, data, 2)
+    assert entry_relerr(gw.cpu().numpy(), go_) < TOL
+    assert entry_relerr(Hw.cpu().numpy(), Ho) < TOL
+    assert entry_relerr(Hw.cpu().numpy(), Hd.cpu().numpy()) < 1e-6
