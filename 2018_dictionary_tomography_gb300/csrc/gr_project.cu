@@ -30,27 +30,43 @@ __global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
                                                      int W, float4 *pairs) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int a = blockIdx.y;
-  if (j >= at.n) return;
-  Frame<K> f;
-  load_frame<K>(g.frames, a, f);
-  Pair<K> p;
-  pair_setup<K>(at, j, f, g, p);
-  if constexpr (K == 1) {
-    if (pairs) {
-      float4 *rec = pairs + ((size_t)a * at.n + j) * 2;
-      rec[0] = make_float4(p.qh[0], p.ql[0], p.G[0], p.l2amp);
-      rec[1] = make_float4(__int_as_float(p.lo[0]), __int_as_float(p.hi[0]), p.sgn, 0.f);
-    }
-  }
-  if (p.lo[0] > p.hi[0]) return;
   const uint32_t bit = 1u << (j & 31);
   const size_t base = (size_t)a * tc.ntiles;
   const int wj = j >> 5;
   if constexpr (K == 1) {
-    const int t_lo = p.lo[0] / tc.t0, t_hi = p.hi[0] / tc.t0;
-    for (int t = t_lo; t <= t_hi; ++t)
-      atomicOr(bitmap + (base + t) * W + wj, bit);
+    // a warp holds 32 consecutive atoms: one bitmap word per tile.  Their
+    // bits are merged per tile across the warp (one atomicOr per tile the
+    // warp touches, not one per atom and tile: the 32 atoms of a word would
+    // otherwise all hit the same address)
+    int t_lo = 1 << 30, t_hi = -1;
+    if (j < at.n) {
+      Frame<1> f;
+      load_frame<1>(g.frames, a, f);
+      Pair<1> p;
+      pair_setup<1>(at, j, f, g, p);
+      if (pairs) {
+        float4 *rec = pairs + ((size_t)a * at.n + j) * 2;
+        rec[0] = make_float4(p.qh[0], p.ql[0], p.G[0], p.l2amp);
+        rec[1] = make_float4(__int_as_float(p.lo[0]), __int_as_float(p.hi[0]), p.sgn, 0.f);
+      }
+      if (p.lo[0] <= p.hi[0]) {
+        t_lo = p.lo[0] / tc.t0;
+        t_hi = p.hi[0] / tc.t0;
+      }
+    }
+    const int w_lo = __reduce_min_sync(0xffffffffu, t_lo);
+    const int w_hi = __reduce_max_sync(0xffffffffu, t_hi);
+    for (int t = w_lo; t <= w_hi; ++t) {
+      const unsigned bits = __reduce_or_sync(0xffffffffu, (t >= t_lo && t <= t_hi) ? bit : 0u);
+      if ((threadIdx.x & 31) == 0 && bits) atomicOr(bitmap + (base + t) * W + wj, bits);
+    }
   } else {
+    if (j >= at.n) return;
+    Frame<K> f;
+    load_frame<K>(g.frames, a, f);
+    Pair<K> p;
+    pair_setup<K>(at, j, f, g, p);
+    if (p.lo[0] > p.hi[0]) return;
     if (p.lo[1] > p.hi[1]) return;
     const int r_lo = p.lo[0] / tc.t0, r_hi = p.hi[0] / tc.t0;
     const int c_lo = p.lo[1] / tc.t1, c_hi = p.hi[1] / tc.t1;
@@ -352,7 +368,11 @@ __global__ void __launch_bounds__(kProjWarps * 32)
 }
 
 // 2D sinograms: atom footprints are a few cells wide, so a block owns a tile
-// of 32 consecutive cells of one angle, one cell per lane of every warp.  The
+// of 32 CPL consecutive cells of one angle, CPL cells per lane of every warp
+// (lane l: cells l, l + 32, ...).  CPL = 2 (Tuning key 3, form 2) halves the
+// tiles an atom of a wide footprint touches, and with them the listing,
+// staging and binning per evaluated cell; narrow footprints leave more lanes
+// idle in it.  The
 // tile's atoms come from its bitmap in index order, in passes: a pass lists
 // as many whole bitmap words as fit in NW*32 entries (block-wide prefix sum
 // of the words' bit counts), every thread sets up the pair data of one listed
@@ -360,24 +380,35 @@ __global__ void __launch_bounds__(kProjWarps * 32)
 // contiguous slices of the pass's list to its lane's cell, in list order, in
 // registers (compensated).  The warps' partial sums are combined in warp
 // order: results depend only on the atoms listed, bitwise reproducible.
-template <bool KAHAN, int NW>
+// LM: a pass lists up to LM * NW * 32 atoms (each thread stages LM of them),
+// so tiles crossed by many atoms take fewer passes and barriers (2150 atoms x
+// 153 angles: 87.9 us with one atom per thread, 82.6 with two, 79.5 with
+// four; 512 atoms: 20.6, 20.7, 21.1 us)
+template <bool KAHAN, int NW, int CPL = 1, int LM = 1>
 __global__ void __launch_bounds__(NW * 32)
     gr_project1d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
                         int W, ProjOut out, double *loss_out, int *done,
                         const float4 *__restrict__ pairs) {
   constexpr int T = NW * 32;
-  __shared__ float4 prm[T][2];
-  __shared__ int list[T];
+  constexpr int LT = LM * T;
+  __shared__ float4 prm[LT][2];
+  __shared__ int list[LT];
   __shared__ int wsum[NW];
-  __shared__ float parts[NW][2][32];
+  __shared__ float parts[NW][2][32 * CPL];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int item = blockIdx.x;
   const int a = item / tc.ntiles, t = item - a * tc.ntiles;
   const int D0 = g.ax[0].n;
-  const int cell = t * tc.t0 + lane;
-  const float pc = cell < D0 ? g.ax[0].coords[cell] : 0.f;
+  int cell[CPL];
+  float pc[CPL], acc[CPL], cmp[CPL];
+#pragma unroll
+  for (int k = 0; k < CPL; ++k) {
+    cell[k] = t * tc.t0 + lane + 32 * k;
+    pc[k] = cell[k] < D0 ? g.ax[0].coords[cell[k]] : 0.f;
+    acc[k] = 0.f;
+    cmp[k] = 0.f;
+  }
   const float4 *apairs = pairs + (size_t)a * at.n * 2;
-  float acc = 0.f, cmp = 0.f;
 
   const uint32_t *words = bitmap + (size_t)item * W;
   for (int wb = 0; wb < W;) {
@@ -397,8 +428,8 @@ __global__ void __launch_bounds__(NW * 32)
     for (int w = 0; w < NW; ++w)
       if (w < warp) incl += wsum[w];
     // the words that fit form a prefix (incl never decreases); one word
-    // always fits (a word holds at most 32 <= T atoms)
-    const bool take = incl <= T;
+    // always fits (a word holds at most 32 <= LT atoms)
+    const bool take = incl <= LT;
     const int pos = incl - cnt;
     if (take)
       for (int p = pos; wd; ++p) {
@@ -413,11 +444,11 @@ __global__ void __launch_bounds__(NW * 32)
     total = wsum[0];
     wb += ntake > 0 ? ntake : W;   // ntake = 0 only past the last word
     // pair data of the listed atoms (set up once per pair by the binning
-    // launch), one per thread
-    if ((int)threadIdx.x < total) {
-      const float4 *rec = apairs + (size_t)list[threadIdx.x] * 2;
-      prm[threadIdx.x][0] = __ldg(rec);
-      prm[threadIdx.x][1] = __ldg(rec + 1);
+    // launch), up to LM per thread
+    for (int e = threadIdx.x; e < total; e += T) {
+      const float4 *rec = apairs + (size_t)list[e] * 2;
+      prm[e][0] = __ldg(rec);
+      prm[e][1] = __ldg(rec + 1);
     }
     __syncthreads();
     // warp w: slice [w total / NW, (w + 1) total / NW) in list order
@@ -427,57 +458,67 @@ __global__ void __launch_bounds__(NW * 32)
       const float4 q0 = prm[s2][0];
       const float4 q1 = prm[s2][1];
       const int lo = __float_as_int(q1.x), hi = __float_as_int(q1.y);
-      if (cell >= lo && cell <= hi) {
-        const float d = (pc - q0.x) - q0.y;
-        const float m = q0.z * d * d;
-        if (m <= 1.f) {
-          const float v = q1.z * ex2_approx(fmaf(m, kNegThirtyLog2e, q0.w));
-          if (KAHAN) {
-            const float tt = acc + v;
-            cmp += (fabsf(acc) >= fabsf(v)) ? ((acc - tt) + v) : ((v - tt) + acc);
-            acc = tt;
-          } else {
-            acc += v;
+#pragma unroll
+      for (int k = 0; k < CPL; ++k) {
+        if (cell[k] >= lo && cell[k] <= hi) {
+          const float d = (pc[k] - q0.x) - q0.y;
+          const float m = q0.z * d * d;
+          if (m <= 1.f) {
+            const float v = q1.z * ex2_approx(fmaf(m, kNegThirtyLog2e, q0.w));
+            if (KAHAN) {
+              const float tt = acc[k] + v;
+              cmp[k] += (fabsf(acc[k]) >= fabsf(v)) ? ((acc[k] - tt) + v) : ((v - tt) + acc[k]);
+              acc[k] = tt;
+            } else {
+              acc[k] += v;
+            }
           }
         }
       }
     }
     __syncthreads();  // list, prm and wsum are reused by the next pass
   }
-  parts[warp][0][lane] = acc;
-  parts[warp][1][lane] = cmp;
+#pragma unroll
+  for (int k = 0; k < CPL; ++k) {
+    parts[warp][0][lane + 32 * k] = acc[k];
+    parts[warp][1][lane + 32 * k] = cmp[k];
+  }
   __syncthreads();
   __shared__ int s_last;
   if (warp == 0) {
     // combine the warps' partial sums in warp order (compensated)
-    float s0 = 0.f, c0 = 0.f;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) {
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const float v = parts[w][h][lane];
-        const float tt = s0 + v;
-        c0 += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
-        s0 = tt;
-      }
-    }
-
     float l = 0.f;
-    if (cell < D0) {
-      const float v = s0 + c0;
-      const size_t gi = (size_t)a * D0 + cell;
-      if (out.R) out.R[gi] = v;
-      if (out.epilogue == kEpiL2) {
-        const float res = v - out.data[gi];
-        if (out.alpha) out.alpha[gi] = res;
-        l = 0.5f * res * res;
-      } else if (out.epilogue == kEpiKL) {
-        const float fo = out.data[gi];
-        const float gg = v + out.bg;
-        const float ig = 1.f / gg;
-        if (out.alpha) out.alpha[gi] = 1.f - fo * ig;
-        if (out.beta) out.beta[gi] = fo * ig * ig;
-        l = kl_term(fo, gg);
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+      float s0 = 0.f, c0 = 0.f;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const float v = parts[w][h][lane + 32 * k];
+          const float tt = s0 + v;
+          c0 += (fabsf(s0) >= fabsf(v)) ? ((s0 - tt) + v) : ((v - tt) + s0);
+          s0 = tt;
+        }
+      }
+      if (cell[k] < D0) {
+        const float v = s0 + c0;
+        const size_t gi = (size_t)a * D0 + cell[k];
+        float lk = 0.f;
+        if (out.R) out.R[gi] = v;
+        if (out.epilogue == kEpiL2) {
+          const float res = v - out.data[gi];
+          if (out.alpha) out.alpha[gi] = res;
+          lk = 0.5f * res * res;
+        } else if (out.epilogue == kEpiKL) {
+          const float fo = out.data[gi];
+          const float gg = v + out.bg;
+          const float ig = 1.f / gg;
+          if (out.alpha) out.alpha[gi] = 1.f - fo * ig;
+          if (out.beta) out.beta[gi] = fo * ig * ig;
+          lk = kl_term(fo, gg);
+        }
+        l += lk;
       }
     }
     if (out.loss_part) {
@@ -791,10 +832,11 @@ static void launch_project3d(size_t items, const Atoms &at, const Geom &g, const
       at, g, tc, bitmap, W, o, next_item, loss_out);
 }
 
+// rows: the tile's rows (3D) or cells (2D)
 TileCfg make_tiles(int K, int D0, int D1, int rows) {
   TileCfg tc;
   if (K == 1) {
-    tc.t0 = kTile1D;
+    tc.t0 = rows;
     tc.t1 = 1;
     tc.nt0 = (D0 + tc.t0 - 1) / tc.t0;
     tc.nt1 = 1;
@@ -811,7 +853,9 @@ TileCfg make_tiles(int K, int D0, int D1, int rows) {
 size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1,
                                const Tuning &t) {
   // sized for the smaller of the point-sampled and pixel-integrated tilings
-  const int rows = proj_rows(t.proj_form) < kTileDim0 ? proj_rows(t.proj_form) : kTileDim0;
+  const int rows = K == 1 ? kTile1D
+                          : (proj_rows(t.proj_form) < kTileDim0 ? proj_rows(t.proj_form)
+                                                                : kTileDim0);
   TileCfg tc = make_tiles(K, D0, D1, rows);
   const size_t W = (size_t)(n_atoms + 31) / 32;
   const size_t items = (size_t)n_angles * tc.ntiles;
@@ -832,7 +876,11 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   const int K = g.K;
   const int D0 = g.ax[0].n, D1 = K == 1 ? 1 : g.ax[1].n;
   const int form = t.proj_form;
-  TileCfg tc = make_tiles(K, D0, D1, (K == 2 && !o_in.psf) ? proj_rows(form) : kTileDim0);
+  // 2D: 64-cell tiles (two cells per lane) for form 2, else 32
+  const bool wide2d = K == 1 && !o_in.psf && form == 2;
+  TileCfg tc = make_tiles(K, D0, D1,
+                          K == 1 ? (wide2d ? 2 * kTile1D : kTile1D)
+                                 : (!o_in.psf ? proj_rows(form) : kTileDim0));
   const int W = (at.n + 31) / 32;
   const size_t items = (size_t)g.n_angles * tc.ntiles;
   const size_t need = project_workspace_bytes(K, at.n, g.n_angles, D0, D1, t);
@@ -882,8 +930,17 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
     // last block also sums the loss partials (no separate finalize launch)
     fused_loss = loss_out != nullptr && items <= kFusedLossItems;
     double *lo = fused_loss ? loss_out : nullptr;
-    if (W >= 8)  // 8 warps share a tile's atoms from 8 bitmap words (256 atoms) up
-      gr_project1d_kernel<true, 8><<<(unsigned)items, 8 * 32, 0, stream>>>(
+    if (wide2d && W >= 8)
+      gr_project1d_kernel<true, 8, 2, 2><<<(unsigned)items, 8 * 32, 0, stream>>>(
+          at, g, tc, bitmap, W, o, lo, next_item + 1, pairs);
+    else if (wide2d)
+      gr_project1d_kernel<true, kProjWarps, 2><<<(unsigned)items, kProjWarps * 32, 0, stream>>>(
+          at, g, tc, bitmap, W, o, lo, next_item + 1, pairs);
+    else if (W >= 32)  // 1024 atoms up: four list entries per thread
+      gr_project1d_kernel<true, 8, 1, 4><<<(unsigned)items, 8 * 32, 0, stream>>>(
+          at, g, tc, bitmap, W, o, lo, next_item + 1, pairs);
+    else if (W >= 8)  // 8 warps share a tile's atoms from 8 bitmap words (256 atoms) up
+      gr_project1d_kernel<true, 8, 1, 2><<<(unsigned)items, 8 * 32, 0, stream>>>(
           at, g, tc, bitmap, W, o, lo, next_item + 1, pairs);
     else
       gr_project1d_kernel<true, kProjWarps><<<(unsigned)items, kProjWarps * 32, 0, stream>>>(
@@ -927,8 +984,11 @@ int preload_project() {
          preload_fn(gr_project3d_kernel<16, 37, kProjWarps>) +
          preload_fn(gr_project3d_kernel<32, 34, 1>) +
          preload_fn(gr_project3d_kernel<32, 34, kProjWarps>) +
-         preload_fn(gr_project1d_kernel<true, 8>) +
+         preload_fn(gr_project1d_kernel<true, 8, 1, 4>) +
+         preload_fn(gr_project1d_kernel<true, 8, 1, 2>) +
          preload_fn(gr_project1d_kernel<true, kProjWarps>) +
+         preload_fn(gr_project1d_kernel<true, 8, 2, 2>) +
+         preload_fn(gr_project1d_kernel<true, kProjWarps, 2>) +
          preload_fn(gr_psf_project_kernel<1>) + preload_fn(gr_psf_project_kernel<2>) +
          preload_fn(gr_loss_finalize_kernel);
 }

@@ -32,9 +32,13 @@ checks that results alone and in the mix agree).
 Host-side care that keeps the loop from stalling behind fits in flight:
 buffers of a new request are built on a separate setup stream; finished
 loop graphs are destroyed only when no fit runs (destroying an executable
-graph waits for the device to idle); pinned host buffers are pooled.  Among
-requests that have arrived, the largest are admitted first, so the longest
-fits start early.  A request is admitted only onto a stream with no fit in
+graph waits for the device to idle); pinned host buffers are pooled.  Requests
+are admitted in arrival order (``largest_first`` admits the largest of
+those that have arrived first, or with "both_ends" the largest and the
+smallest alternately; on the 512-request stream submitted at once arrival
+order finished in 1.66 s, largest-first in 1.79 s and both-ends in 1.69 s:
+with the largest first, the small fits, whose time is mostly host set-up,
+are left to the end).  A request is admitted only onto a stream with no fit in
 flight (``exclusive_streams``): a stream runs its work in order, and a
 whole fit is one graph launch, so a request queued behind another on the
 same stream would wait for that entire fit however little work it has.
@@ -537,7 +541,7 @@ class GaussFitServer:
 
     def __init__(self, device=None, max_slots=32, n_streams=16, hbm_budget=None,
                  hbm_reserve=4 << 30, use_graphs=True, iters_per_launch=4, device_loop=True,
-                 largest_first=True, exclusive_streams=True, tuned=False):
+                 largest_first=False, exclusive_streams=True, tuned=False):
         self.dev = torch.device(device or "cuda")
         engine._require_cuda(self.dev)
         self.max_slots = max_slots
@@ -559,9 +563,12 @@ class GaussFitServer:
         self.admit_seconds = 0.0     # host time spent setting up admitted requests
         self.admit_phases = {}       # the same by phase (buffers, streams, capture)
         self.device_loops = 0        # requests run as one device-resident loop graph
-        # Finished requests' loop graphs are destroyed only when no fit runs:
-        # destroying an executable graph waits for the whole device to idle,
-        # which would stall the host loop behind every fit in flight.
+        # Finished requests' loop graphs are destroyed only when no fit runs
+        # and more requests are waiting to arrive (an idle moment of a
+        # running server), or by close(): destroying an executable graph
+        # waits for the whole device to idle, which would stall the host loop
+        # behind every fit in flight, and the last results should not wait
+        # for the clean-up of all the others.
         self._retired_loops = []
         # launches of each request run under the plans tuned for its shape
         # class (tune_classes), when there are any
@@ -715,6 +722,7 @@ class GaussFitServer:
                         self.cancelled.discard(slot.req.id)
                         res = {"status": "cancelled"}
                     res["arrival"] = slot.req.arrival
+                    res["admitted"] = slot.t_admit - t0
                     res["finish"] = time.perf_counter() - t0
                     res["latency"] = res["finish"] - slot.req.arrival
                     self.results[slot.req.id] = res
@@ -729,7 +737,7 @@ class GaussFitServer:
                     if on_done:
                         on_done(slot.req, res)
                     del slot
-                    if not self.active:
+                    if not self.active and self.pending:
                         self._release_loops()
                 else:
                     slot.launch()
@@ -740,8 +748,12 @@ class GaussFitServer:
                         time.sleep(min(wait, 0.01))
                 else:
                     time.sleep(20e-6)
-        self._release_loops()
         return self.results
+
+    def close(self):
+        """Destroy the loop graphs of the finished fits (waits for the device
+        to idle); the server can take more requests afterwards."""
+        self._release_loops()
 
     def _release_loops(self):
         """Destroy the retired loop graphs (nothing of this server runs)."""

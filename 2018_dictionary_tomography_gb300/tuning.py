@@ -142,8 +142,10 @@ def apply_for(atoms, geom, order, psf=False):
 _req_plans = {}
 # small candidate sets: a server tunes each new class once, on its first
 # request, and the fits of the class then run under the winners
-DERIV_CANDIDATES = ((131072, 1, 1, 0), (131072, 1, 1, 1), (32768, 1, 1, 0), (8192, 1, 1, 0),
-                    (131072, 2, 1, 0), (32768, 4, 1, 0))
+# (only the row-walk switch for the derivatives: splits into fewer warps won
+# alone on an idle GPU but lost among concurrent fits, 1.655 s against 1.624 s
+# untuned on the 512-request stream)
+DERIV_CANDIDATES = ((131072, 1, 1, 0), (131072, 1, 1, 1))
 PROJ_CANDIDATES = ((1, 4 << 20), (1, 0), (2, 4 << 20), (2, 0))
 
 

@@ -807,6 +807,7 @@ def run_serving(args):
     for r in warm:
         srv.submit(r)
     srv.run()
+    srv.close()
     serving.serve_plain(wl.config3_requests(n=2, rate=1e9, seed=98, atoms=(16, 64), det=(64, 96)), dev)
 
     # (1) saturation comparison on the same requests: served vs plain
@@ -828,12 +829,14 @@ def run_serving(args):
     for r in cmp_reqs:
         srv.submit(r)
     srv.run()
+    srv.close()
     t0 = time.perf_counter()
     srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31, tuned=True)
     for r in cmp_reqs:
         srv.submit(r)
     served_cmp = srv.run(t0=t0)
     t_served = time.perf_counter() - t0
+    srv.close()
     admit_cmp = srv.admit_seconds
     phases_cmp = dict(srv.admit_phases)
     loops_cmp = srv.device_loops
@@ -866,6 +869,7 @@ def run_serving(args):
     res = srv.run(t0=t0)
     makespan = time.perf_counter() - t0
     clocks = sampler.stop()
+    srv.close()
     lat = [v["latency"] for v in res.values()]
     its = [v["iterations"] for v in res.values()]
     fits_s = len(res) / makespan

@@ -283,3 +283,27 @@ def test_wide_row_hessian_walk_matches_oracle(eng, cuda_ready, case):
     assert entry_relerr(gw.cpu().numpy(), go_) < TOL
     assert entry_relerr(Hw.cpu().numpy(), Ho) < TOL
     assert entry_relerr(Hw.cpu().numpy(), Hd.cpu().numpy()) < 1e-6
+
+
+def test_2d_two_cells_per_lane_tiles_match_oracle(eng, cuda_ready):
+    """2D projection with 64-cell tiles (plan key 3 = 2: two cells per lane)
+    against the oracle, on wide and narrow footprints, and against the
+    32-cell tiles (the atoms a cell sums are the same; their grouping into
+    passes differs, so the sums agree to FP32 rounding)."""
+    lib = __import__("importlib").import_module("2018_dictionary_tomography_gb300._lib")
+    g = make_geometry("2d", 40, 300)
+    for rdiag in ((0.8, 2.0), (6.0, 12.0)):
+        I, x, r = make_atoms(2, 300, 13, rdiag=rdiag, roff=0.3)
+        rng = np.random.default_rng(14)
+        data = go.radproj(I * 0.9, x, r, g) + rng.normal(0, 0.01, g.shape)
+        data = data.astype(np.float32).astype(np.float64)
+        atoms, geom = engine_atoms(I, x, r), engine_geometry(g)
+        d = torch.from_numpy(data).float().cuda()
+        plan = eng.Plan(lib.GR_OP_PROJECT, atoms, geom).set(3, 2)
+        fw2 = eng.fit_forward(atoms, geom, d, "l2", 0.0, want_R=True, plan=plan)
+        fw1 = eng.fit_forward(atoms, geom, d, "l2", 0.0, want_R=True)
+        Ro = go.radproj(I, x, r, g)
+        assert relerr(fw2["R"].cpu().numpy(), Ro) < TOL
+        lo = go.l2_value(Ro, data)
+        assert abs(fw2["loss"].item() - lo) <= TOL * abs(lo)
+        assert relerr(fw2["R"].cpu().numpy(), fw1["R"].cpu().numpy()) < 1e-6

@@ -63,6 +63,11 @@ def test_admission_by_memory_budget_and_while_busy(cuda_ready):
     assert peak_bytes[0] <= budget
     assert peak[0] < 8
     assert srv.admitted_while_busy > 0
+    # the finished fits' loop graphs wait for close(), not for the results
+    assert srv._retired_loops
+    srv.close()
+    assert not srv._retired_loops
+    assert all(res[i]["admitted"] <= res[i]["finish"] for i in res)
 
 
 def test_served_fit_matches_plain_fit(cuda_ready):
