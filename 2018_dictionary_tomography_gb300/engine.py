@@ -490,10 +490,16 @@ class FitStep:
     is one graph launch.  ``run`` copies new inputs into the pinned buffers
     (when given), replays and waits; its results are views of the pinned
     output buffers, overwritten by the next run.
+
+    Large sinograms are fitted in ``chunks`` ranges of angles (default: one
+    per 128 MB of data, at most 8): a side stream copies range i+1 in while
+    the projection of range i runs, so the copy of the data overlaps the
+    projection instead of preceding it; the loss is the FP64 sum of the
+    ranges' losses, and the derivatives run once over all angles.
     """
 
     def __init__(self, geom, n_atoms, iso=False, fit="l2", background=0.0, order=2,
-                 psf=False):
+                 psf=False, chunks=None):
         dev = geom.device
         _require_cuda(dev)
         if fit not in ("l2", "kl"):
@@ -539,6 +545,19 @@ class FitStep:
         # the bytes each step copies (the arenas, with their alignment gaps)
         self.h2d_bytes = self.in_h.numel() * self.in_h.element_size()
         self.d2h_bytes = self.out_h.numel() * self.out_h.element_size()
+        A = geom.n_angles
+        data_bytes = int(self.data_d.numel()) * 4
+        if chunks is None:
+            chunks = min(8, (data_bytes + (128 << 20) - 1) >> 27) if data_bytes >= (128 << 20) else 1
+        chunks = max(1, min(int(chunks), A))
+        bounds = [(i * A) // chunks for i in range(chunks + 1)]
+        self.ranges = [(a0, a1, geom.angle_range(a0, a1) if chunks > 1 else geom)
+                       for a0, a1 in zip(bounds[:-1], bounds[1:])]
+        if chunks > 1:
+            self.data_off = ilay["data"][0]
+            self.loss_parts = torch.zeros(chunks, **f64)
+            self.copy_stream = torch.cuda.Stream(dev)
+            self.copied = [torch.cuda.Event() for _ in range(chunks)]
         stream = torch.cuda.Stream(dev)
         stream.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(stream):
@@ -550,9 +569,26 @@ class FitStep:
         torch.cuda.synchronize(dev)
 
     def _body(self):
-        self.in_d.copy_(self.in_h, non_blocking=True)
-        fit_forward_into(self.atoms, self.geom, self.data_d, self.fit, self.background, None,
-                         self.alpha, self.beta, self.loss, self.ws, psf=self.psf)
+        if len(self.ranges) == 1:
+            self.in_d.copy_(self.in_h, non_blocking=True)
+            fit_forward_into(self.atoms, self.geom, self.data_d, self.fit, self.background, None,
+                             self.alpha, self.beta, self.loss, self.ws, psf=self.psf)
+        else:
+            main = torch.cuda.current_stream(self.geom.device)
+            k = self.data_off
+            self.in_d[:k].copy_(self.in_h[:k], non_blocking=True)     # the atoms
+            self.copy_stream.wait_stream(main)
+            with torch.cuda.stream(self.copy_stream):
+                for (a0, a1, _g), ev in zip(self.ranges, self.copied):
+                    self.data_d[a0:a1].copy_(self.data_h[a0:a1], non_blocking=True)
+                    ev.record()
+            for i, ((a0, a1, g), ev) in enumerate(zip(self.ranges, self.copied)):
+                main.wait_event(ev)
+                fit_forward_into(self.atoms, g, self.data_d[a0:a1], self.fit, self.background,
+                                 None, self.alpha[a0:a1],
+                                 None if self.beta is None else self.beta[a0:a1],
+                                 self.loss_parts[i:i + 1], self.ws, psf=self.psf)
+            torch.sum(self.loss_parts, dim=0, out=self.loss)
         bc = 1.0 if self.fit == "l2" else 0.0
         atom_derivs_into(self.atoms, self.geom, "field", self.alpha, self.beta, bc, self.order,
                          self.f, self.g, self.H, self.ws, psf=self.psf)

@@ -168,6 +168,25 @@ class DeviceGeometry:
                 s.det_inv_step[k] = 1.0
         self.struct = s
 
+    def angle_range(self, a0, a1):
+        """The geometry of angles [a0, a1) over this one's device buffers
+        (no allocation, no copy): rows a0..a1-1 of a sinogram on this
+        geometry are a sinogram on it."""
+        if not 0 <= a0 < a1 <= self.n_angles:
+            raise ValueError("angle range [%d, %d) outside [0, %d)" % (a0, a1, self.n_angles))
+        sub = DeviceGeometry.__new__(DeviceGeometry)
+        sub.kdet, sub.dim = self.kdet, self.dim
+        sub.n_angles = a1 - a0
+        sub.frames_host = self.frames_host[a0:a1]
+        sub.frames = self.frames[a0:a1]
+        sub.det, sub.grid, sub.device = self.det, self.grid, self.device
+        sub.shape = (a1 - a0,) + tuple(self.shape[1:])
+        st = _lib.GrGeometry.from_buffer_copy(self.struct)
+        st.n_angles = sub.n_angles
+        st.frames = sub.frames.data_ptr()
+        sub.struct = st
+        return sub
+
     @staticmethod
     def from_space(space, device=None):
         """From an object with .orientations, .ortho, .detector (ProjSpace)."""

@@ -226,6 +226,14 @@ def test_fit_step_graph_matches_direct_calls(eng, cuda_ready, case):
     atoms2 = engine_atoms(I * 0.9, x, r)
     fw2 = eng.fit_forward(atoms2, geom, d, fit, bg)
     assert loss2 == fw2["loss"].item()
+    # angle ranges copied in while the previous range is projected: every
+    # cell sums the same atoms in the same order (fields, gradient and
+    # Hessian bitwise equal); the loss is a sum of the ranges' losses
+    fc = eng.FitStep(geom, len(I), fit=fit, background=bg, order=order, chunks=4)
+    assert len(fc.ranges) == 4
+    loss_c, gc, Hc = fc.run(I, x, r, data)
+    assert torch.equal(gc, gd.cpu()) and torch.equal(Hc, Hd.cpu())
+    assert abs(loss_c - fw["loss"].item()) <= 1e-12 * abs(fw["loss"].item())
 
 
 @pytest.mark.parametrize("accepted", [True, False])

@@ -163,3 +163,22 @@ def test_malformed_requests_are_refused_before_the_device():
     for what, rq in cases:
         with pytest.raises(ValueError):
             serving.validate_request(rq)
+
+
+def test_angle_range_views_the_parent_geometry():
+    """DeviceGeometry.angle_range: a sub-geometry over the parent's buffers
+    (frame records offset by a0 records, same detector), no copy."""
+    geometry = importlib.import_module(PKG + ".geometry")
+    th = np.linspace(0, np.pi, 12, endpoint=False)
+    T = np.stack([-np.sin(th), np.cos(th)], 1)
+    w = np.stack([np.cos(th), np.sin(th)], 1)
+    g = geometry.DeviceGeometry(T, (w,), (np.linspace(-1, 1, 40),), device="cpu")
+    sub = g.angle_range(3, 9)
+    assert sub.n_angles == 6 and sub.shape == (6, 40)
+    assert sub.struct.n_angles == 6 and sub.struct.kdet == g.struct.kdet
+    stride = g.frames.shape[1] * g.frames.element_size()
+    assert sub.struct.frames == g.struct.frames + 3 * stride
+    assert sub.struct.det[0] == g.struct.det[0]
+    assert np.array_equal(sub.frames.numpy(), g.frames.numpy()[3:9])
+    with pytest.raises(ValueError):
+        g.angle_range(5, 13)
