@@ -61,7 +61,33 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-orient", type=int, default=None,
                     help="config4: fewer orientations (a reduced case for profiling)")
+    ap.add_argument("--request", default=None, choices=["2d", "3d"],
+                    help="profiling: fit evaluations (forward + Hessians) of the largest "
+                         "2D or 3D request of the served stream, then exit")
     return ap.parse_args()
+
+
+def run_request(args):
+    """Three fit evaluations of the largest 2D or 3D request of the served
+    stream (its 200 first requests): fit_forward and order-2 derivatives,
+    for ncu captures of the served kernels on their own shapes."""
+    import torch
+    importlib.import_module("__graft_entry__").build()
+    engine = importlib.import_module(PKG + ".engine")
+    geometry = importlib.import_module(PKG + ".geometry")
+    wl = importlib.import_module(PKG + ".workloads")
+    k = 1 if args.request == "2d" else 2
+    reqs = [r for r in wl.config3_requests(n=200, seed=3) if len(r.detector) == k]
+    W = max(reqs, key=lambda r: r.size_hint[0] * r.size_hint[1])
+    geom = geometry.DeviceGeometry(W.orientations, W.ortho, W.detector)
+    atoms = engine.DeviceAtoms(*W.init)
+    d = W.make_data(geom, geom.device, torch.cuda.current_stream())
+    for _ in range(3):
+        fw = engine.fit_forward(atoms, geom, d, "l2", 0.0)
+        engine.atom_derivs(atoms, geom, "field", fw["alpha"], None, 1.0, 2)
+    torch.cuda.synchronize()
+    print(json.dumps({"request": W.id, "atoms": W.size_hint[0], "angles": len(W.orientations),
+                      "detector": [len(c) for c in W.detector], "loss": float(fw["loss"])}))
 
 
 def dist_env():
@@ -930,7 +956,9 @@ def run_serving(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.request:
+        run_request(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "config3":
         run_serving(args)
