@@ -83,7 +83,7 @@ class FitRequest:
 
     def __init__(self, rid, orientations, ortho, detector, init, make_data, fit="l2",
                  background=0.0, max_iter=100, tol=1e-6, arrival=0.0, lam0=1.0,
-                 lam_max=1e8):
+                 lam_max=1e8, reg=None):
         self.id = rid
         self.orientations = orientations
         self.ortho = ortho
@@ -103,6 +103,10 @@ class FitRequest:
         # there, repeating one rejected trial (on the 512-request stream 204
         # fits ended without an accepted step; with 1e8 none)
         self.lam_max = lam_max
+        # optional regulariser (a regularisation.Joubert/Mass/Volume/Radius/Iso):
+        # its value joins the fit's loss and its gradient and Hessian the
+        # blocks, as in the reference's Newton loop (NewtonGaussian.py:59-66)
+        self.reg = reg
         self.data_host = None       # optional payload (pinned host tensor)
         n = len(init[0])
         cells = len(orientations) * int(np.prod([len(d) for d in detector]))
@@ -150,6 +154,15 @@ def validate_request(req):
         raise ValueError("request %s: the KL fit needs a positive background" % req.id)
     if int(req.max_iter) < 1 or not req.tol >= 0:
         raise ValueError("request %s: max_iter >= 1 and tol >= 0" % req.id)
+    if req.reg is not None:
+        kind = getattr(req.reg, "kind", None)
+        if kind not in engine.REG_KINDS or not hasattr(req.reg, "_p"):
+            raise ValueError("request %s: reg must be a device regulariser "
+                             "(regularisation.Joubert, Mass, Volume, Radius or Iso)" % req.id)
+        p = np.asarray(req.reg._p(), dtype=np.float64)
+        if p.size > 8 or not np.all(np.isfinite(p)):
+            raise ValueError("request %s: regulariser parameters must be at most 8 finite "
+                             "numbers" % req.id)
     if req.data_host is not None:
         d = req.data_host
         shape = (A,) + tuple(v.size for v in det)
@@ -309,13 +322,16 @@ class _Slot:
                                                self.plan_p))
         ws_d = max(256, engine.workspace_bytes(_lib.GR_OP_DERIVS_2, self.cur, self.geom,
                                                self.plan_d))
+        reg = req.reg is not None
         wl, n_work = _layout([("data", np.float32, shape), ("alpha", np.float32, shape),
                               ("alpha_t", np.float32, shape)] +
                              ([("beta", np.float32, shape), ("beta_t", np.float32, shape)]
                               if kl else []) +
                              [("f", np.float64, (n,)), ("g", np.float64, (n, P)),
                               ("H", np.float64, (n, P, P)), ("step", np.float64, (n,)),
-                              ("ws_p", np.uint8, (ws_p,)), ("ws_d", np.uint8, (ws_d,))])
+                              ("ws_p", np.uint8, (ws_p,)), ("ws_d", np.uint8, (ws_d,))] +
+                             ([("reg_f", np.float64, (n,)), ("reg_g", np.float64, (n, P)),
+                               ("reg_sum", np.float64, ())] if reg else []))
         self.arena_work = torch.empty(n_work, dtype=torch.uint8, device=device)
         vwork = _typed_views(self.arena_work)
         w = lambda name: vwork(wl[name])
@@ -329,6 +345,10 @@ class _Slot:
         self.beta, self.beta_t = (w("beta"), w("beta_t")) if kl else (None, None)
         self.f, self.g, self.H, self.step = w("f"), w("g"), w("H"), w("step")
         self.ws_p, self.ws_d = w("ws_p"), w("ws_d")
+        if reg:
+            self.reg_kind = req.reg.kind
+            self.reg_params = np.asarray(req.reg._p(), dtype=np.float64)
+            self.reg_f, self.reg_g, self.reg_sum = w("reg_f"), w("reg_g"), w("reg_sum")
         # results come back into pinned memory: history, counter, parameters
         # and loss, read after the completion event without a stream sync
         self.res_layout, n_res = _layout([("hist", np.float64, (L,)), ("acc", np.int32, (L,)),
@@ -416,6 +436,7 @@ class _Slot:
         alpha, beta = self._current_fields(self.loop is not None)
         engine.fit_forward_into(self.cur, self.geom, self.data, r.fit, r.background, None,
                                 alpha, beta, self.loss_cur, self.ws_p, plan=self.plan_p)
+        self._add_reg_value(self.cur, self.loss_cur)
         self.h_loss0.copy_(self.loss_cur.reshape(1), non_blocking=True)
 
     def iterate(self, loop=None):
@@ -430,17 +451,31 @@ class _Slot:
         with (loop.unless_rejected() if loop is not None else contextlib.nullcontext()):
             engine.atom_derivs_into(self.cur, self.geom, "field", alpha, beta, beta_c,
                                     2, self.f, self.g, self.H, self.ws_d, plan=self.plan_d)
+            if r.reg is not None:
+                engine.regulariser(self.reg_kind, self.reg_params, self.cur, self.f, self.g,
+                                   self.H, accumulate=True, order=2)
         engine.newton_solve_into(self.dim, self.iso, self.g, self.H, self.lam, self.theta,
                                  self.theta_trial, self.step, self.trial, self.dev)
         engine.fit_forward_into(self.trial, self.geom, self.data, r.fit, r.background, None,
                                 self.alpha_t, self.beta_t, self.loss_trial, self.ws_p,
                                 plan=self.plan_p)
+        self._add_reg_value(self.trial, self.loss_trial)
         engine.newton_accept_into(self.dim, self.iso, self.loss_cur, self.loss_trial,
                                   self.theta, self.theta_trial, self.lam, 1e-4, r.lam_max,
                                   self.cur, self.trial, self.hist, self.hist_acc,
                                   self.counter, self.dev,
                                   fields=None if loop is not None else
                                   (self.alpha_t, self.alpha, self.beta_t, self.beta))
+
+    def _add_reg_value(self, atoms, loss):
+        """With a regulariser, add its value at ``atoms`` to ``loss`` (FP64, on
+        the stream: no allocation, so it can be captured)."""
+        if self.req.reg is None:
+            return
+        engine.regulariser(self.reg_kind, self.reg_params, atoms, f=self.reg_f, g=self.reg_g,
+                           H=None, accumulate=False, order=1)
+        torch.sum(self.reg_f, dim=0, out=self.reg_sum)
+        loss.add_(self.reg_sum)
 
     def _copy_back(self):
         self.h_counter.copy_(self.counter, non_blocking=True)
@@ -783,17 +818,19 @@ def serve_plain(requests, device=None, t0=None, lean=False):
         geom = DeviceGeometry(req.orientations, req.ortho, req.detector, dev)
         data = req.device_data(geom, dev, stream)
         atoms = engine.DeviceAtoms(*req.init, dev)
-        cur, losses, accepted = _plain_fit(atoms, geom, data, req, lean)
+        cur, losses, accepted, trials = _plain_fit(atoms, geom, data, req, lean)
         torch.cuda.synchronize(dev)
         fin = time.perf_counter() - t0
-        out[req.id] = {"loss": losses[-1], "loss0": losses[0], "iterations": len(losses) - 1,
+        # iterations: trials, accepted or not (as the served loop counts them)
+        out[req.id] = {"loss": losses[-1], "loss0": losses[0], "iterations": trials,
                        "accepted": accepted, "status": "ok" if accepted else "no_progress",
                        "arrival": req.arrival, "finish": fin, "latency": fin - req.arrival}
     return out
 
 
 def _plain_fit(atoms, geom, data, req, lean=False):
-    """Eager damped Newton with the same accept rule and stopping test."""
+    """Eager damped Newton with the same accept rule and stopping test.
+    Returns (atoms, loss after every accepted step, accepted steps, trials)."""
     from . import solvers
     dim, iso = atoms.dim, atoms.iso
     theta = solvers.theta_of(atoms.I, atoms.x, atoms.r)
@@ -804,21 +841,28 @@ def _plain_fit(atoms, geom, data, req, lean=False):
     losses = []
     rejects = 0
     accepted = 0
+    reg = req.reg
+    # with a regulariser: its value joins the loss, its terms the blocks
+    reg_value = (lambda a: float(reg.terms(a, order=1)[0].sum().item())) if reg else (lambda a: 0.0)
     fw = engine.fit_forward(cur, geom, data, fit, bg)
-    loss = float(fw["loss"].item())
+    loss = float(fw["loss"].item()) + reg_value(cur)
     g = H = None
+    trials = 0
     for it in range(req.max_iter):
+        trials += 1
         if not lean and it > 0:
             fw = engine.fit_forward(cur, geom, data, fit, bg)
-            loss = float(fw["loss"].item())
+            loss = float(fw["loss"].item()) + reg_value(cur)
         if not losses:
             losses.append(loss)
         if g is None or not lean or rejects == 0:
-            _f, g, H = engine.atom_derivs(cur, geom, "field", fw["alpha"], fw["beta"], beta_c, 2)
+            f_, g, H = engine.atom_derivs(cur, geom, "field", fw["alpha"], fw["beta"], beta_c, 2)
+            if reg:
+                reg.device_terms(cur, f_, g, H)
         th, _s, _fl = engine.newton_solve(dim, iso, g.contiguous(), H.contiguous(), lam, theta)
         trial = solvers.atoms_of(th, dim, geom.device)
         fwt = engine.fit_forward(trial, geom, data, fit, bg, want_fields=lean)
-        new = float(fwt["loss"].item())
+        new = float(fwt["loss"].item()) + reg_value(trial)
         if new <= loss:
             theta, cur = th, trial
             if lean:
@@ -835,4 +879,4 @@ def _plain_fit(atoms, geom, data, req, lean=False):
             rejects += 1
             if rejects >= MAX_BACKTRACK:
                 break
-    return cur, losses, accepted
+    return cur, losses, accepted, trials

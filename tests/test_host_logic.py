@@ -152,6 +152,13 @@ def test_malformed_requests_are_refused_before_the_device():
     r.max_iter = 0
     cases.append(("max_iter", r))
     r = copy.copy(req)
+    r.reg = "joubert"
+    cases.append(("regulariser object", r))
+    r = copy.copy(req)
+    regm = importlib.import_module(PKG + ".regularisation")
+    r.reg = regm.Joubert(len(req.init[1][0]), float("nan"), 1e-2, (1e-3, 1e-4))
+    cases.append(("regulariser parameters", r))
+    r = copy.copy(req)
     shape = (len(req.orientations),) + tuple(len(d) for d in req.detector)
     bad = torch.zeros(shape)
     bad[0].view(-1)[0] = float("inf")

@@ -253,3 +253,31 @@ def test_tuned_server_runs_each_class_under_its_plans(cuda_ready):
     for k in a:
         assert abs(a[k]["loss"] - b[k]["loss"]) <= 1e-4 * abs(b[k]["loss"])
         assert a[k]["loss"] <= a[k]["loss0"]
+
+
+def test_regularised_served_fit_matches_plain_fit(cuda_ready):
+    """A request with a regulariser (the reference's Newton loop takes one:
+    NewtonGaussian.py:59-66): its value joins the loss and its gradient and
+    Hessian the blocks, in the device loop as in the plain loop."""
+    regm = importlib.import_module(PKG + ".regularisation")
+
+    def reqs():
+        out = _requests(n=4)
+        for r in out:
+            r.arrival = 0.0
+            dim = len(r.init[1][0])
+            r.reg = regm.Joubert(dim, 1e-3, 1e-2, (1e-3, 1e-4))
+        return out
+    srv = serving.GaussFitServer(max_slots=4, n_streams=2)
+    for r in reqs():
+        srv.submit(r)
+    served = srv.run()
+    srv.close()
+    plain = serving.serve_plain(reqs())
+    bare = serving.serve_plain(_requests(n=4))
+    for k in plain:
+        # the same trajectory: the same accepted steps and trials, the same loss
+        assert served[k]["accepted"] == plain[k]["accepted"]
+        assert abs(served[k]["loss"] - plain[k]["loss"]) <= 1e-12 * abs(plain[k]["loss"])
+        # the regulariser changed the fit
+        assert served[k]["loss"] != bare[k]["loss"]
