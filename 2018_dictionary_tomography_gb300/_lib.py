@@ -34,6 +34,32 @@ class GrGeometry(ctypes.Structure):
                 ("det_inv_step", ctypes.c_float * 2)]
 
 
+class GrBatchMember(ctypes.Structure):
+    """gr_batch_member: one 2D fit of a batch (device pointers)."""
+    _fields_ = [("cur", GrAtoms),
+                ("trial", GrAtoms),
+                ("geom", GrGeometry),
+                ("data", ctypes.c_void_p),
+                ("fields", ctypes.c_void_p),
+                ("loss_cur", ctypes.c_void_p),
+                ("loss_trial", ctypes.c_void_p),
+                ("theta", ctypes.c_void_p),
+                ("theta_trial", ctypes.c_void_p),
+                ("lam", ctypes.c_void_p),
+                ("step", ctypes.c_void_p),
+                ("f", ctypes.c_void_p),
+                ("g", ctypes.c_void_p),
+                ("H", ctypes.c_void_p),
+                ("hist", ctypes.c_void_p),
+                ("hist_acc", ctypes.c_void_p),
+                ("counter", ctypes.c_void_p),
+                ("hist_len", ctypes.c_int),
+                ("max_iter", ctypes.c_int),
+                ("tol", ctypes.c_double),
+                ("lam_min", ctypes.c_double),
+                ("lam_max", ctypes.c_double)]
+
+
 class EngineError(RuntimeError):
     pass
 
@@ -49,7 +75,8 @@ EXPORTS = ("gr_version", "gr_preload", "gr_status_string", "gr_workspace_bytes",
            "gr_sino_moments", "gr_accept_fields", "gr_newton_accept_fields",
            "gr_plan_create", "gr_plan_destroy", "gr_plan_set", "gr_plan_get",
            "gr_plan_workspace_bytes", "gr_radproj_plan", "gr_fit_forward_plan",
-           "gr_atom_derivs_plan")
+           "gr_atom_derivs_plan", "gr_batch_workspace_bytes", "gr_batch_create",
+           "gr_batch_prologue", "gr_batch_iterate", "gr_fit_loop_end_open", "gr_batch_destroy")
 
 _lock = threading.Lock()
 _lib = None
@@ -162,6 +189,20 @@ def load(build_if_missing=True):
         lib.gr_fit_loop_launch.argtypes = [vp, vp]
         lib.gr_fit_loop_destroy.restype = ctypes.c_int
         lib.gr_fit_loop_destroy.argtypes = [vp]
+        bm = ctypes.POINTER(GrBatchMember)
+        lib.gr_batch_workspace_bytes.restype = ctypes.c_size_t
+        lib.gr_batch_workspace_bytes.argtypes = [bm, ctypes.c_int]
+        lib.gr_batch_create.restype = ctypes.c_int
+        lib.gr_batch_create.argtypes = [bm, ctypes.c_int, vp, ctypes.c_size_t, ctypes.c_int, vp,
+                                        ctypes.POINTER(vp)]
+        lib.gr_batch_prologue.restype = ctypes.c_int
+        lib.gr_batch_prologue.argtypes = [vp, vp]
+        lib.gr_batch_iterate.restype = ctypes.c_int
+        lib.gr_batch_iterate.argtypes = [vp, vp, vp]
+        lib.gr_fit_loop_end_open.restype = ctypes.c_int
+        lib.gr_fit_loop_end_open.argtypes = [vp, vp]
+        lib.gr_batch_destroy.restype = ctypes.c_int
+        lib.gr_batch_destroy.argtypes = [vp]
         lib.gr_kernel_timer_read.restype = ctypes.c_int
         lib.gr_kernel_timer_read.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                              ctypes.POINTER(ctypes.c_int)]

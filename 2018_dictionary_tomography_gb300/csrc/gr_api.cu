@@ -1,5 +1,6 @@
 // C ABI of the Gaussian-atom Radon engine (declared in include/gauss_radon.h).
 #include <new>
+#include <vector>
 
 #include "gr_kernels.cuh"
 #include "gauss_radon.h"
@@ -42,9 +43,62 @@ bool to_internal(const gr_atoms *a, const gr_geometry *g, Atoms &at, Geom &ge,
   return true;
 }
 
+// A batch member as the kernels' problem descriptor (buffers and atoms; the
+// launch shapes are set by batch_create).
+bool batch_member(const gr_batch_member &m, BatchProb &p) {
+  int st;
+  Geom g2;
+  if (!to_internal(&m.cur, &m.geom, p.cur, p.g, &st)) return false;
+  if (!to_internal(&m.trial, &m.geom, p.trial, g2, &st)) return false;
+  if (p.g.K != 1 || p.cur.order || p.trial.order || !m.data || !m.fields || !m.loss_cur ||
+      !m.loss_trial || !m.theta || !m.theta_trial || !m.lam || !m.step || !m.f || !m.g || !m.H ||
+      !m.hist || !m.hist_acc || !m.counter || m.hist_len < 1 || m.max_iter < 1 ||
+      !(m.tol >= 0.0))
+    return false;
+  p.out = ProjOut{nullptr, kEpiL2, m.data, 0.f, m.fields, nullptr, nullptr, 0};
+  p.loss_cur = m.loss_cur;
+  p.loss_trial = m.loss_trial;
+  p.dout = DerivOut{m.f, m.g, m.H};
+  p.theta = m.theta;
+  p.theta_trial = m.theta_trial;
+  p.lam = m.lam;
+  p.step = m.step;
+  p.hist = m.hist;
+  p.hist_acc = m.hist_acc;
+  p.counter = m.counter;
+  p.hist_len = m.hist_len;
+  p.max_iter = m.max_iter;
+  p.tol = m.tol;
+  p.lam_min = m.lam_min;
+  p.lam_max = m.lam_max;
+  return true;
+}
+
 }  // namespace
 
 extern "C" {
+
+size_t gr_batch_workspace_bytes(const gr_batch_member *members, int n) {
+  if (!members || n < 1) return 0;
+  std::vector<BatchProb> probs(n);
+  for (int i = 0; i < n; ++i)
+    if (!batch_member(members[i], probs[i])) return 0;
+  return batch_workspace_bytes(probs.data(), n);
+}
+
+int gr_batch_create(const gr_batch_member *members, int n, void *ws, size_t ws_bytes,
+                    int max_reject, void *stream, void **batch) {
+  if (!members || n < 1 || !batch) return GR_ERR_ARG;
+  *batch = nullptr;
+  std::vector<BatchProb> probs(n);
+  for (int i = 0; i < n; ++i)
+    if (!batch_member(members[i], probs[i])) return GR_ERR_ARG;
+  Batch *b = nullptr;
+  const int rc = batch_create(probs.data(), n, ws, ws_bytes, max_reject,
+                              static_cast<cudaStream_t>(stream), &b);
+  *batch = b;
+  return rc;
+}
 
 int gr_version(void) { return 10000; }
 

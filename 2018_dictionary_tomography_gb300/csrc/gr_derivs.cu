@@ -29,15 +29,6 @@
 
 namespace gr {
 
-struct DerivCfg {
-  int ag;       // distinct atoms per warp (power of two)
-  int sg;       // lanes per atom (32 / ag)
-  int ch;       // angles per chunk
-  int nchunks;
-  int qn;       // partial values per atom
-  int rs;       // lanes sharing one (atom, angle) pair's cells (power of two)
-};
-
 inline int next_pow2(int v) {
   int p = 1;
   while (p < v && p < 32) p <<= 1;
@@ -83,8 +74,7 @@ constexpr int kRowChunk3 = GR_ROW_CHUNK_3D;
 // On 8192 atoms x 20000 orientations the one-angle split (625 chunks, 225 MB
 // of partials) runs the gradient kernel in 23.6 ms against 25.7 ms for 16
 // chunks.
-inline DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order, const Tuning &t,
-                          bool split = true) {
+DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order, const Tuning &t, bool split) {
   DerivCfg c;
   c.ag = next_pow2(n_atoms < 1 ? 1 : n_atoms);
   const int ag_cap = t.deriv_atoms_per_warp > 0 ? t.deriv_atoms_per_warp
@@ -292,10 +282,11 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
 // costs idle lanes on narrow ones (Tuning key 8; measured: 2936 atoms x 148
 // angles of 493^2 cells 460 -> 408 us, config 2's atoms 192 -> 200 us; 16
 // instead of 8 cells slowed every 2D Hessian measured, by up to 25 %)
+// The body of one 128-thread block (the launch's block; a multi-problem
+// launch maps its blocks to (problem, block)).
 template <int K, int ORDER, bool ONE, bool WIDE = false>
-__global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS
-                                           : (ONE ? (K == 1 ? GR_HESS2D_MIN_BLOCKS : 3) : 1))
-    gr_deriv_kernel(Atoms at, Geom g, DerivIn in, DerivCfg cfg, float *part) {
+__device__ __forceinline__ void deriv_body(const Atoms &at, const Geom &g, const DerivIn &in,
+                                           const DerivCfg &cfg, float *part, int block) {
   constexpr int D = K + 1;
   constexpr int PR = n_rparam<K>();
   constexpr int P = n_par<K>();
@@ -304,7 +295,7 @@ __global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS
   constexpr int DEG = ORDER == 1 ? 2 : 4;
   constexpr int NH = P * (P + 1) / 2;
   constexpr bool GN = ORDER > 1;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int gw = (block * 128 + (int)threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int warps_atoms = (at.n + cfg.ag - 1) / cfg.ag;
   if (gw >= warps_atoms * cfg.nchunks) return;
@@ -413,6 +404,13 @@ __global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS
 #pragma unroll
     for (int i = 0; i < NH; ++i) dst[(1 + P + i) * N] = hacc[i];
   }
+}
+
+template <int K, int ORDER, bool ONE, bool WIDE = false>
+__global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS
+                                           : (ONE ? (K == 1 ? GR_HESS2D_MIN_BLOCKS : 3) : 1))
+    gr_deriv_kernel(Atoms at, Geom g, DerivIn in, DerivCfg cfg, float *part) {
+  deriv_body<K, ORDER, ONE, WIDE>(at, g, in, cfg, part, blockIdx.x);
 }
 
 // Pixel-integrated operator: per cell, the quadrature points' moments give
@@ -602,11 +600,12 @@ __global__ void __launch_bounds__(128)
 constexpr int kRedSlices = 8;
 constexpr int kFinAtoms = 4;
 constexpr int kFinThreads = 32 * kRedSlices;
+// The body of one block of the finalize launch (the launch's block; a
+// multi-problem launch maps its blocks to (problem, block)).
 template <int K>
-__global__ void __launch_bounds__(kFinThreads)
-    gr_deriv_finalize_kernel(const float *part, DerivCfg cfg, int n, int deriv_order,
-                             int r_iso, DerivOut out, const double *f_extra,
-                             const int *order) {
+__device__ __forceinline__ void finalize_body(const float *part, const DerivCfg &cfg, int n,
+                                              int deriv_order, int r_iso, const DerivOut &out,
+                                              const double *f_extra, const int *order, int block) {
   constexpr int D = K + 1;
   constexpr int P = n_par<K>();
   constexpr int QN = 1 + P + P * (P + 1) / 2;
@@ -614,7 +613,7 @@ __global__ void __launch_bounds__(kFinThreads)
   // q = ty, ty + 32, ... of its atom, all loads independent
   __shared__ double vs[QN][kFinAtoms];
   const int tx = threadIdx.x % kFinAtoms, ty = threadIdx.x / kFinAtoms;
-  const int slot = blockIdx.x * kFinAtoms + tx;
+  const int slot = block * kFinAtoms + tx;
   if (slot < n)
     for (int q = ty; q < cfg.qn; q += kFinThreads / kFinAtoms) {
       double t = 0.0;
@@ -625,9 +624,9 @@ __global__ void __launch_bounds__(kFinThreads)
   __syncthreads();
   // outputs of the block's atoms, written by all threads from the sums
   // (consecutive threads write consecutive entries of an atom's block)
-  const int nb = min(kFinAtoms, n - (int)blockIdx.x * kFinAtoms);
+  const int nb = min(kFinAtoms, n - (int)block * kFinAtoms);
   auto atom_of = [&](int t) {
-    const int sl = blockIdx.x * kFinAtoms + t;
+    const int sl = block * kFinAtoms + t;
     return order ? order[sl] : sl;
   };
   // entry (a, b) of the full Hessian from the packed upper triangle
@@ -680,6 +679,14 @@ __global__ void __launch_bounds__(kFinThreads)
         for (int qb = 0; qb < nbb; ++qb) hs += hv(src(a, qa), src(b, qb), t);
       out.H[(size_t)atom_of(t) * PI * PI + ab] = hs;
     }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kFinThreads)
+    gr_deriv_finalize_kernel(const float *part, DerivCfg cfg, int n, int deriv_order,
+                             int r_iso, DerivOut out, const double *f_extra,
+                             const int *order) {
+  finalize_body<K>(part, cfg, n, deriv_order, r_iso, out, f_extra, order, blockIdx.x);
 }
 
 // 1/2 sum C^2 helper: block partial sums (FP32 compensated per thread, FP64
@@ -850,6 +857,46 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
+// ---- multi-problem launches (2D Hessians, one angle per lane) ------------
+// The derivatives of a problem run only on its first iteration or after an
+// accepted trial (a rejected trial leaves its atoms and fields unchanged),
+// and not once its fit has stopped.
+__device__ __forceinline__ bool batch_derivs_wanted(const BatchProb &B, int active) {
+  if (!active) return false;
+  const int c = *B.counter;
+  return !(c > 0 && c <= B.hist_len && !B.hist_acc[c - 1]);
+}
+
+__global__ void __launch_bounds__(128, GR_HESS2D_MIN_BLOCKS)
+    gr_batch_deriv_kernel(const BatchProb *__restrict__ probs, const int *__restrict__ off,
+                          int n, const int *__restrict__ active) {
+  const int p = batch_find(off, n, blockIdx.x);
+  const BatchProb &B = probs[p];
+  if (!batch_derivs_wanted(B, active[p])) return;
+  deriv_body<1, 2, true>(B.cur, B.g, B.din, B.cfg, B.part, blockIdx.x - off[p]);
+}
+
+__global__ void __launch_bounds__(kFinThreads)
+    gr_batch_finalize_kernel(const BatchProb *__restrict__ probs, const int *__restrict__ off,
+                             int n, const int *__restrict__ active) {
+  const int p = batch_find(off, n, blockIdx.x);
+  const BatchProb &B = probs[p];
+  if (!batch_derivs_wanted(B, active[p])) return;
+  finalize_body<1>(B.part, B.cfg, B.cur.n, 2, B.cur.r_iso, B.dout, nullptr, nullptr,
+                   blockIdx.x - off[p]);
+}
+
+int finalize_blocks(int n_atoms) { return (n_atoms + kFinAtoms - 1) / kFinAtoms; }
+
+int launch_batch_derivs(const BatchLaunch &b, cudaStream_t stream) {
+  if (b.grid_deriv <= 0) return kOk;
+  gr_batch_deriv_kernel<<<b.grid_deriv, 128, 0, stream>>>(b.probs, b.off_deriv, b.n, b.active);
+  gr_batch_finalize_kernel<<<b.grid_fin, kFinThreads, 0, stream>>>(b.probs, b.off_fin, b.n,
+                                                                   b.active);
+  note_launches(2);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
 int preload_derivs() {
   return preload_fn(gr_deriv_kernel<1, 1, false>) + preload_fn(gr_deriv_kernel<1, 2, false>) +
          preload_fn(gr_deriv_kernel<2, 1, false>) + preload_fn(gr_deriv_kernel<2, 2, false>) +
@@ -860,7 +907,8 @@ int preload_derivs() {
          preload_fn(gr_psf_deriv_kernel<1, 1>) + preload_fn(gr_psf_deriv_kernel<1, 2>) +
          preload_fn(gr_psf_deriv_kernel<2, 1>) + preload_fn(gr_psf_deriv_kernel<2, 2>) +
          preload_fn(gr_deriv_finalize_kernel<1>) + preload_fn(gr_deriv_finalize_kernel<2>) +
-         preload_fn(gr_sumsq_kernel) + preload_fn(gr_sumsq_finalize_kernel);
+         preload_fn(gr_sumsq_kernel) + preload_fn(gr_sumsq_finalize_kernel) +
+         preload_fn(gr_batch_deriv_kernel) + preload_fn(gr_batch_finalize_kernel);
 }
 
 }  // namespace gr

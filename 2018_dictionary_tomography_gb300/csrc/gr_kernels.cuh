@@ -62,6 +62,16 @@ struct DerivOut {
   double *H;   // (N, P_out, P_out), order 2
 };
 
+// Work split of a derivative launch (gr_derivs.cu, deriv_cfg).
+struct DerivCfg {
+  int ag;       // distinct atoms per warp (power of two)
+  int sg;       // lanes per atom (32 / ag)
+  int ch;       // angles per chunk
+  int nchunks;
+  int qn;       // partial values per atom
+  int rs;       // lanes sharing one (atom, angle) pair's cells (power of two)
+};
+
 inline size_t align_up(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // Work-split and tiling schedule of the projection and derivative launches
@@ -91,6 +101,9 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o,
 
 size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order,
                               const Tuning &t = g_tuning);
+DerivCfg deriv_cfg(int K, int n_atoms, int n_angles, int order, const Tuning &t,
+                   bool split = true);
+int finalize_blocks(int n_atoms);   // grid of the derivative finalize launch
 int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
                   const DerivOut &out, void *ws, size_t ws_bytes,
                   cudaStream_t stream, const Tuning &t = g_tuning);
@@ -134,6 +147,70 @@ int launch_newton_accept(int n, int P, int pr, int dim, double *loss_cur,
 
 int launch_volproj(const Atoms &at, int dim, const int *n, const float *const *y,
                    float *u, int psf, float s, cudaStream_t stream);
+
+// ---- multi-problem launches (gr_loop.cu builds them) -----------------------
+// One 2D L2 damped-Newton problem of a multi-problem launch: its device
+// buffers and launch shapes.  A table of them lives in device memory, and
+// each kernel of the batched iteration maps its blocks to (problem, block of
+// that problem) through per-kernel block offsets, then runs the same block
+// body as the problem's own launch would: every problem gets the results it
+// gets alone.
+struct BatchProb {
+  Atoms cur, trial;
+  Geom g;
+  TileCfg tc;
+  int W, items;                 // bitmap words per tile, (angle, tile) items
+  ProjOut out;                  // data, fit fields, loss partials (L2 epilogue)
+  uint32_t *bitmap;
+  float4 *pairs;
+  int *done;                    // finished-block counter of the projection
+  double *loss_cur, *loss_trial;
+  DerivIn din;                  // field mode on the fit fields, order 2
+  DerivCfg cfg;
+  float *part;                  // derivative chunk partials
+  DerivOut dout;                // f, g, H of the current atoms
+  double *theta, *theta_trial, *lam, *step;
+  double *hist;
+  int *hist_acc, *counter;
+  int hist_len, max_iter;
+  double tol, lam_min, lam_max;
+  int P, pr;                    // parameters and r entries per atom
+};
+
+// The device tables of a batch: per kernel, off[p] is problem p's first
+// block and off[n] the launch's grid.
+struct BatchLaunch {
+  const BatchProb *probs;
+  int n;
+  int *active;                  // 1 while problem p's fit runs
+  const int *off_bin, *off_proj, *off_deriv, *off_fin, *off_solve, *off_acc;
+  int grid_bin, grid_proj, grid_deriv, grid_fin, grid_solve, grid_acc;
+};
+
+// the problem owning block b: the last p with off[p] <= b (off[0] = 0,
+// b < off[n]; problems of no blocks are skipped)
+__device__ __forceinline__ int batch_find(const int *off, int n, int b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(off + mid) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct Batch;
+// workspace of a batch of these problems (0: a problem cannot be batched)
+size_t batch_workspace_bytes(const BatchProb *probs, int n);
+// probs: atoms, geometry and the caller's per-problem buffers filled in; the
+// launch shapes and workspace pointers are set here
+int batch_create(const BatchProb *probs, int n, void *ws, size_t ws_bytes, int max_reject,
+                 cudaStream_t stream, Batch **out);
+int launch_batch_bin(const BatchLaunch &b, int use_trial, cudaStream_t stream);
+int launch_batch_project(const BatchLaunch &b, int use_trial, cudaStream_t stream);
+int launch_batch_derivs(const BatchLaunch &b, cudaStream_t stream);
+int launch_batch_solve(const BatchLaunch &b, int P, cudaStream_t stream);
+int launch_batch_accept(const BatchLaunch &b, cudaStream_t stream);
 
 
 // host-side count of kernels launched by this library

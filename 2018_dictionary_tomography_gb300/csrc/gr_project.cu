@@ -24,12 +24,14 @@ namespace gr {
 // pairs (2D only, nullable): the pair's projection data as the 2D
 // projection stages it, two float4 per (angle, atom) at [a n + j], written
 // here once instead of being recomputed by every tile the atom touches
+// The body of a 128-thread block of the binning launch: atoms bx * 128 ..,
+// angle a (the launch's block (bx, a); a multi-problem launch maps its
+// blocks to (problem, bx, a)).
 template <int K>
-__global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
-                                                     TileCfg tc, uint32_t *bitmap,
-                                                     int W, float4 *pairs) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int a = blockIdx.y;
+__device__ __forceinline__ void bin_body(const Atoms &at, const Geom &g, const TileCfg &tc,
+                                         uint32_t *bitmap, int W, float4 *pairs, int bx,
+                                         int a) {
+  const int j = bx * 128 + (int)threadIdx.x;
   const uint32_t bit = 1u << (j & 31);
   const size_t base = (size_t)a * tc.ntiles;
   const int wj = j >> 5;
@@ -74,6 +76,13 @@ __global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
       for (int tcix = c_lo; tcix <= c_hi; ++tcix)
         atomicOr(bitmap + (base + (size_t)tr * tc.nt1 + tcix) * W + wj, bit);
   }
+}
+
+template <int K>
+__global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
+                                                     TileCfg tc, uint32_t *bitmap,
+                                                     int W, float4 *pairs) {
+  bin_body<K>(at, g, tc, bitmap, W, pairs, blockIdx.x, blockIdx.y);
 }
 
 // Per-cell KL term f log(f/g) - f + g = g h(u), u = f/g, h(u) = u log u - u + 1,
@@ -384,11 +393,15 @@ __global__ void __launch_bounds__(kProjWarps * 32)
 // so tiles crossed by many atoms take fewer passes and barriers (2150 atoms x
 // 153 angles: 87.9 us with one atom per thread, 82.6 with two, 79.5 with
 // four; 512 atoms: 20.6, 20.7, 21.1 us)
+// The body of one block of the 2D projection: (angle, tile) item of n_items
+// (the launch's block; a multi-problem launch maps its blocks to (problem,
+// item)).
 template <bool KAHAN, int NW, int CPL = 1, int LM = 1>
-__global__ void __launch_bounds__(NW * 32)
-    gr_project1d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
-                        int W, ProjOut out, double *loss_out, int *done,
-                        const float4 *__restrict__ pairs) {
+__device__ __forceinline__ void project1d_body(const Atoms &at, const Geom &g, const TileCfg &tc,
+                                               const uint32_t *bitmap, int W, const ProjOut &out,
+                                               double *loss_out, int *done,
+                                               const float4 *__restrict__ pairs, int item,
+                                               int n_items) {
   constexpr int T = NW * 32;
   constexpr int LT = LM * T;
   __shared__ float4 prm[LT][2];
@@ -396,7 +409,6 @@ __global__ void __launch_bounds__(NW * 32)
   __shared__ int wsum[NW];
   __shared__ float parts[NW][2][32 * CPL];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int item = blockIdx.x;
   const int a = item / tc.ntiles, t = item - a * tc.ntiles;
   const int D0 = g.ax[0].n;
   int cell[CPL];
@@ -526,7 +538,7 @@ __global__ void __launch_bounds__(NW * 32)
       if (lane == 0) out.loss_part[item] = d;
       if (loss_out && lane == 0) {
         __threadfence();
-        s_last = atomicAdd(done, 1) == (int)gridDim.x - 1;
+        s_last = atomicAdd(done, 1) == n_items - 1;
       }
     }
   }  // warp 0
@@ -535,7 +547,16 @@ __global__ void __launch_bounds__(NW * 32)
   if (!s_last) return;
   // the last block to finish sums the per-tile partials, all its threads
   __threadfence();
-  sum_partials_block<NW>(out.loss_part, (int)gridDim.x, loss_out);
+  sum_partials_block<NW>(out.loss_part, n_items, loss_out);
+}
+
+template <bool KAHAN, int NW, int CPL = 1, int LM = 1>
+__global__ void __launch_bounds__(NW * 32)
+    gr_project1d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap,
+                        int W, ProjOut out, double *loss_out, int *done,
+                        const float4 *__restrict__ pairs) {
+  project1d_body<KAHAN, NW, CPL, LM>(at, g, tc, bitmap, W, out, loss_out, done, pairs,
+                                     blockIdx.x, gridDim.x);
 }
 
 // ---- pixel-integrated operator: binning and projection -------------------
@@ -977,6 +998,47 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
+// ---- multi-problem launches (2D) -------------------------------------------
+// Blocks of problems whose fit has stopped return at once (the whole block).
+__global__ void __launch_bounds__(128)
+    gr_batch_bin_kernel(const BatchProb *__restrict__ probs, const int *__restrict__ off, int n,
+                        const int *__restrict__ active, int use_trial) {
+  const int p = batch_find(off, n, blockIdx.x);
+  if (!active[p]) return;
+  const BatchProb &B = probs[p];
+  const int lb = blockIdx.x - off[p];
+  const int bxn = (B.cur.n + 127) / 128;
+  bin_body<1>(use_trial ? B.trial : B.cur, B.g, B.tc, B.bitmap, B.W, B.pairs, lb % bxn,
+              lb / bxn);
+}
+
+__global__ void __launch_bounds__(kProjWarps * 32)
+    gr_batch_project_kernel(const BatchProb *__restrict__ probs, const int *__restrict__ off,
+                            int n, const int *__restrict__ active, int use_trial) {
+  const int p = batch_find(off, n, blockIdx.x);
+  if (!active[p]) return;
+  const BatchProb &B = probs[p];
+  project1d_body<true, kProjWarps>(use_trial ? B.trial : B.cur, B.g, B.tc, B.bitmap, B.W, B.out,
+                                   use_trial ? B.loss_trial : B.loss_cur, B.done, B.pairs,
+                                   blockIdx.x - off[p], B.items);
+}
+
+int launch_batch_bin(const BatchLaunch &b, int use_trial, cudaStream_t stream) {
+  if (b.grid_bin <= 0) return kOk;
+  gr_batch_bin_kernel<<<b.grid_bin, 128, 0, stream>>>(b.probs, b.off_bin, b.n, b.active,
+                                                      use_trial);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
+int launch_batch_project(const BatchLaunch &b, int use_trial, cudaStream_t stream) {
+  if (b.grid_proj <= 0) return kOk;
+  gr_batch_project_kernel<<<b.grid_proj, kProjWarps * 32, 0, stream>>>(
+      b.probs, b.off_proj, b.n, b.active, use_trial);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
 int preload_project() {
   return preload_fn(gr_bin_kernel<1>) + preload_fn(gr_bin_kernel<2>) +
          preload_fn(gr_psf_bin_kernel<1>) + preload_fn(gr_psf_bin_kernel<2>) +
@@ -990,7 +1052,8 @@ int preload_project() {
          preload_fn(gr_project1d_kernel<true, 8, 2, 2>) +
          preload_fn(gr_project1d_kernel<true, kProjWarps, 2>) +
          preload_fn(gr_psf_project_kernel<1>) + preload_fn(gr_psf_project_kernel<2>) +
-         preload_fn(gr_loss_finalize_kernel);
+         preload_fn(gr_loss_finalize_kernel) + preload_fn(gr_batch_bin_kernel) +
+         preload_fn(gr_batch_project_kernel);
 }
 
 }  // namespace gr

@@ -278,14 +278,16 @@ __device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, double
 // and |dtheta|.  lam (N) adds lam_j to the diagonal.  mask (nullable): atoms
 // with mask[j] == 0 keep their parameters.  One group of G lanes per atom;
 // after the solve lane l forms parameter l only.
+// The body of one 32-thread block (the launch's block; a multi-problem launch
+// maps its blocks to (problem, block)).
 template <int P, int D, int G>
-__global__ void __launch_bounds__(32)
-    gr_newton_solve_kernel(int n, const double *g, const double *H,
-                           const double *lam, const double *theta,
-                           const unsigned char *mask, double *theta_new,
-                           double *step_norm, int *fail, AtomOut ao) {
+__device__ __forceinline__ void solve_body(int n, const double *g, const double *H,
+                                           const double *lam, const double *theta,
+                                           const unsigned char *mask, double *theta_new,
+                                           double *step_norm, int *fail, const AtomOut &ao,
+                                           int block) {
   constexpr unsigned kAll = 0xffffffffu;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = block * 32 + (int)threadIdx.x;
   if ((t & ~31) / G >= n) return;       // whole warp past the last atom
   const int l = t & (G - 1);
   const int j = t / G;
@@ -365,6 +367,15 @@ __global__ void __launch_bounds__(32)
   }
 }
 
+template <int P, int D, int G>
+__global__ void __launch_bounds__(32)
+    gr_newton_solve_kernel(int n, const double *g, const double *H,
+                           const double *lam, const double *theta,
+                           const unsigned char *mask, double *theta_new,
+                           double *step_norm, int *fail, AtomOut ao) {
+  solve_body<P, D, G>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao, blockIdx.x);
+}
+
 // dst[e] = src[e] for e in [0, n), the grid's threads striding from t0 by
 // stride: float4 accesses when both arrays are 16-byte aligned, four of them
 // loaded before any is stored, so a thread keeps 64 bytes in flight (a
@@ -399,15 +410,18 @@ __device__ __forceinline__ void copy_field(const float *__restrict__ src, float 
 // takes the decision itself.  Block 0 writes loss_cur last, and the decision
 // does not change when another block reads loss_cur after that write (an
 // accepted trial then compares equal; a rejected one leaves it untouched).
-__global__ void __launch_bounds__(256)
-    gr_newton_accept_kernel(int n, int P, int pr, int dim, double *loss_cur,
-                            const double *loss_trial, double *theta,
-                            const double *theta_trial, double *lam, double lam_min,
-                            double lam_max, AtomOut cur, AtomIn trial, double *hist,
-                            int *hist_acc, int *counter, int hist_len, FieldCopy fc) {
+// The body of block `block` of `nblocks` 256-thread blocks (the launch's
+// grid; a multi-problem launch maps its blocks to (problem, block)).
+__device__ __forceinline__ void accept_body(int n, int P, int pr, int dim, double *loss_cur,
+                                            const double *loss_trial, double *theta,
+                                            const double *theta_trial, double *lam,
+                                            double lam_min, double lam_max, const AtomOut &cur,
+                                            const AtomIn &trial, double *hist, int *hist_acc,
+                                            int *counter, int hist_len, const FieldCopy &fc,
+                                            int block, int nblocks) {
   const bool acc = *loss_trial <= *loss_cur;
-  const int stride = gridDim.x * blockDim.x;
-  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = nblocks * 256;
+  const int t0 = block * 256 + (int)threadIdx.x;
   if (acc)
     for (int e = t0; e < n * P; e += stride) theta[e] = theta_trial[e];
   for (int j = t0; j < n; j += stride) {
@@ -434,6 +448,16 @@ __global__ void __launch_bounds__(256)
     }
     *counter = k + 1;
   }
+}
+
+__global__ void __launch_bounds__(256)
+    gr_newton_accept_kernel(int n, int P, int pr, int dim, double *loss_cur,
+                            const double *loss_trial, double *theta,
+                            const double *theta_trial, double *lam, double lam_min,
+                            double lam_max, AtomOut cur, AtomIn trial, double *hist,
+                            int *hist_acc, int *counter, int hist_len, FieldCopy fc) {
+  accept_body(n, P, pr, dim, loss_cur, loss_trial, theta, theta_trial, lam, lam_min, lam_max,
+              cur, trial, hist, hist_acc, counter, hist_len, fc, blockIdx.x, gridDim.x);
 }
 
 // After gr_newton_accept: when the trial was accepted (the accept kernel
@@ -501,13 +525,62 @@ int launch_newton_solve(int dim, int iso, int n, const double *g, const double *
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
 
+// ---- multi-problem launches (2D) -------------------------------------------
+template <int PP>
+__global__ void __launch_bounds__(32)
+    gr_batch_solve_kernel(const BatchProb *__restrict__ probs, const int *__restrict__ off, int n,
+                          const int *__restrict__ active) {
+  const int p = batch_find(off, n, blockIdx.x);
+  if (!active[p]) return;
+  const BatchProb &B = probs[p];
+  const AtomOut ao{const_cast<float *>(B.trial.I), const_cast<float *>(B.trial.x),
+                   const_cast<float *>(B.trial.r)};
+  solve_body<PP, 2, 8>(B.cur.n, B.dout.g, B.dout.H, B.lam, B.theta, nullptr, B.theta_trial,
+                       B.step, nullptr, ao, blockIdx.x - off[p]);
+}
+
+__global__ void __launch_bounds__(256)
+    gr_batch_accept_kernel(const BatchProb *__restrict__ probs, const int *__restrict__ off,
+                           int n, const int *__restrict__ active) {
+  const int p = batch_find(off, n, blockIdx.x);
+  if (!active[p]) return;
+  const BatchProb &B = probs[p];
+  const AtomOut cur{const_cast<float *>(B.cur.I), const_cast<float *>(B.cur.x),
+                    const_cast<float *>(B.cur.r)};
+  const AtomIn trial{B.trial.I, B.trial.x, B.trial.r};
+  const FieldCopy none{nullptr, nullptr, nullptr, nullptr, 0};
+  accept_body(B.cur.n, B.P, B.pr, 2, B.loss_cur, B.loss_trial, B.theta, B.theta_trial, B.lam,
+              B.lam_min, B.lam_max, cur, trial, B.hist, B.hist_acc, B.counter, B.hist_len, none,
+              blockIdx.x - off[p], off[p + 1] - off[p]);
+}
+
+int launch_batch_solve(const BatchLaunch &b, int P, cudaStream_t stream) {
+  if (b.grid_solve <= 0) return kOk;
+  if (P == 4)
+    gr_batch_solve_kernel<4><<<b.grid_solve, 32, 0, stream>>>(b.probs, b.off_solve, b.n, b.active);
+  else if (P == 6)
+    gr_batch_solve_kernel<6><<<b.grid_solve, 32, 0, stream>>>(b.probs, b.off_solve, b.n, b.active);
+  else
+    return kErrArg;
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
+int launch_batch_accept(const BatchLaunch &b, cudaStream_t stream) {
+  if (b.grid_acc <= 0) return kOk;
+  gr_batch_accept_kernel<<<b.grid_acc, 256, 0, stream>>>(b.probs, b.off_acc, b.n, b.active);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
+}
+
 int preload_update() {
   return preload_fn(gr_atom_update_kernel<1>) + preload_fn(gr_atom_update_kernel<2>) +
          preload_fn(gr_sum_partials_kernel) + preload_fn(gr_newton_solve_kernel<4, 2, 8>) +
          preload_fn(gr_newton_solve_kernel<6, 2, 8>) +
          preload_fn(gr_newton_solve_kernel<5, 3, 8>) +
          preload_fn(gr_newton_solve_kernel<10, 3, 16>) + preload_fn(gr_newton_accept_kernel) +
-         preload_fn(gr_accept_fields_kernel);
+         preload_fn(gr_accept_fields_kernel) + preload_fn(gr_batch_solve_kernel<4>) +
+         preload_fn(gr_batch_solve_kernel<6>) + preload_fn(gr_batch_accept_kernel);
 }
 
 }  // namespace gr

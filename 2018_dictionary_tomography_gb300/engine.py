@@ -701,6 +701,100 @@ class FitLoop:
             pass
 
 
+class BatchLoop:
+    """Several small 2D L2 damped-Newton fits as one device loop
+    (``gr_batch_*``): each kernel of an iteration is one launch over a table
+    of the problems, and a problem leaves the loop when its own stop test
+    (that of ``FitLoop``) says so.
+
+    ``members``: objects with the device buffers of one fit each --
+    ``cur``, ``trial`` (``DeviceAtoms``), ``geom``, ``data``, ``alpha_t``
+    (the fit fields), ``loss_cur``, ``loss_trial``, ``theta``,
+    ``theta_trial``, ``lam``, ``step``, ``f``, ``g``, ``H``, ``hist``,
+    ``hist_acc``, ``counter`` and ``req`` (``max_iter``, ``tol``,
+    ``lam_max``).  Raises ``EngineError`` when the members cannot share a
+    batch (``gr_batch_workspace_bytes`` is 0).  ``launch()`` runs the
+    prologue (fields and loss of every current atom set) and the loop on
+    ``stream``."""
+
+    def __init__(self, members, stream, setup_stream, device, max_reject, lam_min=1e-4):
+        lib = _lib.load()
+        self._lib = lib
+        self.stream = stream
+        self.handle = None
+        self.batch = None
+        n = len(members)
+        arr = (_lib.GrBatchMember * n)()
+        for a, m in zip(arr, members):
+            a.cur = m.cur.struct
+            a.trial = m.trial.struct
+            a.geom = m.geom.struct
+            a.data = m.data.data_ptr()
+            a.fields = m.alpha_t.data_ptr()
+            for name in ("loss_cur", "loss_trial", "theta", "theta_trial", "lam", "step", "f",
+                         "g", "H", "hist", "counter"):
+                setattr(a, name, getattr(m, name).data_ptr())
+            a.hist_acc = m.hist_acc.data_ptr()
+            a.hist_len = int(m.hist.numel())
+            a.max_iter = int(m.req.max_iter)
+            a.tol = float(m.req.tol)
+            a.lam_min = float(lam_min)
+            a.lam_max = float(m.req.lam_max)
+        self._members = arr
+        nb = int(lib.gr_batch_workspace_bytes(arr, n))
+        if nb == 0:
+            raise _lib.EngineError("these fits cannot share a batch")
+        self.ws = torch.empty(nb, dtype=torch.uint8, device=device)
+        h = ctypes.c_void_p()
+        _lib.check(lib.gr_batch_create(arr, n, self.ws.data_ptr(), nb, int(max_reject),
+                                       ctypes.c_void_p(setup_stream.cuda_stream),
+                                       ctypes.byref(h)), "gr_batch_create")
+        self.batch = h
+        self.guard = torch.zeros(1, dtype=torch.int32, device=device)
+        sh = ctypes.c_void_p(stream.cuda_stream)
+        loop = ctypes.c_void_p()
+        with torch.cuda.stream(stream):
+            _lib.check(lib.gr_fit_loop_begin(sh, self.guard.data_ptr(), ctypes.byref(loop)),
+                       "gr_fit_loop_begin")
+            self.handle = loop
+            rc = lib.gr_batch_iterate(self.batch, loop, sh)
+            rc2 = lib.gr_fit_loop_end_open(loop, sh)
+        if rc == 0:
+            rc = rc2
+        if rc == 0:
+            rc = lib.gr_fit_loop_instantiate(loop)
+        if rc != 0:
+            self.close()
+            _lib.check(rc, "gr_batch_iterate")
+
+    def prologue(self):
+        """Every member active; fit fields and loss of its current atoms."""
+        sh = ctypes.c_void_p(self.stream.cuda_stream)
+        _lib.check(self._lib.gr_batch_prologue(self.batch, sh), "gr_batch_prologue")
+
+    def launch_loop(self):
+        sh = ctypes.c_void_p(self.stream.cuda_stream)
+        _lib.check(self._lib.gr_fit_loop_launch(self.handle, sh), "gr_fit_loop_launch")
+
+    def launch(self):
+        self.prologue()
+        self.launch_loop()
+
+    def close(self):
+        if self.handle is not None and self.handle.value:
+            self._lib.gr_fit_loop_destroy(self.handle)
+        self.handle = None
+        if self.batch is not None and self.batch.value:
+            self._lib.gr_batch_destroy(self.batch)
+        self.batch = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 REG_KINDS = {"null": 0, "joubert": 1, "mass": 2, "volume": 3, "radius": 4, "iso": 5}
 
 

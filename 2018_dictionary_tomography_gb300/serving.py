@@ -43,6 +43,15 @@ flight (``exclusive_streams``): a stream runs its work in order, and a
 whole fit is one graph launch, so a request queued behind another on the
 same stream would wait for that entire fit however little work it has.
 
+Small 2D fits (up to 224 atoms, L2, no regulariser) that are admitted
+together run as one batched device loop (``engine.BatchLoop``, up to
+``batch_max`` fits): every kernel of an iteration is one launch over a table
+of the fits, each fit leaves the batch at its own stop test, and every fit
+ends bitwise where its own loop would (tests/test_serving_gpu.py).  On the
+512-request stream the batched and unbatched mixes finish within 1 % of each
+other (the mix is bound by device work, which batching does not change); the
+admission host time drops from 0.48 to 0.38 s (fewer graphs to build).
+
 The process should give every stream its own hardware work queue
 (environment ``CUDA_DEVICE_MAX_CONNECTIONS`` >= n_streams + 1, at most 32,
 set before CUDA starts): streams that share a queue are serialised the same
@@ -254,7 +263,7 @@ class _Slot:
     """Device state of one admitted request."""
 
     def __init__(self, req, stream, device, use_graph=True, iters_per_launch=4,
-                 device_loop=True, setup_stream=None, plans=(None, None)):
+                 device_loop=True, setup_stream=None, plans=(None, None), build_loop=True):
         self.req = req
         # launch schedules of this request's shape class (engine.Plan, or
         # None for the process-wide one): projection, derivatives
@@ -375,6 +384,12 @@ class _Slot:
             self.graph = None
             self.loop = None
             self.loss0 = None
+            if not build_loop:
+                # a member of a batch: the batch's loop runs its iterations
+                self.phase_seconds = {"host_prep": t_host - t_start, "buffers": t_bufs - t_host,
+                                      "streams": t_cap - t_bufs}
+                self.iterations_launched = 0
+                return
             if use_graph and device_loop:
                 # the whole fit as one graph: the iteration repeats on the
                 # device until the device-side stop test ends it
@@ -477,13 +492,23 @@ class _Slot:
         torch.sum(self.reg_f, dim=0, out=self.reg_sum)
         loss.add_(self.reg_sum)
 
-    def _copy_back(self):
+    def _copy_results(self):
         self.h_counter.copy_(self.counter, non_blocking=True)
         self.h_hist.copy_(self.hist, non_blocking=True)
         self.h_acc.copy_(self.hist_acc, non_blocking=True)
         self.h_theta.copy_(self.theta, non_blocking=True)
         self.h_loss.copy_(self.loss_cur.reshape(1), non_blocking=True)
+
+    def _copy_back(self):
+        self._copy_results()
         self.event.record(self.stream)
+
+    @property
+    def reqs(self):
+        return [self.req]
+
+    def result_map(self):
+        return {self.req.id: self.result()}
 
     def launch(self):
         if self.loop is not None:
@@ -540,6 +565,70 @@ class _Slot:
                 "status": "ok" if accepted > 0 else "no_progress"}
 
 
+def batchable(req):
+    """Whether a request can run in a batch of small 2D fits (a shared
+    engine.BatchLoop): 2D, L2, no regulariser, at most 224 atoms and 8192
+    (angle, 32-cell tile) items.  The engine checks the rest."""
+    if len(req.detector) != 1 or req.fit != "l2" or req.reg is not None:
+        return False
+    n = len(req.init[0])
+    tiles = -(-len(np.asarray(req.detector[0]).reshape(-1)) // 32)
+    return 1 <= n <= 224 and len(req.orientations) * tiles <= 8192
+
+
+def _r_layout(req):
+    return np.asarray(req.init[2]).reshape(len(req.init[0]), -1).shape[1]
+
+
+class _BatchSlot:
+    """Small 2D fits admitted together: each keeps its own buffers (a _Slot
+    built without a loop of its own) and one engine.BatchLoop runs all their
+    iterations, every kernel of an iteration one launch over the batch.  A
+    request's result is the one its own device loop gives (the batch runs
+    the same block bodies on the same buffers)."""
+
+    def __init__(self, reqs, stream, device, setup_stream):
+        t0 = time.perf_counter()
+        self.stream = stream
+        self.members = [_Slot(r, stream, device, True, 1, True, setup_stream, (None, None),
+                              build_loop=False) for r in reqs]
+        t1 = time.perf_counter()
+        self.loop = engine.BatchLoop(self.members, stream, setup_stream, device, MAX_BACKTRACK)
+        self.phase_seconds = {}
+        for m in self.members:
+            for k, v in m.phase_seconds.items():
+                self.phase_seconds[k] = self.phase_seconds.get(k, 0.0) + v
+        self.phase_seconds["batch_loop"] = time.perf_counter() - t1
+        self.phase_seconds["batch_members"] = t1 - t0
+        with torch.cuda.stream(stream):
+            self.event = torch.cuda.Event()
+        self.req = reqs[0]
+
+    @property
+    def reqs(self):
+        return [m.req for m in self.members]
+
+    def launch(self):
+        with torch.cuda.stream(self.stream):
+            self.loop.prologue()
+            for m in self.members:
+                m.h_loss0.copy_(m.loss_cur.reshape(1), non_blocking=True)
+            self.loop.launch_loop()
+            for m in self.members:
+                m._copy_results()
+            self.event.record(self.stream)
+
+    def done(self):
+        return True
+
+    def result_map(self):
+        return {m.req.id: m.result() for m in self.members}
+
+    def release(self):
+        for m in self.members:
+            m.release()
+
+
 _warmed = set()
 
 
@@ -576,7 +665,7 @@ class GaussFitServer:
 
     def __init__(self, device=None, max_slots=32, n_streams=16, hbm_budget=None,
                  hbm_reserve=4 << 30, use_graphs=True, iters_per_launch=4, device_loop=True,
-                 largest_first=False, exclusive_streams=True, tuned=False):
+                 largest_first=False, exclusive_streams=True, tuned=False, batch_max=8):
         self.dev = torch.device(device or "cuda")
         engine._require_cuda(self.dev)
         self.max_slots = max_slots
@@ -613,6 +702,10 @@ class GaussFitServer:
         self.cancelled = set()       # ids of requests cancelled while in flight
         self.errors = {}             # id -> reason, for requests that could not run
         self._admit_fault = None     # test hook: called before a slot is built
+        # small 2D fits admitted together share one batched device loop (up
+        # to batch_max per batch; 1: every fit runs its own loop)
+        self.batch_max = batch_max if (device_loop and use_graphs) else 1
+        self.batches = 0
         _warm_engine(self.dev)
 
     @staticmethod
@@ -646,7 +739,7 @@ class GaussFitServer:
                 self.pending.remove(req)
                 self.results[rid] = {"status": "cancelled", "arrival": req.arrival}
                 return True
-        if any(slot.req.id == rid for slot in self.active):
+        if any(r.id == rid for slot in self.active for r in slot.reqs):
             self.cancelled.add(rid)
             return True
         return False
@@ -693,15 +786,41 @@ class GaussFitServer:
                                       % (req.id, need, self.budget))
                 break
             self.pending.popleft()
+            group = [req]
+            if self.batch_max > 1 and batchable(req):
+                # the other arrived requests that can share its batch, in
+                # queue order, as long as the budget holds
+                for r in list(self.pending):
+                    if len(group) >= self.batch_max or r.arrival > now:
+                        break
+                    if batchable(r) and _r_layout(r) == _r_layout(req):
+                        nr = self.estimate_bytes(r)
+                        if self.in_use + need + nr > self.budget:
+                            break
+                        group.append(r)
+                        need += nr
+                for r in group[1:]:
+                    self.pending.remove(r)
             ta = time.perf_counter()
             try:
                 if self._admit_fault is not None:
                     self._admit_fault(req)
-                slot = _Slot(req, self.streams[si], self.dev, self.use_graphs, self.k,
-                             self.device_loop, self.setup_stream, self._plans(req))
+                if len(group) > 1 or (self.batch_max > 1 and batchable(req)):
+                    slot = _BatchSlot(group, self.streams[si], self.dev, self.setup_stream)
+                    self.batches += 1
+                else:
+                    slot = _Slot(req, self.streams[si], self.dev, self.use_graphs, self.k,
+                                 self.device_loop, self.setup_stream, self._plans(req))
             except _lib.EngineError as e:
-                # the engine refused the request's set-up: it cannot run
                 self.admit_seconds += time.perf_counter() - ta
+                if len(group) > 1:
+                    # the batch could not be built: its requests go back to
+                    # the head of the queue and run one fit per loop
+                    for r in reversed(group):
+                        self.pending.appendleft(r)
+                    self.batch_max = 1
+                    continue
+                # the engine refused the request's set-up: it cannot run
                 self.errors[req.id] = "%s: %s" % (type(e).__name__, e)
                 self.results[req.id] = {"status": "error", "error": self.errors[req.id],
                                         "arrival": req.arrival}
@@ -712,12 +831,16 @@ class GaussFitServer:
                 # fits in flight it waits (at the head of the queue) until
                 # one finishes; with none it can never fit.
                 self.admit_seconds += time.perf_counter() - ta
-                if not self.active:
+                if not self.active and len(group) == 1:
                     self.errors[req.id] = "%s: %s" % (type(e).__name__, e)
                     self.results[req.id] = {"status": "error", "error": self.errors[req.id],
                                             "arrival": req.arrival}
                     continue
-                self.pending.appendleft(req)
+                for r in reversed(group):
+                    self.pending.appendleft(r)
+                if not self.active:
+                    self.batch_max = 1       # alone the fits may still fit
+                    continue
                 self.admission_retries += 1
                 self._hold_admission = True
                 break
@@ -726,13 +849,13 @@ class GaussFitServer:
                 self.admitted_while_busy += 1
             self.admit_seconds += time.perf_counter() - ta
             phases = dict(slot.phase_seconds)
-            if slot.loop is not None:
+            if slot.loop is not None and hasattr(slot.loop, "seconds"):
                 phases.update(slot.loop.seconds)
             for k, v in phases.items():
                 self.admit_phases[k] = self.admit_phases.get(k, 0.0) + v
             slot.stream_index = si
             if slot.loop is not None:
-                self.device_loops += 1
+                self.device_loops += len(slot.reqs)
             slot.need = need
             slot.t_admit = time.perf_counter()
             self.in_use += need
@@ -751,16 +874,21 @@ class GaussFitServer:
                 if not slot.event.query():
                     continue
                 progressed = True
-                if slot.done() or slot.req.id in self.cancelled:
-                    res = slot.result()
-                    if slot.req.id in self.cancelled:
-                        self.cancelled.discard(slot.req.id)
-                        res = {"status": "cancelled"}
-                    res["arrival"] = slot.req.arrival
-                    res["admitted"] = slot.t_admit - t0
-                    res["finish"] = time.perf_counter() - t0
-                    res["latency"] = res["finish"] - slot.req.arrival
-                    self.results[slot.req.id] = res
+                if slot.done() or any(r.id in self.cancelled for r in slot.reqs):
+                    fin = time.perf_counter() - t0
+                    done_reqs = []
+                    all_res = slot.result_map()
+                    for r in slot.reqs:
+                        res = all_res[r.id]
+                        if r.id in self.cancelled:
+                            self.cancelled.discard(r.id)
+                            res = {"status": "cancelled"}
+                        res["arrival"] = r.arrival
+                        res["admitted"] = slot.t_admit - t0
+                        res["finish"] = fin
+                        res["latency"] = fin - r.arrival
+                        self.results[r.id] = res
+                        done_reqs.append((r, res))
                     self.active.remove(slot)
                     self._hold_admission = False
                     self.in_use -= slot.need
@@ -770,7 +898,8 @@ class GaussFitServer:
                         slot.loop = None
                     slot.release()
                     if on_done:
-                        on_done(slot.req, res)
+                        for r, res in done_reqs:
+                            on_done(r, res)
                     del slot
                     if not self.active and self.pending:
                         self._release_loops()

@@ -466,6 +466,60 @@ int gr_fit_loop_instantiate(void *loop);
 int gr_fit_loop_launch(void *loop, void *stream);
 int gr_fit_loop_destroy(void *loop);
 
+/* ---- batches of small 2D fits ------------------------------------------
+ * Several 2D L2 damped-Newton fits run as one device loop in which every
+ * kernel of an iteration is one launch over a table of the problems (each
+ * kernel maps its blocks to (problem, block of that problem) and runs the
+ * block body of the problem's own launch, so every problem gets the results
+ * of its own loop): the launches and graph nodes an iteration costs are
+ * shared by the batch.  A problem leaves the batch when its own stop test
+ * (as gr_fit_loop_end's) says so; the loop ends when none is left.
+ * Replaces, for small problems, one gr_fit_loop per problem; the reference
+ * fits one problem at a time from the host (NewtonGaussian.py:18-109).
+ *
+ * A member is a 2D problem (geom.kdet 1) of n_atoms <= 224, every member of
+ * a batch with the same r layout (isotropic: P = 4, else P = 6), at most 8192
+ * (angle, 32-cell tile) items, whose derivative split gives every lane one
+ * angle; gr_batch_workspace_bytes returns 0 for members that cannot be
+ * batched.  Buffers as gr_newton_solve / gr_newton_accept use them; `fields`
+ * holds the residual field of the latest projection (the current atoms' after
+ * an accepted trial, which is when the derivatives read it).
+ *
+ *   gr_batch_create(members, n, ws, ws_bytes, max_reject, stream, &batch)
+ *       lays the batch out in ws (gr_batch_workspace_bytes) and copies its
+ *       tables (waits for that copy);
+ *   gr_batch_prologue(batch, stream)  all members active, fields and
+ *       loss_cur of their current atoms (before every launch of the loop);
+ *   the loop: gr_fit_loop_begin(stream, guard, &loop),
+ *       gr_batch_iterate(batch, loop, stream) (captured: derivatives, solves,
+ *       trial projection, accept, batch stop test), gr_fit_loop_end_open(loop,
+ *       stream) (no single-problem stop test), gr_fit_loop_instantiate,
+ *       gr_fit_loop_launch;
+ *   gr_batch_destroy(batch)  (the workspace stays the caller's). */
+typedef struct gr_batch_member {
+  gr_atoms cur;          /* current atoms (accepted steps update them) */
+  gr_atoms trial;        /* trial atoms, same layout */
+  gr_geometry geom;      /* 2D */
+  const float *data;     /* data sinogram (n_angles, n_det) */
+  float *fields;         /* residual field of the latest projection */
+  double *loss_cur, *loss_trial;
+  double *theta, *theta_trial;  /* (n, P) FP64 parameters [I, x, r] */
+  double *lam, *step;           /* (n) damping, step norms */
+  double *f, *g, *H;            /* (n), (n, P), (n, P, P) derivatives */
+  double *hist;          /* (hist_len) loss after each iteration */
+  int *hist_acc;         /* (hist_len) 1: accepted, 0: rejected */
+  int *counter;          /* iterations done (zero before the first launch) */
+  int hist_len, max_iter;
+  double tol, lam_min, lam_max;
+} gr_batch_member;
+size_t gr_batch_workspace_bytes(const gr_batch_member *members, int n);
+int gr_batch_create(const gr_batch_member *members, int n, void *ws, size_t ws_bytes,
+                    int max_reject, void *stream, void **batch);
+int gr_batch_prologue(void *batch, void *stream);
+int gr_batch_iterate(void *batch, void *loop, void *stream);
+int gr_fit_loop_end_open(void *loop, void *stream);
+int gr_batch_destroy(void *batch);
+
 /*
  * Kernel timers (no counterpart in the reference; measurement only).  While
  * enabled, CUDA events are recorded on the launching stream around each

@@ -137,3 +137,38 @@ def test_plan_create_set_get_without_gpu():
             lib.gr_workspace_bytes(2, ctypes.byref(at), ctypes.byref(g)))
     assert lib.gr_plan_destroy(h) == 0
     assert lib.gr_radproj_plan(None, ctypes.byref(at), ctypes.byref(g), None, None, 0, None) == -1
+
+
+def test_batch_layout_without_gpu():
+    """gr_batch_workspace_bytes: sizes only (no pointer is dereferenced); a
+    member that cannot be batched (3D, or 8 bitmap words and more) gives 0."""
+    lib_mod = importlib.import_module("2018_dictionary_tomography_gb300._lib")
+    lib = lib_mod.load()
+
+    def member(n, kdet=1, A=30, D=64, iso=1):
+        m = lib_mod.GrBatchMember()
+        for at in (m.cur, m.trial):
+            at.n_atoms, at.I, at.x, at.r, at.r_iso = n, 16, 16, 16, iso
+        m.geom.kdet, m.geom.n_angles, m.geom.frames = kdet, A, 16
+        for k in range(kdet):
+            m.geom.n_det[k], m.geom.det[k] = D, 16
+            m.geom.det_first[k], m.geom.det_inv_step[k] = -1.0, D / 2.0
+        for name in ("data", "fields", "loss_cur", "loss_trial", "theta", "theta_trial", "lam",
+                     "step", "f", "g", "H", "hist", "hist_acc", "counter"):
+            setattr(m, name, 16)
+        m.hist_len, m.max_iter, m.tol, m.lam_min, m.lam_max = 120, 100, 1e-6, 1e-4, 1e8
+        return m
+
+    arr = (lib_mod.GrBatchMember * 3)(member(20), member(100, A=50), member(7, D=300))
+    one = lib.gr_batch_workspace_bytes(arr, 1)
+    three = lib.gr_batch_workspace_bytes(arr, 3)
+    assert one > 0 and three > one and three % 256 == 0
+    assert lib.gr_batch_workspace_bytes((lib_mod.GrBatchMember * 1)(member(300)), 1) == 0
+    assert lib.gr_batch_workspace_bytes((lib_mod.GrBatchMember * 1)(member(20, kdet=2)), 1) == 0
+    bad = member(20)
+    bad.counter = None
+    assert lib.gr_batch_workspace_bytes((lib_mod.GrBatchMember * 1)(bad), 1) == 0
+    h = ctypes.c_void_p()
+    assert lib.gr_batch_create(arr, 0, None, 0, 8, None, ctypes.byref(h)) == -1
+    assert lib.gr_batch_create(arr, 3, None, 0, 8, None, ctypes.byref(h)) == -1
+    assert lib.gr_batch_destroy(None) == 0

@@ -281,3 +281,52 @@ def test_regularised_served_fit_matches_plain_fit(cuda_ready):
         assert abs(served[k]["loss"] - plain[k]["loss"]) <= 1e-12 * abs(plain[k]["loss"])
         # the regulariser changed the fit
         assert served[k]["loss"] != bare[k]["loss"]
+
+
+def _small_2d(n=8, seed=21):
+    return workloads.config3_requests(n=n, rate=1e9, seed=seed, p2d=1.0, atoms=(8, 150),
+                                      angles=(10, 40), det=(24, 96), max_iter=40, tol=1e-6)
+
+
+def test_batched_small_fits_equal_their_own_loops(cuda_ready):
+    """Small 2D fits admitted together run as one batched device loop
+    (engine.BatchLoop: each kernel one launch over the batch's table of
+    problems); every fit ends exactly where its own device loop ends."""
+    def run(batch_max):
+        srv = serving.GaussFitServer(max_slots=16, n_streams=4, batch_max=batch_max)
+        for r in _small_2d():
+            r.arrival = 0.0
+            srv.submit(r)
+        res = srv.run()
+        srv.close()
+        return srv, res
+    s1, own = run(1)
+    s8, batched = run(32)
+    assert s1.batches == 0 and s8.batches >= 1
+    assert set(own) == set(batched)
+    for k in own:
+        a, b = own[k], batched[k]
+        assert a["iterations"] == b["iterations"] and a["accepted"] == b["accepted"]
+        assert np.array_equal(a["theta"], b["theta"])
+        assert a["loss"] == b["loss"] and a["loss0"] == b["loss0"]
+
+
+def test_batch_members_alone_equal_members_in_a_batch(cuda_ready):
+    """A batchable fit alone (a batch of one) and among others: the same."""
+    alone = {}
+    for r in _small_2d(n=5, seed=22):
+        r.arrival = 0.0
+        srv = serving.GaussFitServer(max_slots=1, n_streams=1)
+        srv.submit(r)
+        alone.update(srv.run())
+        srv.close()
+    srv = serving.GaussFitServer(max_slots=8, n_streams=2)
+    for r in _small_2d(n=5, seed=22):
+        r.arrival = 0.0
+        srv.submit(r)
+    mix = srv.run()
+    srv.close()
+    assert srv.batches >= 1
+    for k in alone:
+        assert np.array_equal(alone[k]["theta"], mix[k]["theta"])
+        assert alone[k]["iterations"] == mix[k]["iterations"]
