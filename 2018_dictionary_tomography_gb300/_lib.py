@@ -76,7 +76,8 @@ EXPORTS = ("gr_version", "gr_preload", "gr_status_string", "gr_workspace_bytes",
            "gr_plan_create", "gr_plan_destroy", "gr_plan_set", "gr_plan_get",
            "gr_plan_workspace_bytes", "gr_radproj_plan", "gr_fit_forward_plan",
            "gr_atom_derivs_plan", "gr_batch_workspace_bytes", "gr_batch_create",
-           "gr_batch_prologue", "gr_batch_iterate", "gr_fit_loop_end_open", "gr_batch_destroy")
+           "gr_batch_prologue", "gr_batch_iterate", "gr_fit_loop_end_open", "gr_batch_destroy",
+           "gr_fit_items", "gr_fit_empty_loss", "gr_fit_forward_skip")
 
 _lock = threading.Lock()
 _lib = None
@@ -224,6 +225,15 @@ def load(build_if_missing=True):
         lib.gr_fit_forward_plan.argtypes = [vp] + lib.gr_fit_forward.argtypes
         lib.gr_atom_derivs_plan.restype = ctypes.c_int
         lib.gr_atom_derivs_plan.argtypes = [vp] + lib.gr_atom_derivs.argtypes
+        lib.gr_fit_items.restype = ctypes.c_int
+        lib.gr_fit_items.argtypes = [vp, P(GrGeometry), P(ctypes.c_size_t)]
+        lib.gr_fit_empty_loss.restype = ctypes.c_int
+        lib.gr_fit_empty_loss.argtypes = [vp, P(GrAtoms), P(GrGeometry), ctypes.c_int, vp,
+                                          ctypes.c_float, vp, vp, ctypes.c_size_t, vp]
+        lib.gr_fit_forward_skip.restype = ctypes.c_int
+        lib.gr_fit_forward_skip.argtypes = [vp, P(GrAtoms), P(GrGeometry), ctypes.c_int, vp,
+                                            ctypes.c_float, vp, vp, vp, vp, vp, ctypes.c_size_t,
+                                            vp]
         _lib = lib
         return lib
 

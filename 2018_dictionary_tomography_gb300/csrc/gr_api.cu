@@ -169,7 +169,8 @@ static int fit_forward_impl(const gr_atoms *atoms, const gr_geometry *geom, int 
                             const float *data, float background, float *R, float *alpha,
                             float *beta, double *loss, void *workspace,
                             size_t workspace_bytes, void *stream, int psf,
-                            const Tuning &t = g_tuning) {
+                            const Tuning &t = g_tuning, int empty_mode = kEmptyNone,
+                            double *empty_loss = nullptr) {
   Atoms at;
   Geom g;
   int st;
@@ -186,6 +187,10 @@ static int fit_forward_impl(const gr_atoms *atoms, const gr_geometry *geom, int 
   o.alpha = alpha;
   o.beta = beta;
   o.psf = psf;
+  o.empty_mode = empty_mode;
+  o.empty_loss = empty_loss;
+  if (empty_mode != kEmptyNone && (g.K != 2 || psf || R || fit == GR_FIT_NONE || !empty_loss))
+    return GR_ERR_ARG;
   return launch_project(at, g, o, loss, workspace, workspace_bytes,
                         static_cast<cudaStream_t>(stream), t);
 }
@@ -458,6 +463,35 @@ int gr_fit_forward_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geo
   if (!plan) return GR_ERR_ARG;
   return fit_forward_impl(atoms, geom, fit, data, background, R, alpha, beta, loss, workspace,
                           workspace_bytes, stream, 0, plan->t);
+}
+
+int gr_fit_items(const gr_plan *plan, const gr_geometry *geom, size_t *n_items) {
+  if (!n_items) return GR_ERR_ARG;
+  *n_items = 0;
+  gr_atoms none{};
+  Atoms at;
+  Geom g;
+  int st;
+  if (!to_internal(&none, geom, at, g, &st)) return st;
+  *n_items = project_skip_items(g, 0, plan ? plan->t : g_tuning);
+  return GR_OK;
+}
+
+int gr_fit_empty_loss(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                      int fit, const float *data, float background, double *empty_loss,
+                      void *workspace, size_t workspace_bytes, void *stream) {
+  return fit_forward_impl(atoms, geom, fit, data, background, nullptr, nullptr, nullptr, nullptr,
+                          workspace, workspace_bytes, stream, 0, plan ? plan->t : g_tuning,
+                          kEmptyRecord, empty_loss);
+}
+
+int gr_fit_forward_skip(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                        int fit, const float *data, float background, float *alpha,
+                        float *beta, double *loss, const double *empty_loss, void *workspace,
+                        size_t workspace_bytes, void *stream) {
+  return fit_forward_impl(atoms, geom, fit, data, background, nullptr, alpha, beta, loss,
+                          workspace, workspace_bytes, stream, 0, plan ? plan->t : g_tuning,
+                          kEmptySkip, const_cast<double *>(empty_loss));
 }
 
 int gr_atom_derivs_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,

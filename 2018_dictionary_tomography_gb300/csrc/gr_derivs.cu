@@ -282,11 +282,13 @@ __device__ __forceinline__ void pair_moments(const Pair<K> &p, const Geom &g,
 // costs idle lanes on narrow ones (Tuning key 8; measured: 2936 atoms x 148
 // angles of 493^2 cells 460 -> 408 us, config 2's atoms 192 -> 200 us; 16
 // instead of 8 cells slowed every 2D Hessian measured, by up to 25 %)
-// The body of one 128-thread block (the launch's block; a multi-problem
-// launch maps its blocks to (problem, block)).
+// The body of one block whose first warp is warp0 of the launch's warps
+// (warp w takes the w-th (atom group, angle chunk); a multi-problem launch
+// maps its blocks to (problem, first warp)).  What a warp computes depends on
+// its warp index only, so the block size changes no result.
 template <int K, int ORDER, bool ONE, bool WIDE = false>
 __device__ __forceinline__ void deriv_body(const Atoms &at, const Geom &g, const DerivIn &in,
-                                           const DerivCfg &cfg, float *part, int block) {
+                                           const DerivCfg &cfg, float *part, int warp0) {
   constexpr int D = K + 1;
   constexpr int PR = n_rparam<K>();
   constexpr int P = n_par<K>();
@@ -295,7 +297,7 @@ __device__ __forceinline__ void deriv_body(const Atoms &at, const Geom &g, const
   constexpr int DEG = ORDER == 1 ? 2 : 4;
   constexpr int NH = P * (P + 1) / 2;
   constexpr bool GN = ORDER > 1;
-  const int gw = (block * 128 + (int)threadIdx.x) >> 5;
+  const int gw = warp0 + ((int)threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   const int warps_atoms = (at.n + cfg.ag - 1) / cfg.ag;
   if (gw >= warps_atoms * cfg.nchunks) return;
@@ -406,11 +408,17 @@ __device__ __forceinline__ void deriv_body(const Atoms &at, const Geom &g, const
   }
 }
 
-template <int K, int ORDER, bool ONE, bool WIDE = false>
-__global__ void __launch_bounds__(128, ORDER == 1 ? GR_GRAD_MIN_BLOCKS
-                                           : (ONE ? (K == 1 ? GR_HESS2D_MIN_BLOCKS : 3) : 1))
+// BW warps per block.  With one-warp blocks a warp that finishes frees its
+// slot at once; with four, a block holds its slot until its slowest warp
+// (the one with the widest supports) is done, which lowers the resident
+// warps of the register-limited Hessian kernels (Tuning key 9).
+template <int K, int ORDER, bool ONE, bool WIDE = false, int BW = 4>
+__global__ void __launch_bounds__(BW * 32,
+                                  (ORDER == 1 ? GR_GRAD_MIN_BLOCKS
+                                              : (ONE ? (K == 1 ? GR_HESS2D_MIN_BLOCKS : 3) : 1)) *
+                                      4 / BW)
     gr_deriv_kernel(Atoms at, Geom g, DerivIn in, DerivCfg cfg, float *part) {
-  deriv_body<K, ORDER, ONE, WIDE>(at, g, in, cfg, part, blockIdx.x);
+  deriv_body<K, ORDER, ONE, WIDE>(at, g, in, cfg, part, (int)blockIdx.x * BW);
 }
 
 // Pixel-integrated operator: per cell, the quadrature points' moments give
@@ -764,6 +772,10 @@ int tuning_set(Tuning &t, int key, int value) {
     t.deriv_wide_rows = value;
     return kOk;
   }
+  if (key == 9 && (value == 1 || value == 4)) {
+    t.deriv_block_warps = value;
+    return kOk;
+  }
   return kErrArg;
 }
 
@@ -772,7 +784,7 @@ int tuning_get(const Tuning &t, int key) {
          : key == 2 ? t.deriv_atoms_per_warp : key == 3 ? t.proj_form
          : key == 4 ? t.proj_split_cells
          : key == 6 ? t.deriv_split_lanes : key == 7 ? t.deriv_one_mb
-         : key == 8 ? t.deriv_wide_rows : -1;
+         : key == 8 ? t.deriv_wide_rows : key == 9 ? t.deriv_block_warps : -1;
 }
 
 size_t derivs_workspace_bytes(int K, int n_atoms, int n_angles, int order, const Tuning &t) {
@@ -810,6 +822,9 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
   const int warps = ((at.n + c.ag - 1) / c.ag) * c.nchunks;
   const int blocks = (warps + 3) / 4;
   const float s = 0.5f / g.ax[0].inv_step;  // cell half-width (pixel-integrated operator)
+  // one-warp blocks (Tuning key 9) for the kernels with one angle per lane
+  const bool bw1 = t.deriv_block_warps == 1;
+  const int blocks1 = warps;
   timer_mark(2, 0, stream);
   if (in.psf) {
     if (K == 1) {
@@ -829,18 +844,27 @@ int launch_derivs(const Atoms &at, const Geom &g, const DerivIn &in,
         if (one) gr_deriv_kernel<1, 1, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
         else gr_deriv_kernel<1, 1, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
       } else {
-        if (one) gr_deriv_kernel<1, 2, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+        if (one && bw1)
+          gr_deriv_kernel<1, 2, true, false, 1><<<blocks1, 32, 0, stream>>>(at, g, in, c, part);
+        else if (one) gr_deriv_kernel<1, 2, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
         else gr_deriv_kernel<1, 2, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
       }
     } else {
       if (in.order == 1) {
-        if (one) gr_deriv_kernel<2, 1, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+        if (one && bw1)
+          gr_deriv_kernel<2, 1, true, false, 1><<<blocks1, 32, 0, stream>>>(at, g, in, c, part);
+        else if (one) gr_deriv_kernel<2, 1, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
         else gr_deriv_kernel<2, 1, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
       } else if (wide) {
-        if (one) gr_deriv_kernel<2, 2, true, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+        if (one && bw1)
+          gr_deriv_kernel<2, 2, true, true, 1><<<blocks1, 32, 0, stream>>>(at, g, in, c, part);
+        else if (one)
+          gr_deriv_kernel<2, 2, true, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
         else gr_deriv_kernel<2, 2, false, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
       } else {
-        if (one) gr_deriv_kernel<2, 2, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
+        if (one && bw1)
+          gr_deriv_kernel<2, 2, true, false, 1><<<blocks1, 32, 0, stream>>>(at, g, in, c, part);
+        else if (one) gr_deriv_kernel<2, 2, true><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
         else gr_deriv_kernel<2, 2, false><<<blocks, 128, 0, stream>>>(at, g, in, c, part);
       }
     }
@@ -873,7 +897,7 @@ __global__ void __launch_bounds__(128, GR_HESS2D_MIN_BLOCKS)
   const int p = batch_find(off, n, blockIdx.x);
   const BatchProb &B = probs[p];
   if (!batch_derivs_wanted(B, active[p])) return;
-  deriv_body<1, 2, true>(B.cur, B.g, B.din, B.cfg, B.part, blockIdx.x - off[p]);
+  deriv_body<1, 2, true>(B.cur, B.g, B.din, B.cfg, B.part, ((int)blockIdx.x - off[p]) * 4);
 }
 
 __global__ void __launch_bounds__(kFinThreads)
@@ -904,6 +928,10 @@ int preload_derivs() {
          preload_fn(gr_deriv_kernel<2, 1, true>) + preload_fn(gr_deriv_kernel<2, 2, true>) +
          preload_fn(gr_deriv_kernel<2, 2, false, true>) +
          preload_fn(gr_deriv_kernel<2, 2, true, true>) +
+         preload_fn(gr_deriv_kernel<1, 2, true, false, 1>) +
+         preload_fn(gr_deriv_kernel<2, 1, true, false, 1>) +
+         preload_fn(gr_deriv_kernel<2, 2, true, false, 1>) +
+         preload_fn(gr_deriv_kernel<2, 2, true, true, 1>) +
          preload_fn(gr_psf_deriv_kernel<1, 1>) + preload_fn(gr_psf_deriv_kernel<1, 2>) +
          preload_fn(gr_psf_deriv_kernel<2, 1>) + preload_fn(gr_psf_deriv_kernel<2, 2>) +
          preload_fn(gr_deriv_finalize_kernel<1>) + preload_fn(gr_deriv_finalize_kernel<2>) +

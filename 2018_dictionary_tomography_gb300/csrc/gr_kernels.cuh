@@ -38,7 +38,14 @@ struct ProjOut {
   float *beta;         // Gauss-Newton weight field (KL, nullable)
   double *loss_part;   // per-(angle, tile) loss partials (set by the launcher)
   int psf;             // 1: pixel-integrated values (point-spread operator)
+  // Items no atom meets (point-sampled 3D only; R not written):
+  // kEmptyRecord writes every item's loss with no atom in it to empty_loss
+  // and no field; kEmptySkip gives an item whose bitmap is empty the loss
+  // recorded in empty_loss and leaves its fields unwritten.
+  int empty_mode;
+  double *empty_loss;
 };
+enum EmptyMode : int { kEmptyNone = 0, kEmptyRecord = 1, kEmptySkip = 2 };
 
 // ---- derivatives -----------------------------------------------------------
 enum DerivMode : int {
@@ -87,12 +94,16 @@ struct Tuning {
   int deriv_split_lanes = 65536;    // key 6
   int deriv_one_mb = 1024;          // key 7
   int deriv_wide_rows = 0;          // key 8 (1: 3D Hessian rows in 8-cell chunks)
+  int deriv_block_warps = 1;        // key 9 (warps per block, one-angle-per-lane kernels)
 };
 extern Tuning g_tuning;
 int tuning_set(Tuning &t, int key, int value);
 int tuning_get(const Tuning &t, int key);
 
 TileCfg make_tiles(int K, int D0, int D1, int rows);
+// (angle, tile) items of a forward that can skip items no atom meets (the
+// point-sampled 3D projection under t's tiling; 0 for the others)
+size_t project_skip_items(const Geom &g, int psf, const Tuning &t = g_tuning);
 size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1,
                                const Tuning &t = g_tuning);
 int launch_project(const Atoms &at, const Geom &g, const ProjOut &o,

@@ -168,6 +168,22 @@ __global__ void __launch_bounds__(kProjWarps * 32)
     item = s_item;
     if (item >= n_items) break;  // whole block leaves together
   }
+  if (out.empty_mode == kEmptySkip) {
+    // an item that no atom meets takes its recorded loss and writes no field
+    // (its cells would all be zero): no accumulator clear, data read or store
+    const uint32_t *wds = bitmap + (size_t)item * W;
+    int nz = 0;
+    for (int wi = NW == 1 ? lane : (int)threadIdx.x; wi < W; wi += NW * 32)
+      nz |= wds[wi] != 0u ? 1 : 0;
+    bool empty;
+    if constexpr (NW == 1) empty = !__any_sync(0xffffffffu, nz);
+    else empty = !__syncthreads_or(nz);  // every thread has read s_item
+    if (empty) {
+      if (out.loss_part && (NW == 1 ? lane : (int)threadIdx.x) == 0)
+        out.loss_part[item] = out.empty_loss[item];
+      continue;
+    }
+  }
   const int a = item / tc.ntiles, t = item - a * tc.ntiles;
   const int tr = t / tc.nt1, tcix = t - tr * tc.nt1;
   const int r0 = tr * ROWS, c0 = tcix * 32;
@@ -871,6 +887,12 @@ TileCfg make_tiles(int K, int D0, int D1, int rows) {
   return tc;
 }
 
+size_t project_skip_items(const Geom &g, int psf, const Tuning &t) {
+  if (g.K != 2 || psf) return 0;
+  const TileCfg tc = make_tiles(2, g.ax[0].n, g.ax[1].n, proj_rows(t.proj_form));
+  return (size_t)g.n_angles * tc.ntiles;
+}
+
 size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1,
                                const Tuning &t) {
   // sized for the smaller of the point-sampled and pixel-integrated tilings
@@ -905,6 +927,12 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   const int W = (at.n + 31) / 32;
   const size_t items = (size_t)g.n_angles * tc.ntiles;
   const size_t need = project_workspace_bytes(K, at.n, g.n_angles, D0, D1, t);
+  // items no atom meets: point-sampled 3D only, fields only
+  const int emode = o_in.empty_mode;
+  if (emode != kEmptyNone &&
+      (K != 2 || o_in.psf || o_in.R || !o_in.empty_loss || emode < 0 || emode > kEmptySkip))
+    return kErrArg;
+  const bool record = emode == kEmptyRecord;
   if (ws_bytes < need || (ws == nullptr && need > 0)) return kErrWorkspace;
   char *wp = static_cast<char *>(ws);
   int *next_item = reinterpret_cast<int *>(wp);
@@ -920,9 +948,17 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
     return kErrLaunch;
   ProjOut o = o_in;
   o.loss_part = loss_out ? loss_part : nullptr;
+  if (record) {
+    // every item as if no atom met it: its loss partial goes to empty_loss,
+    // under the schedule (split, tiling) of a forward of these atoms, so it
+    // equals bitwise what that forward computes for an empty item
+    o.alpha = o.beta = nullptr;
+    o.loss_part = o_in.empty_loss;
+    loss_out = nullptr;
+  }
   // half-width of the (square) cells of the pixel-integrated operator
   const float psf_s = 0.5f / g.ax[0].inv_step;
-  if (W > 0) {
+  if (W > 0 && !record) {
     dim3 bgrid((at.n + 127) / 128, g.n_angles);
     if (o.psf) {
       if (K == 1) gr_psf_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, psf_s);
@@ -973,12 +1009,13 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
                        (size_t)g.n_angles * D0 * D1 < (size_t)t.proj_split_cells;
     fused_loss = loss_out != nullptr && items <= kFusedLossItems;
     double *lo = fused_loss ? loss_out : nullptr;
+    const int Wk = record ? 0 : W;  // recording: no atom in any item
     if (form == 2) {
-      if (split) launch_project3d<32, 34, kProjWarps>(items, at, g, tc, bitmap, W, o, next_item, lo, stream);
-      else launch_project3d<32, 34, 1>(items, at, g, tc, bitmap, W, o, next_item, lo, stream);
+      if (split) launch_project3d<32, 34, kProjWarps>(items, at, g, tc, bitmap, Wk, o, next_item, lo, stream);
+      else launch_project3d<32, 34, 1>(items, at, g, tc, bitmap, Wk, o, next_item, lo, stream);
     } else {
-      if (split) launch_project3d<16, 37, kProjWarps>(items, at, g, tc, bitmap, W, o, next_item, lo, stream);
-      else launch_project3d<16, 37, 1>(items, at, g, tc, bitmap, W, o, next_item, lo, stream);
+      if (split) launch_project3d<16, 37, kProjWarps>(items, at, g, tc, bitmap, Wk, o, next_item, lo, stream);
+      else launch_project3d<16, 37, 1>(items, at, g, tc, bitmap, Wk, o, next_item, lo, stream);
     }
   }
   timer_mark(1, 1, stream);

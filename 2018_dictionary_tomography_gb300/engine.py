@@ -401,9 +401,46 @@ def _ptr(t):
     return None if t is None else t.data_ptr()
 
 
-def fit_forward_into(atoms, geom, data, fit, background, R, alpha, beta, loss, ws, psf=False,
-                     plan=None):
+def fit_items(geom, plan=None):
+    """(angle, tile) items of the 3D forward that can skip the items no atom
+    meets (0 for 2D geometries, which do not skip)."""
+    n = ctypes.c_size_t(0)
+    _lib.check(_lib.load().gr_fit_items(plan.handle if plan is not None else None,
+                                        ctypes.byref(geom.struct), ctypes.byref(n)),
+               "gr_fit_items")
+    return int(n.value)
+
+
+def fit_empty_loss_into(atoms, geom, data, fit, background, empty_loss, ws, plan=None):
+    """Each item's loss with no atom in it (float64, fit_items(geom, plan)
+    entries), under the schedule a forward of ``atoms`` takes: the record
+    that fit_forward_into(empty_loss=...) gives the items no atom meets."""
     code = {"l2": _lib.GR_FIT_L2, "kl": _lib.GR_FIT_KL}[fit]
+    st = _lib.load().gr_fit_empty_loss(
+        plan.handle if plan is not None else None, ctypes.byref(atoms.struct),
+        ctypes.byref(geom.struct), code, data.data_ptr(), float(background),
+        empty_loss.data_ptr(), ws.data_ptr(), ws.numel(), _stream_handle(geom.device))
+    _lib.check(st, "gr_fit_empty_loss")
+
+
+def fit_forward_into(atoms, geom, data, fit, background, R, alpha, beta, loss, ws, psf=False,
+                     plan=None, empty_loss=None):
+    """Fused forward into caller buffers.  With ``empty_loss`` (from
+    fit_empty_loss_into; 3D, R None) the items no atom meets take their loss
+    from it and keep their old field values: the loss is bitwise the same and
+    so are the fields wherever an atom is, which is all a Newton iteration's
+    derivatives read."""
+    code = {"l2": _lib.GR_FIT_L2, "kl": _lib.GR_FIT_KL}[fit]
+    if empty_loss is not None:
+        if psf or R is not None:
+            raise ValueError("skipping empty items needs the point-sampled forward without R")
+        st = _lib.load().gr_fit_forward_skip(
+            plan.handle if plan is not None else None, ctypes.byref(atoms.struct),
+            ctypes.byref(geom.struct), code, data.data_ptr(), float(background), _ptr(alpha),
+            _ptr(beta), _ptr(loss), empty_loss.data_ptr(), ws.data_ptr(), ws.numel(),
+            _stream_handle(geom.device))
+        _lib.check(st, "gr_fit_forward_skip")
+        return
     fn = _fn("fit_forward", psf, plan)
     st = fn(
         ctypes.byref(atoms.struct), ctypes.byref(geom.struct), code, data.data_ptr(),

@@ -263,7 +263,8 @@ class _Slot:
     """Device state of one admitted request."""
 
     def __init__(self, req, stream, device, use_graph=True, iters_per_launch=4,
-                 device_loop=True, setup_stream=None, plans=(None, None), build_loop=True):
+                 device_loop=True, setup_stream=None, plans=(None, None), build_loop=True,
+                 skip_empty=True):
         self.req = req
         # launch schedules of this request's shape class (engine.Plan, or
         # None for the process-wide one): projection, derivatives
@@ -332,10 +333,15 @@ class _Slot:
         ws_d = max(256, engine.workspace_bytes(_lib.GR_OP_DERIVS_2, self.cur, self.geom,
                                                self.plan_d))
         reg = req.reg is not None
+        # 3D forwards skip the (angle, tile) items no atom meets: their loss
+        # comes from a record of the data alone, made once per fit, and their
+        # fields, which no derivative reads, are left unwritten
+        n_items = engine.fit_items(self.geom, self.plan_p) if skip_empty else 0
         wl, n_work = _layout([("data", np.float32, shape), ("alpha", np.float32, shape),
                               ("alpha_t", np.float32, shape)] +
                              ([("beta", np.float32, shape), ("beta_t", np.float32, shape)]
                               if kl else []) +
+                             ([("empty", np.float64, (n_items,))] if n_items else []) +
                              [("f", np.float64, (n,)), ("g", np.float64, (n, P)),
                               ("H", np.float64, (n, P, P)), ("step", np.float64, (n,)),
                               ("ws_p", np.uint8, (ws_p,)), ("ws_d", np.uint8, (ws_d,))] +
@@ -354,6 +360,7 @@ class _Slot:
         self.beta, self.beta_t = (w("beta"), w("beta_t")) if kl else (None, None)
         self.f, self.g, self.H, self.step = w("f"), w("g"), w("H"), w("step")
         self.ws_p, self.ws_d = w("ws_p"), w("ws_d")
+        self.empty = w("empty") if n_items else None
         if reg:
             self.reg_kind = req.reg.kind
             self.reg_params = np.asarray(req.reg._p(), dtype=np.float64)
@@ -449,8 +456,12 @@ class _Slot:
         starting loss is also copied out (the fit's initial loss)."""
         r = self.req
         alpha, beta = self._current_fields(self.loop is not None)
+        if self.empty is not None:
+            engine.fit_empty_loss_into(self.cur, self.geom, self.data, r.fit, r.background,
+                                       self.empty, self.ws_p, plan=self.plan_p)
         engine.fit_forward_into(self.cur, self.geom, self.data, r.fit, r.background, None,
-                                alpha, beta, self.loss_cur, self.ws_p, plan=self.plan_p)
+                                alpha, beta, self.loss_cur, self.ws_p, plan=self.plan_p,
+                                empty_loss=self.empty)
         self._add_reg_value(self.cur, self.loss_cur)
         self.h_loss0.copy_(self.loss_cur.reshape(1), non_blocking=True)
 
@@ -473,7 +484,7 @@ class _Slot:
                                  self.theta_trial, self.step, self.trial, self.dev)
         engine.fit_forward_into(self.trial, self.geom, self.data, r.fit, r.background, None,
                                 self.alpha_t, self.beta_t, self.loss_trial, self.ws_p,
-                                plan=self.plan_p)
+                                plan=self.plan_p, empty_loss=self.empty)
         self._add_reg_value(self.trial, self.loss_trial)
         engine.newton_accept_into(self.dim, self.iso, self.loss_cur, self.loss_trial,
                                   self.theta, self.theta_trial, self.lam, 1e-4, r.lam_max,
@@ -665,8 +676,10 @@ class GaussFitServer:
 
     def __init__(self, device=None, max_slots=32, n_streams=16, hbm_budget=None,
                  hbm_reserve=4 << 30, use_graphs=True, iters_per_launch=4, device_loop=True,
-                 largest_first=False, exclusive_streams=True, tuned=False, batch_max=8):
+                 largest_first=False, exclusive_streams=True, tuned=False, batch_max=8,
+                 skip_empty=True):
         self.dev = torch.device(device or "cuda")
+        self.skip_empty = skip_empty
         engine._require_cuda(self.dev)
         self.max_slots = max_slots
         self.streams = [torch.cuda.Stream(self.dev) for _ in range(n_streams)]
@@ -810,7 +823,8 @@ class GaussFitServer:
                     self.batches += 1
                 else:
                     slot = _Slot(req, self.streams[si], self.dev, self.use_graphs, self.k,
-                                 self.device_loop, self.setup_stream, self._plans(req))
+                                 self.device_loop, self.setup_stream, self._plans(req),
+                                 skip_empty=self.skip_empty)
             except _lib.EngineError as e:
                 self.admit_seconds += time.perf_counter() - ta
                 if len(group) > 1:

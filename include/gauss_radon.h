@@ -294,7 +294,12 @@ unsigned long long gr_launch_count(void);
  * the 3D Hessian (order 2) kernels in chunks of 8 cells instead of 4, which
  * keeps more field loads in flight when supports are many cells wide and
  * idles lanes when they are narrow (default 0; the serving tuner picks it
- * per class of requests).  Set them before
+ * per class of requests).  GR_TUNE_DERIV_BLOCK_WARPS: warps per block of
+ * the derivative kernels that give each lane at most one angle, 1 (default)
+ * or 4; with one-warp blocks a finished warp frees its slot at once instead
+ * of waiting for the slowest warp of its block (3D Hessians of the largest
+ * served requests 458 -> 415 us, config 4's gradient 5 % faster; results are
+ * bitwise the same).  Set them before
  * gr_workspace_bytes and keep them fixed while launches that used the old
  * values are in flight.  Results do not depend on them beyond FP rounding of
  * the derivative chunk and lane sums and of a split tile's combined cell sums (the
@@ -310,7 +315,8 @@ enum {
   GR_TUNE_PROJ_SPLIT_CELLS = 4,
   GR_TUNE_DERIV_SPLIT_LANES = 6,
   GR_TUNE_DERIV_ONE_MB = 7,
-  GR_TUNE_DERIV_WIDE_ROWS = 8
+  GR_TUNE_DERIV_WIDE_ROWS = 8,
+  GR_TUNE_DERIV_BLOCK_WARPS = 9
 };
 int gr_set_tuning(int key, int value);
 int gr_get_tuning(int key);
@@ -353,6 +359,34 @@ int gr_atom_derivs_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geo
                         int mode, const float *field, const float *beta_field,
                         float beta_const, int order, double *f, double *g, double *H,
                         void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * Forwards of a fit that reads its fields only where atoms are (no
+ * counterpart in the reference, whose loop re-reads the whole sinogram per
+ * atom): a damped-Newton loop reads alpha / beta only inside its atoms'
+ * supports, which lie in the (angle, tile) items the forward's binning marks.
+ * For the point-sampled 3D forward (kdet 2):
+ *   gr_fit_items: the forward's items under the plan's tiling (plan NULL:
+ *     the process-wide schedule); 0 for 2D geometries, which do not skip.
+ *   gr_fit_empty_loss: each item's loss with no atom in it (R = 0: the data
+ *     term alone, L2 or KL) into empty_loss[gr_fit_items], computed under the
+ *     schedule a forward of these atoms takes (only n_atoms is read), so it
+ *     equals bitwise what that forward computes for an item no atom meets.
+ *     Once per data sinogram.
+ *   gr_fit_forward_skip: gr_fit_forward_plan without R, where an item that no
+ *     atom meets takes its loss from empty_loss and keeps whatever its fields
+ *     held: the loss is bitwise that of gr_fit_forward_plan, and so are the
+ *     fields in every item an atom meets.
+ * GR_ERR_ARG for a 2D geometry, a missing pointer or fit GR_FIT_NONE.
+ */
+int gr_fit_items(const gr_plan *plan, const gr_geometry *geom, size_t *n_items);
+int gr_fit_empty_loss(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                      int fit, const float *data, float background, double *empty_loss,
+                      void *workspace, size_t workspace_bytes, void *stream);
+int gr_fit_forward_skip(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
+                        int fit, const float *data, float background, float *alpha,
+                        float *beta, double *loss, const double *empty_loss, void *workspace,
+                        size_t workspace_bytes, void *stream);
 
 /*
  * Per-angle detector moments of a sinogram, for the moment-matching initial

@@ -70,7 +70,7 @@ def test_tuning_keys_round_trip_without_gpu():
     lib = lib_mod.load()
     # key: (a valid value, an invalid value)
     cases = {0: (65536, 16), 1: (2, 0), 2: (4, 3), 3: (2, 3), 4: (1 << 20, -1),
-             6: (4096, -5), 7: (0, -1)}
+             6: (4096, -5), 7: (0, -1), 8: (1, 2), 9: (1, 2)}
     for key, (good, bad) in cases.items():
         saved = lib.gr_get_tuning(key)
         try:
@@ -117,7 +117,7 @@ def test_plan_create_set_get_without_gpu():
     assert lib.gr_plan_create(2, ctypes.byref(at), ctypes.byref(g), ctypes.byref(h)) == 0
     assert h.value
     # a copy of the process-wide values, then independent of them
-    for key in (0, 1, 2, 3, 4, 6, 7, 8):
+    for key in (0, 1, 2, 3, 4, 6, 7, 8, 9):
         assert lib.gr_plan_get(h, key) == lib.gr_get_tuning(key)
     # the wide-row Hessian walk is a switch (0 or 1)
     assert lib.gr_plan_set(h, 8, 1) == 0 and lib.gr_plan_get(h, 8) == 1

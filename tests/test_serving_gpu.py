@@ -330,3 +330,25 @@ def test_batch_members_alone_equal_members_in_a_batch(cuda_ready):
     for k in alone:
         assert np.array_equal(alone[k]["theta"], mix[k]["theta"])
         assert alone[k]["iterations"] == mix[k]["iterations"]
+
+
+def test_skipping_empty_items_leaves_served_fits_unchanged(cuda_ready):
+    """3D fits whose forwards skip the items no atom meets end bitwise where
+    the fits with full forwards end (same iterations, parameters, loss)."""
+    def reqs():
+        return workloads.config3_requests(n=4, rate=1e9, seed=12, p2d=0.0, atoms=(6, 40),
+                                          angles=(10, 30), det=(64, 128), max_iter=30, tol=1e-6)
+    out = {}
+    for skip in (True, False):
+        srv = serving.GaussFitServer(max_slots=4, n_streams=2, skip_empty=skip)
+        for r in reqs():
+            r.arrival = 0.0
+            srv.submit(r)
+        out[skip] = srv.run()
+        srv.close()
+    assert set(out[True]) == set(out[False])
+    for k in out[True]:
+        a, b = out[True][k], out[False][k]
+        assert a["iterations"] == b["iterations"]
+        assert np.array_equal(a["theta"], b["theta"])
+        assert a["loss"] == b["loss"]
