@@ -27,10 +27,15 @@ namespace gr {
 // The body of a 128-thread block of the binning launch: atoms bx * 128 ..,
 // angle a (the launch's block (bx, a); a multi-problem launch maps its
 // blocks to (problem, bx, a)).
+// flag, list, n_list (3D, nullable): the items some atom meets, listed once
+// each (in no fixed order: the order changes no result) for a forward that
+// skips the others.  Only the first bit set in a word can be an item's first,
+// so an item's flag is tested once per word it uses, not once per atom.
 template <int K>
 __device__ __forceinline__ void bin_body(const Atoms &at, const Geom &g, const TileCfg &tc,
                                          uint32_t *bitmap, int W, float4 *pairs, int bx,
-                                         int a) {
+                                         int a, uint32_t *flag = nullptr, int *list = nullptr,
+                                         int *n_list = nullptr) {
   const int j = bx * 128 + (int)threadIdx.x;
   const uint32_t bit = 1u << (j & 31);
   const size_t base = (size_t)a * tc.ntiles;
@@ -73,16 +78,24 @@ __device__ __forceinline__ void bin_body(const Atoms &at, const Geom &g, const T
     const int r_lo = p.lo[0] / tc.t0, r_hi = p.hi[0] / tc.t0;
     const int c_lo = p.lo[1] / tc.t1, c_hi = p.hi[1] / tc.t1;
     for (int tr = r_lo; tr <= r_hi; ++tr)
-      for (int tcix = c_lo; tcix <= c_hi; ++tcix)
-        atomicOr(bitmap + (base + (size_t)tr * tc.nt1 + tcix) * W + wj, bit);
+      for (int tcix = c_lo; tcix <= c_hi; ++tcix) {
+        const size_t item = base + (size_t)tr * tc.nt1 + tcix;
+        if (flag == nullptr) {
+          atomicOr(bitmap + item * W + wj, bit);
+        } else if (atomicOr(bitmap + item * W + wj, bit) == 0u &&
+                   atomicExch(flag + item, 1u) == 0u) {
+          list[atomicAdd(n_list, 1)] = (int)item;
+        }
+      }
   }
 }
 
 template <int K>
 __global__ void __launch_bounds__(128) gr_bin_kernel(Atoms at, Geom g,
                                                      TileCfg tc, uint32_t *bitmap,
-                                                     int W, float4 *pairs) {
-  bin_body<K>(at, g, tc, bitmap, W, pairs, blockIdx.x, blockIdx.y);
+                                                     int W, float4 *pairs, uint32_t *flag,
+                                                     int *list, int *n_list) {
+  bin_body<K>(at, g, tc, bitmap, W, pairs, blockIdx.x, blockIdx.y, flag, list, n_list);
 }
 
 // Per-cell KL term f log(f/g) - f + g = g h(u), u = f/g, h(u) = u log u - u + 1,
@@ -130,10 +143,13 @@ struct Proj3Smem {
 // the kernel time, and splitting its atom list cuts that item's latency.
 // With loss_out, the last block (or warp) to finish sums the items' loss
 // partials in item order (no separate finalize launch).
+// item_list (nullable): take only the n_list[0] listed items (those some
+// atom meets; the loss partials of the others are already in place).
 template <int ROWS, int S, int NW>
 __global__ void __launch_bounds__(kProjWarps * 32)
     gr_project3d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap, int W,
-                        ProjOut out, int *next_item, double *loss_out) {
+                        ProjOut out, int *next_item, double *loss_out,
+                        const int *item_list, const int *n_list) {
   static_assert(NW == 1 || NW == kProjWarps, "a split item takes the whole block");
   using L = Proj3Smem<ROWS, S>;
   constexpr int kRing = L::kRing;
@@ -143,6 +159,7 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   __shared__ double s_loss[NW];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_items = g.n_angles * tc.ntiles;
+  const int n_take = item_list ? *n_list : n_items;
   float *acc = smem + (size_t)warp * L::kFloats;
   float *cmp = acc + L::kAcc;
   float4 *prm = reinterpret_cast<float4 *>(cmp + L::kAcc);  // 16-byte aligned
@@ -160,30 +177,15 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   if constexpr (NW == 1) {
     if (lane == 0) item = atomicAdd(next_item, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= n_items) break;  // whole warp leaves together
+    if (item >= n_take) break;  // whole warp leaves together
     __syncwarp();  // the previous item's epilogue reads are done
   } else {
     if (threadIdx.x == 0) s_item = atomicAdd(next_item, 1);
     __syncthreads();
     item = s_item;
-    if (item >= n_items) break;  // whole block leaves together
+    if (item >= n_take) break;  // whole block leaves together
   }
-  if (out.empty_mode == kEmptySkip) {
-    // an item that no atom meets takes its recorded loss and writes no field
-    // (its cells would all be zero): no accumulator clear, data read or store
-    const uint32_t *wds = bitmap + (size_t)item * W;
-    int nz = 0;
-    for (int wi = NW == 1 ? lane : (int)threadIdx.x; wi < W; wi += NW * 32)
-      nz |= wds[wi] != 0u ? 1 : 0;
-    bool empty;
-    if constexpr (NW == 1) empty = !__any_sync(0xffffffffu, nz);
-    else empty = !__syncthreads_or(nz);  // every thread has read s_item
-    if (empty) {
-      if (out.loss_part && (NW == 1 ? lane : (int)threadIdx.x) == 0)
-        out.loss_part[item] = out.empty_loss[item];
-      continue;
-    }
-  }
+  if (item_list) item = item_list[item];
   const int a = item / tc.ntiles, t = item - a * tc.ntiles;
   const int tr = t / tc.nt1, tcix = t - tr * tc.nt1;
   const int r0 = tr * ROWS, c0 = tcix * 32;
@@ -845,7 +847,7 @@ constexpr size_t kFusedLossItems = 8192;
 template <int ROWS, int S, int NW>
 static void launch_project3d(size_t items, const Atoms &at, const Geom &g, const TileCfg &tc,
                              const uint32_t *bitmap, int W, const ProjOut &o, int *next_item,
-                             double *loss_out, cudaStream_t stream) {
+                             double *loss_out, const int *item_list, cudaStream_t stream) {
   constexpr size_t smem = kProjWarps * Proj3Smem<ROWS, S>::kFloats * sizeof(float);
   // with the few static bytes, below the 48 KB that needs no opt-in, so no
   // function attribute is set (safe under stream capture)
@@ -866,7 +868,7 @@ static void launch_project3d(size_t items, const Atoms &at, const Geom &g, const
   const size_t want = NW == 1 ? (items + kProjWarps - 1) / kProjWarps : items;
   const int grid = (int)(want < (size_t)resident[dev] ? want : (size_t)resident[dev]);
   gr_project3d_kernel<ROWS, S, NW><<<grid, kProjWarps * 32, smem, stream>>>(
-      at, g, tc, bitmap, W, o, next_item, loss_out);
+      at, g, tc, bitmap, W, o, next_item, loss_out, item_list, next_item + 2);
 }
 
 // rows: the tile's rows (3D) or cells (2D)
@@ -902,14 +904,18 @@ size_t project_workspace_bytes(int K, int n_atoms, int n_angles, int D0, int D1,
   TileCfg tc = make_tiles(K, D0, D1, rows);
   const size_t W = (size_t)(n_atoms + 31) / 32;
   const size_t items = (size_t)n_angles * tc.ntiles;
-  // item counter of the persistent 3D kernel, finished-block counter of the
-  // 2D kernel
-  size_t bytes = align_up(2 * sizeof(int));
-  bytes += align_up(items * W * sizeof(uint32_t));
+  // item counter of the persistent 3D kernel, finished-block counter, count
+  // of listed items
+  size_t bytes = align_up(4 * sizeof(int));
+  // 3D: the bitmap is followed by a flag per item (cleared with it) and the
+  // list of items some atom meets (a forward that skips the others)
+  bytes += align_up(items * W * sizeof(uint32_t) + (K == 2 ? items * sizeof(uint32_t) : 0));
   bytes += align_up(items * sizeof(double));
   bytes += align_up(kLossMaxBlocks * sizeof(double));  // block sums of the loss finalize
   if (K == 1)  // per-(angle, atom) pair records of the 2D projection
     bytes += align_up((size_t)n_angles * (size_t)n_atoms * 2 * sizeof(float4));
+  else
+    bytes += align_up(items * sizeof(int));
   return bytes;
 }
 
@@ -936,18 +942,29 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   if (ws_bytes < need || (ws == nullptr && need > 0)) return kErrWorkspace;
   char *wp = static_cast<char *>(ws);
   int *next_item = reinterpret_cast<int *>(wp);
-  wp += align_up(2 * sizeof(int));
+  wp += align_up(4 * sizeof(int));
   uint32_t *bitmap = reinterpret_cast<uint32_t *>(wp);
-  wp += align_up(items * W * sizeof(uint32_t));
+  uint32_t *flag = bitmap + items * W;  // 3D: one per item
+  wp += align_up(items * W * sizeof(uint32_t) + (K == 2 ? items * sizeof(uint32_t) : 0));
   double *loss_part = reinterpret_cast<double *>(wp);
   wp += align_up(items * sizeof(double)) + align_up(kLossMaxBlocks * sizeof(double));
   float4 *pairs = K == 1 ? reinterpret_cast<float4 *>(wp) : nullptr;
-  // one clear covers the counters and the bitmap
-  if (cudaMemsetAsync(ws, 0, align_up(2 * sizeof(int)) + items * W * sizeof(uint32_t), stream) !=
-      cudaSuccess)
+  int *item_list = K == 2 ? reinterpret_cast<int *>(wp) : nullptr;
+  const bool skip = emode == kEmptySkip;
+  // one clear covers the counters and the bitmap (and the item flags)
+  if (cudaMemsetAsync(ws, 0,
+                      align_up(4 * sizeof(int)) + items * W * sizeof(uint32_t) +
+                          (skip ? items * sizeof(uint32_t) : 0),
+                      stream) != cudaSuccess)
     return kErrLaunch;
   ProjOut o = o_in;
   o.loss_part = loss_out ? loss_part : nullptr;
+  // skipping: the items no atom meets take their recorded loss partials
+  // (copied first, the listed items' partials overwrite theirs)
+  if (skip && o.loss_part &&
+      cudaMemcpyAsync(o.loss_part, o_in.empty_loss, items * sizeof(double),
+                      cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+    return kErrLaunch;
   if (record) {
     // every item as if no atom met it: its loss partial goes to empty_loss,
     // under the schedule (split, tiling) of a forward of these atoms, so it
@@ -964,9 +981,12 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
       if (K == 1) gr_psf_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, psf_s);
       else gr_psf_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, psf_s);
     } else if (K == 1) {
-      gr_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, pairs);
+      gr_bin_kernel<1><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, pairs, nullptr, nullptr,
+                                                  nullptr);
     } else {
-      gr_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, nullptr);
+      gr_bin_kernel<2><<<bgrid, 128, 0, stream>>>(at, g, tc, bitmap, W, nullptr,
+                                                  skip ? flag : nullptr, item_list,
+                                                  next_item + 2);
     }
     note_launches(1);
   }
@@ -1010,12 +1030,14 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
     fused_loss = loss_out != nullptr && items <= kFusedLossItems;
     double *lo = fused_loss ? loss_out : nullptr;
     const int Wk = record ? 0 : W;  // recording: no atom in any item
+    // skipping: only the listed items (none without atoms)
+    const int *il = skip ? item_list : nullptr;
     if (form == 2) {
-      if (split) launch_project3d<32, 34, kProjWarps>(items, at, g, tc, bitmap, Wk, o, next_item, lo, stream);
-      else launch_project3d<32, 34, 1>(items, at, g, tc, bitmap, Wk, o, next_item, lo, stream);
+      if (split) launch_project3d<32, 34, kProjWarps>(items, at, g, tc, bitmap, Wk, o, next_item, lo, il, stream);
+      else launch_project3d<32, 34, 1>(items, at, g, tc, bitmap, Wk, o, next_item, lo, il, stream);
     } else {
-      if (split) launch_project3d<16, 37, kProjWarps>(items, at, g, tc, bitmap, Wk, o, next_item, lo, stream);
-      else launch_project3d<16, 37, 1>(items, at, g, tc, bitmap, Wk, o, next_item, lo, stream);
+      if (split) launch_project3d<16, 37, kProjWarps>(items, at, g, tc, bitmap, Wk, o, next_item, lo, il, stream);
+      else launch_project3d<16, 37, 1>(items, at, g, tc, bitmap, Wk, o, next_item, lo, il, stream);
     }
   }
   timer_mark(1, 1, stream);
