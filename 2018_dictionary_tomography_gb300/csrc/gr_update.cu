@@ -165,11 +165,22 @@ int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int 
 // SM's FP64 pipe for 16 cycles, so a P x P factorisation run by one thread is
 // one long dependent chain (about a thousand FP64 operations for P = 10, with
 // divisions and square roots; 94 us for one block of 64 atoms).  Here a group
-// of G lanes (G a power of two >= P) shares one atom: lane l holds row l of
-// the damped block, columns are broadcast with shuffles, each column costs
-// one reciprocal square root (Cholesky) or one reciprocal (LU), after which
-// the lanes update their rows independently; the dependent chain per column
-// is a broadcast, the reciprocal and two multiply-adds.
+// of G >= P lanes shares one atom: lane l holds row l of the damped block,
+// columns are broadcast with shuffles, each column costs one reciprocal
+// square root (Cholesky) or one reciprocal (LU), after which the lanes update
+// their rows independently; the dependent chain per column is a broadcast,
+// the reciprocal and two multiply-adds.  A warp holds 32 / G groups: since
+// an FP64 warp instruction costs the pipe the same whatever lanes it uses,
+// G = P packs the most atoms into each (P = 10: three atoms a warp instead of
+// two with G = 16), the last 32 mod G lanes idle.
+//
+// gshfl: lane k of the caller's group (base: its first lane); a power-of-two
+// G uses the width-G shuffle, any other an explicit source lane.
+template <int G, typename T>
+__device__ __forceinline__ T gshfl(T v, int base, int k) {
+  if constexpr ((G & (G - 1)) == 0) return __shfl_sync(0xffffffffu, v, k, G);
+  else return __shfl_sync(0xffffffffu, v, base + k);
+}
 //
 // Every lane of a warp executes every shuffle (no lane leaves early), so a
 // group whose atom is out of range or masked runs on an identity block and
@@ -180,16 +191,15 @@ int launch_atom_update(const Atoms &olda, const Atoms &newa, const Geom &g, int 
 // Returns (identically on all lanes of the group) whether every pivot was
 // positive; x[] receives the solution on every lane.
 template <int P, int G>
-__device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l,
+__device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l, int base,
                                                double (&x)[P]) {
-  constexpr unsigned kAll = 0xffffffffu;
   double inv[P], col[P];
   bool spd = true;
 #pragma unroll
   for (int k = 0; k < P; ++k) col[k] = 0.0;
 #pragma unroll
   for (int j = 0; j < P; ++j) {
-    const double piv = __shfl_sync(kAll, a[j], j, G);
+    const double piv = gshfl<G>(a[j], base, j);
     spd = spd && (piv > 0.0);
     const double ij = rsqrt(piv > 0.0 ? piv : 1.0);
     inv[j] = ij;
@@ -197,7 +207,7 @@ __device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l,
     a[j] = lij;
 #pragma unroll
     for (int k = j + 1; k < P; ++k) {
-      const double lkj = __shfl_sync(kAll, lij, k, G);
+      const double lkj = gshfl<G>(lij, base, k);
       if (l == j) col[k] = lkj;         // lane j keeps column j of L
       a[k] = fma(-lij, lkj, a[k]);      // trailing rows (only k <= l is used)
     }
@@ -207,7 +217,7 @@ __device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l,
   double y[P];
 #pragma unroll
   for (int j = 0; j < P; ++j) {
-    y[j] = __shfl_sync(kAll, b, j, G) * inv[j];
+    y[j] = gshfl<G>(b, base, j) * inv[j];
     b = fma(-a[j], y[j], b);
   }
   // backward: x_i = (y_i - sum_{k>i} L[k][i] x_k) / L[i][i]; lane i holds
@@ -216,7 +226,7 @@ __device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l,
 #pragma unroll
   for (int k = P - 1; k >= 0; --k) {
     const double v = (y[k] - acc) * inv[k];
-    x[k] = __shfl_sync(kAll, v, k, G);
+    x[k] = gshfl<G>(v, base, k);
     acc = fma(col[k], x[k], acc);
   }
   return spd;
@@ -229,7 +239,8 @@ __device__ __forceinline__ bool group_cholesky(double (&a)[P], double b, int l,
 // column c with the multiplier a[c] * (1 / pivot).  Returns false for a
 // zero pivot column.
 template <int P, int G>
-__device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, double (&x)[P]) {
+__device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, int base,
+                                         double (&x)[P]) {
   constexpr unsigned kAll = 0xffffffffu;
   bool used = l >= P;                   // padding lanes never pivot
   bool ok = true;
@@ -239,17 +250,31 @@ __device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, double
   for (int c = 0; c < P; ++c) {
     double v = used ? -1.0 : fabs(a[c]);
     int idx = l;
+    if constexpr ((G & (G - 1)) == 0) {
 #pragma unroll
-    for (int off = G / 2; off > 0; off >>= 1) {
-      const double ov = __shfl_xor_sync(kAll, v, off, G);
-      const int oi = __shfl_xor_sync(kAll, idx, off, G);
-      if (ov > v || (ov == v && oi < idx)) {
-        v = ov;
-        idx = oi;
+      for (int off = G / 2; off > 0; off >>= 1) {
+        const double ov = __shfl_xor_sync(kAll, v, off, G);
+        const int oi = __shfl_xor_sync(kAll, idx, off, G);
+        if (ov > v || (ov == v && oi < idx)) {
+          v = ov;
+          idx = oi;
+        }
+      }
+    } else {
+      // the same choice (largest, ties to the lower row) by a scan
+      const double mine = v;
+      v = -2.0;
+#pragma unroll
+      for (int i = 0; i < G; ++i) {
+        const double ov = gshfl<G>(mine, base, i);
+        if (ov > v) {
+          v = ov;
+          idx = i;
+        }
       }
     }
     ok = ok && (v > 0.0);
-    const double piv = __shfl_sync(kAll, a[c], idx, G);
+    const double piv = gshfl<G>(a[c], base, idx);
     const double pi = 1.0 / (piv != 0.0 ? piv : 1.0);
     prow[c] = idx;
     pinv[c] = pi;
@@ -257,10 +282,10 @@ __device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, double
     const double m = a[c] * pi;
 #pragma unroll
     for (int k = c + 1; k < P; ++k) {
-      const double pk = __shfl_sync(kAll, a[k], idx, G);
+      const double pk = gshfl<G>(a[k], base, idx);
       if (elim) a[k] = fma(-m, pk, a[k]);
     }
-    const double pb = __shfl_sync(kAll, b, idx, G);
+    const double pb = gshfl<G>(b, base, idx);
     if (elim) b = fma(-m, pb, b);
     used = used || l == idx;
   }
@@ -268,7 +293,7 @@ __device__ __forceinline__ bool group_lu(double (&a)[P], double b, int l, double
   // lane folds each x_k into its rhs as soon as it is known
 #pragma unroll
   for (int c = P - 1; c >= 0; --c) {
-    x[c] = __shfl_sync(kAll, b * pinv[c], prow[c], G);
+    x[c] = gshfl<G>(b * pinv[c], base, prow[c]);
     b = fma(-a[c], x[c], b);
   }
   return ok;
@@ -287,11 +312,14 @@ __device__ __forceinline__ void solve_body(int n, const double *g, const double 
                                            double *step_norm, int *fail, const AtomOut &ao,
                                            int block) {
   constexpr unsigned kAll = 0xffffffffu;
-  const int t = block * 32 + (int)threadIdx.x;
-  if ((t & ~31) / G >= n) return;       // whole warp past the last atom
-  const int l = t & (G - 1);
-  const int j = t / G;
-  const bool live = j < n;
+  constexpr int GPW = 32 / G;           // atoms per warp
+  if (block * GPW >= n) return;         // whole warp past the last atom
+  const int lane = (int)threadIdx.x & 31;
+  const int grp = lane / G;             // GPW: the idle lanes past the last group
+  const int l = lane - grp * G;
+  const int base = grp * G;
+  const int j = block * GPW + grp;
+  const bool live = grp < GPW && j < n;
   const bool active = live && (mask == nullptr || mask[j] != 0);
   const bool row = live && l < P;
   double a[P], b, x[P];
@@ -304,12 +332,14 @@ __device__ __forceinline__ void solve_body(int n, const double *g, const double 
     b = row ? -g[(size_t)j * P + l] : 0.0;
   };
   load();
-  bool ok = group_cholesky<P, G>(a, b, l, x);
-  if (__any_sync(kAll, !ok)) {          // some group of this warp is not positive definite
+  bool ok = group_cholesky<P, G>(a, b, l, base, x);
+  // some atom of this warp is not positive definite (idle lanes, which
+  // shuffle other groups' values, do not count)
+  if (__any_sync(kAll, live && !ok)) {
     const bool chol_ok = ok;
     load();
     double xl[P];
-    const bool lu_ok = group_lu<P, G>(a, b, l, xl);
+    const bool lu_ok = group_lu<P, G>(a, b, l, base, xl);
     if (!chol_ok) {
       ok = lu_ok;
 #pragma unroll
@@ -330,12 +360,19 @@ __device__ __forceinline__ void solve_body(int n, const double *g, const double 
   th += d;
   // |dtheta| over the group, fixed butterfly order
   double nrm = d * d;
+  if constexpr ((G & (G - 1)) == 0) {
 #pragma unroll
-  for (int off = 1; off < G; off <<= 1) nrm += __shfl_xor_sync(kAll, nrm, off, G);
+    for (int off = 1; off < G; off <<= 1) nrm += __shfl_xor_sync(kAll, nrm, off, G);
+  } else {
+    const double mine = nrm;
+    nrm = 0.0;
+#pragma unroll
+    for (int i = 0; i < G; ++i) nrm += gshfl<G>(mine, base, i);
+  }
   // clamps of the reference's update: I >= 0, sign flips keeping
   // diag(r) >= 0 (P fixes the kind: 4 / 5 isotropic 2D / 3D, 6 anisotropic
   // 2D, 10 anisotropic 3D); a flip of r's diagonal entry i negates row i
-  const unsigned neg = __ballot_sync(kAll, th < 0.0) >> (t & 31 & ~(G - 1));
+  const unsigned neg = __ballot_sync(kAll, th < 0.0) >> base;
   if (ok) {
     const int q = l - 1 - D;             // index in packed r
     auto negr = [&](int i) { return ((neg >> (1 + D + i)) & 1u) != 0u; };
@@ -510,17 +547,17 @@ int launch_newton_solve(int dim, int iso, int n, const double *g, const double *
                         const unsigned char *mask, double *theta_new,
                         double *step_norm, int *fail, AtomOut ao, cudaStream_t stream) {
   if (n <= 0) return kOk;
-  // one warp per block: the FP64 work of a few atoms per warp then spreads
-  // over as many SMs' FP64 pipes as there are warps
-  auto blocks = [n](int G) { return (unsigned)(((size_t)n * G + 31) / 32); };
+  // one warp per block (32 / G atoms): the FP64 work then spreads over as
+  // many SMs' FP64 pipes as there are warps
+  auto blocks = [n](int G) { return (unsigned)((n + 32 / G - 1) / (32 / G)); };
   if (dim == 2 && iso)
-    gr_newton_solve_kernel<4, 2, 8><<<blocks(8), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<4, 2, 4><<<blocks(4), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else if (dim == 2)
-    gr_newton_solve_kernel<6, 2, 8><<<blocks(8), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<6, 2, 6><<<blocks(6), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else if (iso)
-    gr_newton_solve_kernel<5, 3, 8><<<blocks(8), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<5, 3, 5><<<blocks(5), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   else
-    gr_newton_solve_kernel<10, 3, 16><<<blocks(16), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
+    gr_newton_solve_kernel<10, 3, 10><<<blocks(10), 32, 0, stream>>>(n, g, H, lam, theta, mask, theta_new, step_norm, fail, ao);
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrLaunch;
 }
@@ -575,10 +612,10 @@ int launch_batch_accept(const BatchLaunch &b, cudaStream_t stream) {
 
 int preload_update() {
   return preload_fn(gr_atom_update_kernel<1>) + preload_fn(gr_atom_update_kernel<2>) +
-         preload_fn(gr_sum_partials_kernel) + preload_fn(gr_newton_solve_kernel<4, 2, 8>) +
-         preload_fn(gr_newton_solve_kernel<6, 2, 8>) +
-         preload_fn(gr_newton_solve_kernel<5, 3, 8>) +
-         preload_fn(gr_newton_solve_kernel<10, 3, 16>) + preload_fn(gr_newton_accept_kernel) +
+         preload_fn(gr_sum_partials_kernel) + preload_fn(gr_newton_solve_kernel<4, 2, 4>) +
+         preload_fn(gr_newton_solve_kernel<6, 2, 6>) +
+         preload_fn(gr_newton_solve_kernel<5, 3, 5>) +
+         preload_fn(gr_newton_solve_kernel<10, 3, 10>) + preload_fn(gr_newton_accept_kernel) +
          preload_fn(gr_accept_fields_kernel) + preload_fn(gr_batch_solve_kernel<4>) +
          preload_fn(gr_batch_solve_kernel<6>) + preload_fn(gr_batch_accept_kernel);
 }

@@ -33,24 +33,34 @@ Host-side care that keeps the loop from stalling behind fits in flight:
 buffers of a new request are built on a separate setup stream; finished
 loop graphs are destroyed only when no fit runs (destroying an executable
 graph waits for the device to idle); pinned host buffers are pooled.  Requests
-are admitted in arrival order (``largest_first`` admits the largest of
-those that have arrived first, or with "both_ends" the largest and the
-smallest alternately; on the 512-request stream submitted at once arrival
-order finished in 1.66 s, largest-first in 1.79 s and both-ends in 1.69 s:
-with the largest first, the small fits, whose time is mostly host set-up,
-are left to the end).  A request is admitted only onto a stream with no fit in
+are admitted in arrival order, except that while fewer than half the streams
+have a fit in flight the largest arrived request goes first
+(``largest_first="when_idle"``, the default): a server starting on a full
+queue otherwise spends its first tens of milliseconds setting up small fits
+that finish at once while the device idles (512 requests submitted at once:
+1.494 s against 1.503 s in arrival order).  ``largest_first=True`` sorts
+every admission by size and "both_ends" alternates the largest and the
+smallest; both leave the small fits, whose time is mostly host set-up, to the
+end.  A request is admitted only onto a stream with no fit in
 flight (``exclusive_streams``): a stream runs its work in order, and a
 whole fit is one graph launch, so a request queued behind another on the
 same stream would wait for that entire fit however little work it has.
 
-Small 2D fits (up to 224 atoms, L2, no regulariser) that are admitted
-together run as one batched device loop (``engine.BatchLoop``, up to
-``batch_max`` fits): every kernel of an iteration is one launch over a table
-of the fits, each fit leaves the batch at its own stop test, and every fit
-ends bitwise where its own loop would (tests/test_serving_gpu.py).  On the
-512-request stream the batched and unbatched mixes finish within 1 % of each
-other (the mix is bound by device work, which batching does not change); the
-admission host time drops from 0.48 to 0.38 s (fewer graphs to build).
+3D fits skip the (angle, tile) items of their forwards that no atom meets
+(``skip_empty``, engine.fit_forward_into(empty_loss=...)): bitwise the same
+fits, 26 % less 3D projection time on the stream's requests.
+
+With ``batch_max`` > 1, small 2D fits (up to 224 atoms, L2, no regulariser)
+that are admitted together run as one batched device loop
+(``engine.BatchLoop``): every kernel of an iteration is one launch over a
+table of the fits, each fit leaves the batch at its own stop test, and every
+fit ends bitwise where its own loop would (tests/test_serving_gpu.py).  It
+is off by default: the batch's kernels cover its stopped members' blocks and
+its loop runs until its last member stops, which costs more device time
+(the stream's 155 batchable fits: 0.100 s batched against 0.079 s in their
+own loops) than the host set-up it saves (admission 0.48 -> 0.38 s), and the
+mix is bound by device work (512 requests: 1.537 s with batches of 8 against
+1.494 s without).
 
 The process should give every stream its own hardware work queue
 (environment ``CUDA_DEVICE_MAX_CONNECTIONS`` >= n_streams + 1, at most 32,
@@ -676,7 +686,7 @@ class GaussFitServer:
 
     def __init__(self, device=None, max_slots=32, n_streams=16, hbm_budget=None,
                  hbm_reserve=4 << 30, use_graphs=True, iters_per_launch=4, device_loop=True,
-                 largest_first=False, exclusive_streams=True, tuned=False, batch_max=8,
+                 largest_first="when_idle", exclusive_streams=True, tuned=False, batch_max=1,
                  skip_empty=True):
         self.dev = torch.device(device or "cuda")
         self.skip_empty = skip_empty
@@ -766,7 +776,7 @@ class GaussFitServer:
     def _admit(self, now):
         if self._hold_admission:
             return                      # retry only after a fit has finished
-        if self.largest_first and len(self.pending) > 1:
+        if self.largest_first and self.largest_first != "when_idle" and len(self.pending) > 1:
             # among the requests that have arrived, the largest go first, so
             # the longest fits start early (arrival order otherwise kept);
             # "both ends": largest and smallest alternately, so the small
@@ -786,6 +796,18 @@ class GaussFitServer:
                     arrived = mixed
                 self.pending = collections.deque(arrived + later)
         while self.pending and len(self.active) < self.max_slots:
+            if self.largest_first == "when_idle" and len(self.active) < len(self.streams) // 2:
+                # few fits in flight (a server starting on a full queue): the
+                # largest arrived request first, so the device gets long work
+                # while the host sets up the next ones
+                best = None
+                for i, r in enumerate(self.pending):
+                    if r.arrival <= now and (best is None or r.size_hint[0] * r.size_hint[1] >
+                                             best[1].size_hint[0] * best[1].size_hint[1]):
+                        best = (i, r)
+                if best is not None and best[0] > 0:
+                    del self.pending[best[0]]
+                    self.pending.appendleft(best[1])
             req = self.pending[0]
             if req.arrival > now:
                 break

@@ -866,6 +866,16 @@ def run_serving(args):
     admit_cmp = srv.admit_seconds
     phases_cmp = dict(srv.admit_phases)
     loops_cmp = srv.device_loops
+    # the same mix with small 2D fits batched into multi-problem loops
+    # (batches of up to 8; off by default: slower on this mix)
+    t0 = time.perf_counter()
+    srv = serving.GaussFitServer(dev, max_slots=64, n_streams=31, tuned=True, batch_max=8)
+    for r in cmp_reqs:
+        srv.submit(r)
+    batched_cmp = srv.run(t0=t0)
+    t_batched = time.perf_counter() - t0
+    srv.close()
+    n_batches = srv.batches
 
     def plain_run(lean):
         reqs = wl.config3_requests(n=args.compare, seed=3)
@@ -928,6 +938,8 @@ def run_serving(args):
             # others (same in every arm: the same rule) are reported apart
             "fits_with_progress": ok_cmp, "fits_without_progress": none_cmp,
             "served_fits_s": ok_cmp / t_served,
+            "served_batched_fits_s": progress(batched_cmp)[0] / t_batched,
+            "served_batched_loops": n_batches,
             "plain_fits_s": ok_plain / t_plain,
             "plain_lean_fits_s": ok_plain / t_lean,
             "speedup": t_plain / t_served,

@@ -119,13 +119,17 @@ def test_atom_step_trial_and_apply(eng, cuda_ready, kind):
     assert relerr(fw["alpha"].cpu().numpy(), fresh["alpha"].cpu().numpy()) < 1e-5
 
 
-def test_newton_solve_matches_numpy(eng, cuda_ready):
-    rng = np.random.default_rng(4)
+@pytest.mark.parametrize("n", [7, 61])
+def test_newton_solve_matches_numpy(eng, cuda_ready, n):
+    """Lane groups of P lanes (32 // P atoms a warp, the last lanes idle):
+    every atom's damped step equals numpy's, with indefinite blocks (the LU
+    fallback) in some warps and partial last warps."""
+    rng = np.random.default_rng(4 + n)
     for dim, P, iso in ((2, 6, False), (3, 10, False), (2, 4, True), (3, 5, True)):
-        n = 7
         A = rng.normal(size=(n, P, P))
         H = A @ A.transpose(0, 2, 1) + 0.1 * np.eye(P)
-        H[3] -= 5 * np.eye(P)       # an indefinite block: LU path
+        for j in range(3, n, 17):
+            H[j] -= 5 * np.eye(P)   # an indefinite block: LU path
         gvec = rng.normal(size=(n, P))
         lam = rng.uniform(0.1, 2, n)
         theta = np.concatenate([rng.uniform(0.5, 1, (n, 1)), rng.normal(size=(n, P - 1))], 1)

@@ -316,11 +316,11 @@ def test_batch_members_alone_equal_members_in_a_batch(cuda_ready):
     alone = {}
     for r in _small_2d(n=5, seed=22):
         r.arrival = 0.0
-        srv = serving.GaussFitServer(max_slots=1, n_streams=1)
+        srv = serving.GaussFitServer(max_slots=1, n_streams=1, batch_max=8)
         srv.submit(r)
         alone.update(srv.run())
         srv.close()
-    srv = serving.GaussFitServer(max_slots=8, n_streams=2)
+    srv = serving.GaussFitServer(max_slots=8, n_streams=2, batch_max=8)
     for r in _small_2d(n=5, seed=22):
         r.arrival = 0.0
         srv.submit(r)
