@@ -143,9 +143,10 @@ struct Proj3Smem {
 // the kernel time, and splitting its atom list cuts that item's latency.
 // With loss_out, the last block (or warp) to finish sums the items' loss
 // partials in item order (no separate finalize launch).
-// item_list (nullable): take only the n_list[0] listed items (those some
-// atom meets; the loss partials of the others are already in place).
-template <int ROWS, int S, int NW>
+// LIST: take only the n_list[0] items of item_list (those some atom meets;
+// the loss partials of the others are already in place).  A template
+// parameter, so that the forward of every item keeps its own registers.
+template <int ROWS, int S, int NW, bool LIST>
 __global__ void __launch_bounds__(kProjWarps * 32)
     gr_project3d_kernel(Atoms at, Geom g, TileCfg tc, const uint32_t *bitmap, int W,
                         ProjOut out, int *next_item, double *loss_out,
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(kProjWarps * 32)
   __shared__ double s_loss[NW];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_items = g.n_angles * tc.ntiles;
-  const int n_take = item_list ? *n_list : n_items;
+  const int n_take = LIST ? *n_list : n_items;
   float *acc = smem + (size_t)warp * L::kFloats;
   float *cmp = acc + L::kAcc;
   float4 *prm = reinterpret_cast<float4 *>(cmp + L::kAcc);  // 16-byte aligned
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(kProjWarps * 32)
     item = s_item;
     if (item >= n_take) break;  // whole block leaves together
   }
-  if (item_list) item = item_list[item];
+  if constexpr (LIST) item = item_list[item];
   const int a = item / tc.ntiles, t = item - a * tc.ntiles;
   const int tr = t / tc.nt1, tcix = t - tr * tc.nt1;
   const int r0 = tr * ROWS, c0 = tcix * 32;
@@ -861,14 +862,18 @@ static void launch_project3d(size_t items, const Atoms &at, const Geom &g, const
   if (resident[dev] == 0) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gr_project3d_kernel<ROWS, S, NW>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gr_project3d_kernel<ROWS, S, NW, false>,
                                                   kProjWarps * 32, smem);
     resident[dev] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   }
   const size_t want = NW == 1 ? (items + kProjWarps - 1) / kProjWarps : items;
   const int grid = (int)(want < (size_t)resident[dev] ? want : (size_t)resident[dev]);
-  gr_project3d_kernel<ROWS, S, NW><<<grid, kProjWarps * 32, smem, stream>>>(
-      at, g, tc, bitmap, W, o, next_item, loss_out, item_list, next_item + 2);
+  if (item_list)
+    gr_project3d_kernel<ROWS, S, NW, true><<<grid, kProjWarps * 32, smem, stream>>>(
+        at, g, tc, bitmap, W, o, next_item, loss_out, item_list, next_item + 2);
+  else
+    gr_project3d_kernel<ROWS, S, NW, false><<<grid, kProjWarps * 32, smem, stream>>>(
+        at, g, tc, bitmap, W, o, next_item, loss_out, nullptr, nullptr);
 }
 
 // rows: the tile's rows (3D) or cells (2D)
@@ -1101,10 +1106,14 @@ int launch_batch_project(const BatchLaunch &b, int use_trial, cudaStream_t strea
 int preload_project() {
   return preload_fn(gr_bin_kernel<1>) + preload_fn(gr_bin_kernel<2>) +
          preload_fn(gr_psf_bin_kernel<1>) + preload_fn(gr_psf_bin_kernel<2>) +
-         preload_fn(gr_project3d_kernel<16, 37, 1>) +
-         preload_fn(gr_project3d_kernel<16, 37, kProjWarps>) +
-         preload_fn(gr_project3d_kernel<32, 34, 1>) +
-         preload_fn(gr_project3d_kernel<32, 34, kProjWarps>) +
+         preload_fn(gr_project3d_kernel<16, 37, 1, false>) +
+         preload_fn(gr_project3d_kernel<16, 37, kProjWarps, false>) +
+         preload_fn(gr_project3d_kernel<32, 34, 1, false>) +
+         preload_fn(gr_project3d_kernel<32, 34, kProjWarps, false>) +
+         preload_fn(gr_project3d_kernel<16, 37, 1, true>) +
+         preload_fn(gr_project3d_kernel<16, 37, kProjWarps, true>) +
+         preload_fn(gr_project3d_kernel<32, 34, 1, true>) +
+         preload_fn(gr_project3d_kernel<32, 34, kProjWarps, true>) +
          preload_fn(gr_project1d_kernel<true, 8, 1, 4>) +
          preload_fn(gr_project1d_kernel<true, 8, 1, 2>) +
          preload_fn(gr_project1d_kernel<true, kProjWarps>) +
