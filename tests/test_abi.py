@@ -139,6 +139,47 @@ def test_plan_create_set_get_without_gpu():
     assert lib.gr_radproj_plan(None, ctypes.byref(at), ctypes.byref(g), None, None, 0, None) == -1
 
 
+def test_skip_forward_items_and_argument_checks_without_gpu():
+    """gr_fit_items counts the 3D forward's (angle, tile) items under a plan's
+    tiling (0 for 2D); the skipping forward and its record refuse 2D
+    geometries and missing data before any device work."""
+    lib_mod = importlib.import_module("2018_dictionary_tomography_gb300._lib")
+    lib = lib_mod.load()
+    at = lib_mod.GrAtoms()
+    at.n_atoms = 100
+    at.I = at.x = at.r = 16            # non-null stand-ins, never read
+    g = lib_mod.GrGeometry()
+    g.kdet, g.n_angles, g.frames = 2, 50, 16
+    for k in range(2):
+        g.det[k], g.det_first[k], g.det_inv_step[k] = 16, -1.0, 32.0
+    g.n_det[0], g.n_det[1] = 70, 65
+    n = ctypes.c_size_t()
+    assert lib.gr_fit_items(None, ctypes.byref(g), ctypes.byref(n)) == 0
+    assert n.value == 50 * 5 * 3                 # 16 x 32 tiles
+    h = ctypes.c_void_p()
+    assert lib.gr_plan_create(0, ctypes.byref(at), ctypes.byref(g), ctypes.byref(h)) == 0
+    assert lib.gr_plan_set(h, 3, 2) == 0
+    assert lib.gr_fit_items(h, ctypes.byref(g), ctypes.byref(n)) == 0
+    assert n.value == 50 * 3 * 3                 # 32 x 32 tiles
+    assert lib.gr_fit_items(h, ctypes.byref(g), None) == -1
+    # no data: refused before any launch
+    assert lib.gr_fit_empty_loss(h, ctypes.byref(at), ctypes.byref(g), 1, None, 0.0, 16,
+                                 None, 0, None) == -1
+    assert lib.gr_fit_forward_skip(h, ctypes.byref(at), ctypes.byref(g), 1, None, 0.0, 16,
+                                   None, 16, 16, None, 0, None) == -1
+    # no record: refused
+    assert lib.gr_fit_forward_skip(h, ctypes.byref(at), ctypes.byref(g), 1, 16, 0.0, 16,
+                                   None, 16, None, None, 0, None) == -1
+    # 2D: no items to skip, and both calls refuse
+    g.kdet = 1
+    assert lib.gr_fit_items(None, ctypes.byref(g), ctypes.byref(n)) == 0 and n.value == 0
+    assert lib.gr_fit_empty_loss(None, ctypes.byref(at), ctypes.byref(g), 1, 16, 0.0, 16,
+                                 None, 0, None) == -1
+    assert lib.gr_fit_forward_skip(None, ctypes.byref(at), ctypes.byref(g), 1, 16, 0.0, 16,
+                                   None, 16, 16, None, 0, None) == -1
+    assert lib.gr_plan_destroy(h) == 0
+
+
 def test_batch_layout_without_gpu():
     """gr_batch_workspace_bytes: sizes only (no pointer is dereferenced); a
     member that cannot be batched (3D, or 8 bitmap words and more) gives 0."""
