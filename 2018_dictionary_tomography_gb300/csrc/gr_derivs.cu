@@ -752,7 +752,7 @@ int tuning_set(Tuning &t, int key, int value) {
     t.deriv_atoms_per_warp = value;
     return kOk;
   }
-  if (key == 3 && value >= 1 && value <= 2) {
+  if (key == 3 && value >= 1 && value <= 3) {
     t.proj_form = value;
     return kOk;
   }

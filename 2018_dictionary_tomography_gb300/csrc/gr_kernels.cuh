@@ -89,7 +89,7 @@ struct Tuning {
   int deriv_target_warps = 131072;  // key 0
   int deriv_min_angles = 1;         // key 1
   int deriv_atoms_per_warp = 0;     // key 2 (0: automatic)
-  int proj_form = 1;                // key 3 (1: 16 x 32 tiles, 2: 32 x 32)
+  int proj_form = 1;                // key 3 (3D 1: 16 x 32 tiles, 2: 32 x 32; 2D 32, 64, 128 cells)
   int proj_split_cells = 4 << 20;   // key 4
   int deriv_split_lanes = 65536;    // key 6
   int deriv_one_mb = 1024;          // key 7

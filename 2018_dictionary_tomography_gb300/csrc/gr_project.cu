@@ -930,10 +930,12 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
   const int K = g.K;
   const int D0 = g.ax[0].n, D1 = K == 1 ? 1 : g.ax[1].n;
   const int form = t.proj_form;
-  // 2D: 64-cell tiles (two cells per lane) for form 2, else 32
+  // 2D: 64-cell tiles (two cells per lane) for form 2, 128 (four) for form
+  // 3, else 32
   const bool wide2d = K == 1 && !o_in.psf && form == 2;
+  const bool wide4 = K == 1 && !o_in.psf && form == 3;
   TileCfg tc = make_tiles(K, D0, D1,
-                          K == 1 ? (wide2d ? 2 * kTile1D : kTile1D)
+                          K == 1 ? (wide4 ? 4 * kTile1D : wide2d ? 2 * kTile1D : kTile1D)
                                  : (!o_in.psf ? proj_rows(form) : kTileDim0));
   const int W = (at.n + 31) / 32;
   const size_t items = (size_t)g.n_angles * tc.ntiles;
@@ -1012,7 +1014,13 @@ int launch_project(const Atoms &at, const Geom &g, const ProjOut &o_in,
     // last block also sums the loss partials (no separate finalize launch)
     fused_loss = loss_out != nullptr && items <= kFusedLossItems;
     double *lo = fused_loss ? loss_out : nullptr;
-    if (wide2d && W >= 8)
+    if (wide4 && W >= 8)
+      gr_project1d_kernel<true, 8, 4, 2><<<(unsigned)items, 8 * 32, 0, stream>>>(
+          at, g, tc, bitmap, W, o, lo, next_item + 1, pairs);
+    else if (wide4)
+      gr_project1d_kernel<true, kProjWarps, 4><<<(unsigned)items, kProjWarps * 32, 0, stream>>>(
+          at, g, tc, bitmap, W, o, lo, next_item + 1, pairs);
+    else if (wide2d && W >= 8)
       gr_project1d_kernel<true, 8, 2, 2><<<(unsigned)items, 8 * 32, 0, stream>>>(
           at, g, tc, bitmap, W, o, lo, next_item + 1, pairs);
     else if (wide2d)
@@ -1119,6 +1127,8 @@ int preload_project() {
          preload_fn(gr_project1d_kernel<true, kProjWarps>) +
          preload_fn(gr_project1d_kernel<true, 8, 2, 2>) +
          preload_fn(gr_project1d_kernel<true, kProjWarps, 2>) +
+         preload_fn(gr_project1d_kernel<true, 8, 4, 2>) +
+         preload_fn(gr_project1d_kernel<true, kProjWarps, 4>) +
          preload_fn(gr_psf_project_kernel<1>) + preload_fn(gr_psf_project_kernel<2>) +
          preload_fn(gr_loss_finalize_kernel) + preload_fn(gr_batch_bin_kernel) +
          preload_fn(gr_batch_project_kernel);

@@ -147,6 +147,8 @@ _req_plans = {}
 # untuned on the 512-request stream)
 DERIV_CANDIDATES = ((131072, 1, 1, 0), (131072, 1, 1, 1))
 PROJ_CANDIDATES = ((1, 4 << 20), (1, 0), (2, 4 << 20), (2, 0))
+# 2D: the block split does not apply; tiles of 32, 64 or 128 cells
+PROJ_CANDIDATES_2D = ((1, 0), (2, 0), (3, 0))
 
 
 def request_key(req, order=2):
@@ -178,7 +180,7 @@ def tune_request_classes(requests, device, reps=3, order=2):
         data = req.device_data(geom, device, stream)
         pp = engine.Plan(_lib.GR_OP_PROJECT, atoms, geom)
         best_p = None
-        for form, split in PROJ_CANDIDATES:
+        for form, split in (PROJ_CANDIDATES_2D if len(req.detector) == 1 else PROJ_CANDIDATES):
             pp.set(3, form).set(4, split)
             ms = _time(lambda: engine.fit_forward(atoms, geom, data, req.fit, req.background,
                                                   plan=pp), reps)

@@ -280,7 +280,9 @@ unsigned long long gr_launch_count(void);
  * atoms (default 0: automatic, one atom per warp for Hessians and for series
  * of 1024 or more angles, else four).  GR_TUNE_PROJ_TILING: tiles of the
  * point-sampled 3D projection, 1 = 16 x 32 cells (default, more resident
- * warps), 2 = 32 x 32 (fewer atoms cut by tile edges).
+ * warps), 2 = 32 x 32 (fewer atoms cut by tile edges), 3 = as 1; of the 2D
+ * projection, 32, 64 and 128 cells (one, two or four per lane: wide
+ * footprints are listed and staged for fewer tiles).
  * GR_TUNE_PROJ_SPLIT_CELLS: 3D problems with fewer detector cells over all
  * angles than this (default 4194304; 0 = never) split each tile's atoms over
  * the four warps of a block, which shortens the slowest tile when there are

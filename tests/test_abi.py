@@ -69,7 +69,7 @@ def test_tuning_keys_round_trip_without_gpu():
     lib_mod = importlib.import_module("2018_dictionary_tomography_gb300._lib")
     lib = lib_mod.load()
     # key: (a valid value, an invalid value)
-    cases = {0: (65536, 16), 1: (2, 0), 2: (4, 3), 3: (2, 3), 4: (1 << 20, -1),
+    cases = {0: (65536, 16), 1: (2, 0), 2: (4, 3), 3: (3, 4), 4: (1 << 20, -1),
              6: (4096, -5), 7: (0, -1), 8: (1, 2), 9: (1, 2)}
     for key, (good, bad) in cases.items():
         saved = lib.gr_get_tuning(key)

@@ -285,11 +285,12 @@ def test_wide_row_hessian_walk_matches_oracle(eng, cuda_ready, case):
     assert entry_relerr(Hw.cpu().numpy(), Hd.cpu().numpy()) < 1e-6
 
 
-def test_2d_two_cells_per_lane_tiles_match_oracle(eng, cuda_ready):
-    """2D projection with 64-cell tiles (plan key 3 = 2: two cells per lane)
-    against the oracle, on wide and narrow footprints, and against the
-    32-cell tiles (the atoms a cell sums are the same; their grouping into
-    passes differs, so the sums agree to FP32 rounding)."""
+@pytest.mark.parametrize("form", [2, 3])
+def test_2d_two_cells_per_lane_tiles_match_oracle(eng, cuda_ready, form):
+    """2D projection with 64- or 128-cell tiles (plan key 3 = 2 or 3: two or
+    four cells per lane) against the oracle, on wide and narrow footprints,
+    and against the 32-cell tiles (the atoms a cell sums are the same; their
+    grouping into passes differs, so the sums agree to FP32 rounding)."""
     lib = __import__("importlib").import_module("2018_dictionary_tomography_gb300._lib")
     g = make_geometry("2d", 40, 300)
     for rdiag in ((0.8, 2.0), (6.0, 12.0)):
@@ -299,7 +300,7 @@ def test_2d_two_cells_per_lane_tiles_match_oracle(eng, cuda_ready):
         data = data.astype(np.float32).astype(np.float64)
         atoms, geom = engine_atoms(I, x, r), engine_geometry(g)
         d = torch.from_numpy(data).float().cuda()
-        plan = eng.Plan(lib.GR_OP_PROJECT, atoms, geom).set(3, 2)
+        plan = eng.Plan(lib.GR_OP_PROJECT, atoms, geom).set(3, form)
         fw2 = eng.fit_forward(atoms, geom, d, "l2", 0.0, want_R=True, plan=plan)
         fw1 = eng.fit_forward(atoms, geom, d, "l2", 0.0, want_R=True)
         Ro = go.radproj(I, x, r, g)
