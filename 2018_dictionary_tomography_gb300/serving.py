@@ -653,6 +653,31 @@ class _BatchSlot:
 _warmed = set()
 
 
+def _work_size(req):
+    return req.size_hint[0] * req.size_hint[1]
+
+
+def promote_when_idle(pending, now, n_active, n_streams):
+    """Admission order under ``largest_first="when_idle"``: while fewer than
+    half the streams hold a fit (a server starting on a full queue), the
+    largest request that has arrived moves to the head of ``pending`` (a
+    deque in arrival order; ties keep the earlier one), so the device gets
+    long work while the host sets up the next requests.  Otherwise the order
+    is left alone.  Returns the promoted request or None."""
+    if n_active >= n_streams // 2:
+        return None
+    best = None
+    for i, r in enumerate(pending):
+        if r.arrival <= now and (best is None or _work_size(r) > _work_size(best[1])):
+            best = (i, r)
+    if best is None:
+        return None
+    if best[0] > 0:
+        del pending[best[0]]
+        pending.appendleft(best[1])
+    return best[1]
+
+
 def _warm_engine(device):
     """Run every kernel family once eagerly on tiny 2D and 3D problems, so
     that the library's one-time per-device set-up happens outside any stream
@@ -796,18 +821,8 @@ class GaussFitServer:
                     arrived = mixed
                 self.pending = collections.deque(arrived + later)
         while self.pending and len(self.active) < self.max_slots:
-            if self.largest_first == "when_idle" and len(self.active) < len(self.streams) // 2:
-                # few fits in flight (a server starting on a full queue): the
-                # largest arrived request first, so the device gets long work
-                # while the host sets up the next ones
-                best = None
-                for i, r in enumerate(self.pending):
-                    if r.arrival <= now and (best is None or r.size_hint[0] * r.size_hint[1] >
-                                             best[1].size_hint[0] * best[1].size_hint[1]):
-                        best = (i, r)
-                if best is not None and best[0] > 0:
-                    del self.pending[best[0]]
-                    self.pending.appendleft(best[1])
+            if self.largest_first == "when_idle":
+                promote_when_idle(self.pending, now, len(self.active), len(self.streams))
             req = self.pending[0]
             if req.arrival > now:
                 break

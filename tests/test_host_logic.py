@@ -189,3 +189,29 @@ def test_angle_range_views_the_parent_geometry():
     assert np.array_equal(sub.frames.numpy(), g.frames.numpy()[3:9])
     with pytest.raises(ValueError):
         g.angle_range(5, 13)
+
+
+def test_when_idle_admission_promotes_the_largest_arrived_request():
+    """Under-loaded (fewer fits in flight than half the streams): the largest
+    arrived request goes first; loaded: arrival order is kept; requests that
+    have not arrived are never promoted."""
+    import collections
+    import types
+    serving = importlib.import_module(PKG + ".serving")
+    R = lambda rid, arr, n, cells: types.SimpleNamespace(id=rid, arrival=arr,
+                                                         size_hint=(n, cells))
+    reqs = [R(0, 0.0, 16, 100), R(1, 0.0, 900, 5000), R(2, 0.1, 4000, 9000),
+            R(3, 0.0, 900, 5000), R(4, 0.0, 30, 40)]
+    pend = collections.deque(reqs)
+    got = serving.promote_when_idle(pend, now=0.05, n_active=3, n_streams=31)
+    # request 2 has not arrived; 1 and 3 tie, the earlier wins
+    assert got.id == 1 and [r.id for r in pend] == [1, 0, 2, 3, 4]
+    pend.popleft()
+    assert serving.promote_when_idle(pend, now=0.2, n_active=0, n_streams=31).id == 2
+    assert [r.id for r in pend] == [2, 0, 3, 4]
+    # loaded: nothing moves
+    assert serving.promote_when_idle(pend, now=0.2, n_active=15, n_streams=31) is None
+    assert [r.id for r in pend] == [2, 0, 3, 4]
+    # nothing arrived yet
+    late = collections.deque([R(7, 1.0, 50, 50)])
+    assert serving.promote_when_idle(late, now=0.0, n_active=0, n_streams=31) is None
