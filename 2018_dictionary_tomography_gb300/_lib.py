@@ -229,11 +229,12 @@ def load(build_if_missing=True):
         lib.gr_fit_items.argtypes = [vp, P(GrGeometry), P(ctypes.c_size_t)]
         lib.gr_fit_empty_loss.restype = ctypes.c_int
         lib.gr_fit_empty_loss.argtypes = [vp, P(GrAtoms), P(GrGeometry), ctypes.c_int, vp,
-                                          ctypes.c_float, vp, vp, ctypes.c_size_t, vp]
+                                          ctypes.c_float, vp, ctypes.c_size_t, vp,
+                                          ctypes.c_size_t, vp]
         lib.gr_fit_forward_skip.restype = ctypes.c_int
         lib.gr_fit_forward_skip.argtypes = [vp, P(GrAtoms), P(GrGeometry), ctypes.c_int, vp,
-                                            ctypes.c_float, vp, vp, vp, vp, vp, ctypes.c_size_t,
-                                            vp]
+                                            ctypes.c_float, vp, vp, vp, vp, ctypes.c_size_t,
+                                            vp, ctypes.c_size_t, vp]
         _lib = lib
         return lib
 

@@ -477,9 +477,17 @@ int gr_fit_items(const gr_plan *plan, const gr_geometry *geom, size_t *n_items) 
   return GR_OK;
 }
 
+// the record of empty items must have one entry per item of the forward's
+// tiling: checked on the host, before any launch
+static bool empty_record_fits(const gr_plan *plan, const gr_geometry *geom, size_t n_empty) {
+  size_t n = 0;
+  return gr_fit_items(plan, geom, &n) == GR_OK && n > 0 && n == n_empty;
+}
+
 int gr_fit_empty_loss(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
                       int fit, const float *data, float background, double *empty_loss,
-                      void *workspace, size_t workspace_bytes, void *stream) {
+                      size_t n_empty, void *workspace, size_t workspace_bytes, void *stream) {
+  if (!empty_record_fits(plan, geom, n_empty)) return GR_ERR_ARG;
   return fit_forward_impl(atoms, geom, fit, data, background, nullptr, nullptr, nullptr, nullptr,
                           workspace, workspace_bytes, stream, 0, plan ? plan->t : g_tuning,
                           kEmptyRecord, empty_loss);
@@ -487,8 +495,9 @@ int gr_fit_empty_loss(const gr_plan *plan, const gr_atoms *atoms, const gr_geome
 
 int gr_fit_forward_skip(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
                         int fit, const float *data, float background, float *alpha,
-                        float *beta, double *loss, const double *empty_loss, void *workspace,
-                        size_t workspace_bytes, void *stream) {
+                        float *beta, double *loss, const double *empty_loss, size_t n_empty,
+                        void *workspace, size_t workspace_bytes, void *stream) {
+  if (!empty_record_fits(plan, geom, n_empty)) return GR_ERR_ARG;
   return fit_forward_impl(atoms, geom, fit, data, background, nullptr, alpha, beta, loss,
                           workspace, workspace_bytes, stream, 0, plan ? plan->t : g_tuning,
                           kEmptySkip, const_cast<double *>(empty_loss));

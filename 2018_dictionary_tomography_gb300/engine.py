@@ -419,7 +419,8 @@ def fit_empty_loss_into(atoms, geom, data, fit, background, empty_loss, ws, plan
     st = _lib.load().gr_fit_empty_loss(
         plan.handle if plan is not None else None, ctypes.byref(atoms.struct),
         ctypes.byref(geom.struct), code, data.data_ptr(), float(background),
-        empty_loss.data_ptr(), ws.data_ptr(), ws.numel(), _stream_handle(geom.device))
+        empty_loss.data_ptr(), empty_loss.numel(), ws.data_ptr(), ws.numel(),
+        _stream_handle(geom.device))
     _lib.check(st, "gr_fit_empty_loss")
 
 
@@ -437,8 +438,8 @@ def fit_forward_into(atoms, geom, data, fit, background, R, alpha, beta, loss, w
         st = _lib.load().gr_fit_forward_skip(
             plan.handle if plan is not None else None, ctypes.byref(atoms.struct),
             ctypes.byref(geom.struct), code, data.data_ptr(), float(background), _ptr(alpha),
-            _ptr(beta), _ptr(loss), empty_loss.data_ptr(), ws.data_ptr(), ws.numel(),
-            _stream_handle(geom.device))
+            _ptr(beta), _ptr(loss), empty_loss.data_ptr(), empty_loss.numel(), ws.data_ptr(),
+            ws.numel(), _stream_handle(geom.device))
         _lib.check(st, "gr_fit_forward_skip")
         return
     fn = _fn("fit_forward", psf, plan)

@@ -371,7 +371,7 @@ int gr_atom_derivs_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geo
  *   gr_fit_items: the forward's items under the plan's tiling (plan NULL:
  *     the process-wide schedule); 0 for 2D geometries, which do not skip.
  *   gr_fit_empty_loss: each item's loss with no atom in it (R = 0: the data
- *     term alone, L2 or KL) into empty_loss[gr_fit_items], computed under the
+ *     term alone, L2 or KL) into empty_loss[n_empty], computed under the
  *     schedule a forward of these atoms takes (only n_atoms is read), so it
  *     equals bitwise what that forward computes for an item no atom meets.
  *     Once per data sinogram.
@@ -379,16 +379,18 @@ int gr_atom_derivs_plan(const gr_plan *plan, const gr_atoms *atoms, const gr_geo
  *     atom meets takes its loss from empty_loss and keeps whatever its fields
  *     held: the loss is bitwise that of gr_fit_forward_plan, and so are the
  *     fields in every item an atom meets.
- * GR_ERR_ARG for a 2D geometry, a missing pointer or fit GR_FIT_NONE.
+ * n_empty must equal gr_fit_items under the same plan (a record made under
+ * another tiling does not fit).  GR_ERR_ARG for a 2D geometry, a missing
+ * pointer, fit GR_FIT_NONE or another n_empty.
  */
 int gr_fit_items(const gr_plan *plan, const gr_geometry *geom, size_t *n_items);
 int gr_fit_empty_loss(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
                       int fit, const float *data, float background, double *empty_loss,
-                      void *workspace, size_t workspace_bytes, void *stream);
+                      size_t n_empty, void *workspace, size_t workspace_bytes, void *stream);
 int gr_fit_forward_skip(const gr_plan *plan, const gr_atoms *atoms, const gr_geometry *geom,
                         int fit, const float *data, float background, float *alpha,
-                        float *beta, double *loss, const double *empty_loss, void *workspace,
-                        size_t workspace_bytes, void *stream);
+                        float *beta, double *loss, const double *empty_loss, size_t n_empty,
+                        void *workspace, size_t workspace_bytes, void *stream);
 
 /*
  * Per-angle detector moments of a sinogram, for the moment-matching initial

@@ -162,21 +162,28 @@ def test_skip_forward_items_and_argument_checks_without_gpu():
     assert lib.gr_fit_items(h, ctypes.byref(g), ctypes.byref(n)) == 0
     assert n.value == 50 * 3 * 3                 # 32 x 32 tiles
     assert lib.gr_fit_items(h, ctypes.byref(g), None) == -1
+    items = n.value
     # no data: refused before any launch
     assert lib.gr_fit_empty_loss(h, ctypes.byref(at), ctypes.byref(g), 1, None, 0.0, 16,
-                                 None, 0, None) == -1
+                                 items, None, 0, None) == -1
     assert lib.gr_fit_forward_skip(h, ctypes.byref(at), ctypes.byref(g), 1, None, 0.0, 16,
-                                   None, 16, 16, None, 0, None) == -1
+                                   None, 16, 16, items, None, 0, None) == -1
     # no record: refused
     assert lib.gr_fit_forward_skip(h, ctypes.byref(at), ctypes.byref(g), 1, 16, 0.0, 16,
-                                   None, 16, None, None, 0, None) == -1
+                                   None, 16, None, items, None, 0, None) == -1
+    # a record of another tiling (the default's 750 items against the plan's
+    # 450): refused, with data, record and workspace present
+    assert lib.gr_fit_empty_loss(h, ctypes.byref(at), ctypes.byref(g), 1, 16, 0.0, 16,
+                                 50 * 5 * 3, 16, 1 << 30, None) == -1
+    assert lib.gr_fit_forward_skip(h, ctypes.byref(at), ctypes.byref(g), 1, 16, 0.0, 16,
+                                   None, 16, 16, 50 * 5 * 3, 16, 1 << 30, None) == -1
     # 2D: no items to skip, and both calls refuse
     g.kdet = 1
     assert lib.gr_fit_items(None, ctypes.byref(g), ctypes.byref(n)) == 0 and n.value == 0
     assert lib.gr_fit_empty_loss(None, ctypes.byref(at), ctypes.byref(g), 1, 16, 0.0, 16,
-                                 None, 0, None) == -1
+                                 0, None, 0, None) == -1
     assert lib.gr_fit_forward_skip(None, ctypes.byref(at), ctypes.byref(g), 1, 16, 0.0, 16,
-                                   None, 16, 16, None, 0, None) == -1
+                                   None, 16, 16, 0, None, 0, None) == -1
     assert lib.gr_plan_destroy(h) == 0
 
 
